@@ -1,0 +1,738 @@
+"""CPU oracle for the SolverFEM per-substep hot path -- TEST INFRASTRUCTURE ONLY.
+
+This module is the checker, never the product: only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import it.
+It restates, in vectorised float64 NumPy, the reference's algorithm for the path:
+Stable Neo-Hookean Tet4/Hex8 forces and approximate PSD tangent, the triplet
+layout and BSR assembly of ``A = M + h^2 K~ + h C_s``, the elastic predictor,
+the fixed-node projection ``PAP + I - P``, RHS normalisation, block-Jacobi and
+the preconditioned CG with warm start.  Every function cites the reference file
+and lines it follows (paths inside ``src/newton_solver_fem/_src/solvers/fem/``
+unless stated).
+
+Parity pinning.  The reference needs Warp 1.17 and Newton 1.7, which cannot be
+installed here, so it cannot be run.  This oracle is instead pinned against the
+reference's own known-answer tests (Hex8 2x3x4 box quadrature and free fall,
+free fall across mass scales, the h/2 force gradient, grid volume and mass,
+rigid-motion invariance, force = -grad(energy), dense-solve agreement, block
+inverse scale invariance) on the reference's ASCII fixture meshes; see
+``tests/test_oracle_pins.py``.  The CG iterate sequence of Warp's ``cg`` is not
+pinned by the reference (only residual/tolerance semantics are), and the bits
+of Warp's ``svd3`` are not pinned (only clamp behaviour), so those parts are
+restated from the published methods.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+
+PARTICLE_FLAG_ACTIVE = 1
+
+# ---------------------------------------------------------------------------
+# Hex8 reference-element data (kernels.py:1356-1419; builder.py:101-104)
+# ---------------------------------------------------------------------------
+
+HEX_SIGNS = np.array(
+    [[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]],
+    dtype=np.float64,
+)
+HEX_GP = 0.5773502691896258  # kernels.py:1357
+
+
+def hex_dN_dxi() -> np.ndarray:
+    """dN_a/d(xi,eta,zeta) at Gauss point g, [8 g, 8 a, 3] (kernels.py:1362-1419)."""
+    gp = HEX_SIGNS * HEX_GP  # g-th point has the signs of corner g (kernels.py:1362-1383)
+    out = np.empty((8, 8, 3))
+    for g in range(8):
+        xi, eta, zeta = gp[g]
+        for a in range(8):
+            xa, ya, za = HEX_SIGNS[a]
+            out[g, a] = (
+                xa * (1 + ya * eta) * (1 + za * zeta) * 0.125,
+                (1 + xa * xi) * ya * (1 + za * zeta) * 0.125,
+                (1 + xa * xi) * (1 + ya * eta) * za * 0.125,
+            )
+    return out
+
+
+def hex_builder_data(rest: np.ndarray, hexes: np.ndarray):
+    """``inv_J0`` [H,8,3,3] and ``|det J0|`` [H,8] in float64 (builder.py:95-135)."""
+    dxi = hex_dN_dxi()
+    J = np.einsum("hai,gaj->hgij", rest[hexes].astype(np.float64), dxi)
+    det = np.linalg.det(J)
+    if np.any(det <= 1.0e-12):
+        raise ValueError("Degenerate or inverted Hex8")
+    return np.linalg.inv(J), np.abs(det)
+
+
+def hex_shape_gradients(inv_J0: np.ndarray) -> np.ndarray:
+    """Reference-config gradients ``grad_X N_a = inv_J0^T dN/dxi``, [H,8 g,8 a,3] (kernels.py:1540-1548)."""
+    return np.einsum("hgji,gaj->hgai", inv_J0, hex_dN_dxi())
+
+
+# ---------------------------------------------------------------------------
+# Principal-stretch clamp (kernels.py:421-444)
+# ---------------------------------------------------------------------------
+
+
+def signed_svd(F: np.ndarray):
+    """SVD with U, V proper rotations and the sign of det(F) on the last singular value.
+
+    This is the rotation-variant convention of McAdams et al. 2011 ("Computing
+    the singular value decomposition of 3x3 matrices with minimal branching and
+    elementary floating point operations"), which the reference's ``wp.svd3`` call
+    follows: an inverted element shows up as a negative smallest stretch.
+    """
+    U, S, Vt = np.linalg.svd(F)
+    V = np.swapaxes(Vt, -1, -2).copy()
+    U = U.copy()
+    S = S.copy()
+    fu = np.linalg.det(U) < 0
+    U[fu, :, 2] *= -1.0
+    S[fu, 2] *= -1.0
+    fv = np.linalg.det(V) < 0
+    V[fv, :, 2] *= -1.0
+    S[fv, 2] *= -1.0
+    return U, S, V
+
+
+def clamp_stretch(F: np.ndarray, lo: float, hi: float) -> np.ndarray:
+    """``U diag(clamp(S, lo, hi)) V^T``; identity map when a bound is negative (kernels.py:421-444)."""
+    if lo < 0.0 or hi < 0.0 or len(F) == 0:
+        return F
+    U, S, V = signed_svd(F)
+    S = np.maximum(np.minimum(S, hi), lo)
+    return np.einsum("eij,ej,ekj->eik", U, S, V)
+
+
+def clamp_active(F: np.ndarray, lo: float, hi: float) -> np.ndarray:
+    """Elements whose signed stretches leave [lo, hi] (the clamp changes F)."""
+    if lo < 0.0 or hi < 0.0 or len(F) == 0:
+        return np.zeros(len(F), bool)
+    _, S, _ = signed_svd(F)
+    return np.any((S < lo) | (S > hi), axis=1)
+
+
+# ---------------------------------------------------------------------------
+# Force terms
+# ---------------------------------------------------------------------------
+
+
+def _cols(a, b, c):
+    return np.stack([a, b, c], axis=-1)
+
+
+def tet_forces(x, v, tets, poses, mats, lo, hi, activation=None, mu_scale=None):
+    """Stable Neo-Hookean Tet4 force + Rayleigh damping (kernels.py:511-632).
+
+    ``activation`` adds Newton's volumetric contraction term (kernels.py:484-508).
+    ``mu_scale`` multiplies the shear modulus per element (the differentiable
+    beam's per-element activation scale; not in the reference).
+    """
+    f = np.zeros_like(x, dtype=np.float64)
+    if len(tets) == 0:
+        return f
+    mu, lam, kd = (mats[:, c].astype(np.float64) for c in range(3))
+    if mu_scale is not None:
+        mu = mu * mu_scale
+    live = ~((mu == 0.0) & (lam == 0.0) & (kd == 0.0))  # kernels.py:545-548
+    t = tets[live]
+    mu, lam, kd = mu[live], lam[live], kd[live]
+    Dm = poses[live].astype(np.float64)
+    xs = x[t].astype(np.float64)
+    vs = v[t].astype(np.float64)
+    x10, x20, x30 = xs[:, 1] - xs[:, 0], xs[:, 2] - xs[:, 0], xs[:, 3] - xs[:, 0]
+    v10, v20, v30 = vs[:, 1] - vs[:, 0], vs[:, 2] - vs[:, 0], vs[:, 3] - vs[:, 0]
+    inv_rest_volume = np.linalg.det(Dm) * 6.0
+    rest_volume = 1.0 / inv_rest_volume
+    with np.errstate(divide="ignore", invalid="ignore"):
+        alpha = 1.0 + mu / lam - mu / (4.0 * lam)  # kernels.py:575
+    k_mu, k_lam, k_damp = mu * rest_volume, lam * rest_volume, kd * rest_volume
+    F = clamp_stretch(_cols(x10, x20, x30) @ Dm, lo, hi)
+    dFdt = _cols(v10, v20, v30) @ Dm
+    Ic = np.sum(F * F, axis=(1, 2))
+    P = F * (k_mu * (1.0 - 1.0 / (Ic + 1.0)))[:, None, None] + dFdt * k_damp[:, None, None]
+    H = P @ np.swapaxes(Dm, 1, 2)
+    f1, f2, f3 = H[:, :, 0], H[:, :, 1], H[:, :, 2]
+    J = np.maximum(np.linalg.det(F), 0.01)  # kernels.py:608-610
+    s = (inv_rest_volume / 6.0)[:, None]
+    d1, d2, d3 = np.cross(x20, x30) * s, np.cross(x30, x10) * s, np.cross(x10, x20) * s
+    f_volume = (J - alpha) * k_lam
+    f_damp = (np.sum(d1 * v10, 1) + np.sum(d2 * v20, 1) + np.sum(d3 * v30, 1)) * k_damp
+    ft = (f_volume + f_damp)[:, None]
+    f1, f2, f3 = f1 + d1 * ft, f2 + d2 * ft, f3 + d3 * ft
+    f0 = -(f1 + f2 + f3)
+    for a, fa in enumerate((f0, f1, f2, f3)):
+        np.subtract.at(f, t[:, a], fa)
+    if activation is not None:
+        f += tet_activation_forces(x, tets, mats, activation)
+    return f
+
+
+def tet_activation_forces(x, tets, mats, activation):
+    """Newton's additive volumetric activation force lambda*a/6 * face crosses (kernels.py:484-508)."""
+    f = np.zeros_like(x, dtype=np.float64)
+    xs = x[tets].astype(np.float64)
+    scale = (mats[:, 1].astype(np.float64) * np.asarray(activation, np.float64) / 6.0)[:, None]
+    xa, xb, xc, xd = xs[:, 0], xs[:, 1], xs[:, 2], xs[:, 3]
+    fb = scale * np.cross(xc - xa, xd - xa)
+    fc = scale * np.cross(xd - xa, xb - xa)
+    fd = scale * np.cross(xb - xa, xc - xa)
+    np.add.at(f, tets[:, 0], fb + fc + fd)
+    np.subtract.at(f, tets[:, 1], fb)
+    np.subtract.at(f, tets[:, 2], fc)
+    np.subtract.at(f, tets[:, 3], fd)
+    return f
+
+
+def _hex_F(xe, dN):
+    # F = sum_a x_a (outer) grad_X N_a; absolute positions (kernels.py:1551-1560)
+    return np.einsum("hai,hgaj->hgij", xe, dN)
+
+
+def hex_forces(x, v, hexes, inv_J0, det_J0_w, mats, lo, hi):
+    """Q1 Hex8 Stable Neo-Hookean force over the 2x2x2 Gauss rule (kernels.py:1481-1601)."""
+    f = np.zeros_like(x, dtype=np.float64)
+    if len(hexes) == 0:
+        return f
+    mu, lam, kd = (mats[:, c].astype(np.float64) for c in range(3))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        alpha = 1.0 + mu / lam - mu / (4.0 * lam)  # kernels.py:1503 (no zero-lambda guard)
+    dN = hex_shape_gradients(inv_J0.astype(np.float64))
+    xe, ve = x[hexes].astype(np.float64), v[hexes].astype(np.float64)
+    H = len(hexes)
+    F = clamp_stretch(_hex_F(xe, dN).reshape(-1, 3, 3), lo, hi).reshape(H, 8, 3, 3)
+    dFdt = _hex_F(ve, dN)
+    Ic = np.sum(F * F, axis=(2, 3))
+    P = F * (mu[:, None] * (1.0 - 1.0 / (Ic + 1.0)))[..., None, None] + dFdt * kd[:, None, None, None]
+    J = np.maximum(np.linalg.det(F), 0.01)
+    c0, c1, c2 = F[..., :, 0], F[..., :, 1], F[..., :, 2]
+    cof = _cols(np.cross(c1, c2), np.cross(c2, c0), np.cross(c0, c1))
+    P = P + cof * (lam[:, None] * (J - alpha[:, None]))[..., None, None]
+    w = det_J0_w.astype(np.float64)
+    fa = np.einsum("hg,hgij,hgaj->hai", w, P, dN)
+    np.subtract.at(f, hexes.ravel(), fa.reshape(-1, 3))
+    return f
+
+
+def spring_forces(x, v, springs, rest, ke, kd):
+    """Linear spring + damping (kernels.py:176-218)."""
+    f = np.zeros_like(x, dtype=np.float64)
+    if len(springs) == 0:
+        return f
+    i, j = springs[:, 0], springs[:, 1]
+    ok = (i >= 0) & (j >= 0)
+    i, j = i[ok], j[ok]
+    xij = x[i].astype(np.float64) - x[j]
+    vij = v[i].astype(np.float64) - v[j]
+    L = np.linalg.norm(xij, axis=1)
+    ok = L >= 1.0e-6
+    i, j, xij, vij, L = i[ok], j[ok], xij[ok], vij[ok], L[ok]
+    d = xij / L[:, None]
+    c = L - rest[ok]
+    fs = d * (ke[ok] * c + kd[ok] * np.sum(d * vij, 1))[:, None]
+    np.subtract.at(f, i, fs)
+    np.add.at(f, j, fs)
+    return f
+
+
+def ground_forces(x, v, radius, inv_mass, flags, ke, kd, kf, mu, plane, gravity):
+    """Analytic ground penalty + weight-capped Coulomb friction (kernels.py:1132-1195)."""
+    x = x.astype(np.float64)
+    v = v.astype(np.float64)
+    n = np.asarray(plane[:3], np.float64)
+    c = np.minimum(x @ n + plane[3] - radius, 0.0)
+    vn = v @ n
+    jn = c * ke
+    jd = np.minimum(vn, 0.0) * kd
+    fn = jn + jd
+    vt = v - n[None] * vn[:, None]
+    vs = np.linalg.norm(vt, axis=1)
+    vt = np.where(vs[:, None] > 0, vt / np.where(vs > 0, vs, 1.0)[:, None], vt)
+    gmag = float(np.linalg.norm(gravity))
+    m = np.where(inv_mass > 0.0, 1.0 / np.maximum(inv_mass, 1e-9), 0.0)
+    fn_eff = np.minimum(np.abs(fn), m * gmag)
+    ft = np.minimum(vs * kf, mu * fn_eff)
+    f = -n[None] * fn[:, None] - vt * ft[:, None]
+    live = ((flags & PARTICLE_FLAG_ACTIVE) != 0) & (c < 0.0)
+    return np.where(live[:, None], f, 0.0)
+
+
+def gravity_forces(mass, flags, gravity):
+    """f = m g for active particles (kernels.py:1273-1286)."""
+    f = np.outer(mass.astype(np.float64), np.asarray(gravity, np.float64))
+    return np.where(((flags & PARTICLE_FLAG_ACTIVE) != 0)[:, None], f, 0.0)
+
+
+def damping_forces(v, mass, flags, alpha):
+    """f = -alpha m v (kernels.py:1289-1307)."""
+    f = -alpha * mass[:, None].astype(np.float64) * v
+    return np.where(((flags & PARTICLE_FLAG_ACTIVE) != 0)[:, None], f, 0.0)
+
+
+# ---------------------------------------------------------------------------
+# Tangent blocks and triplets
+# ---------------------------------------------------------------------------
+
+
+def tet_tangent(x, tets, poses, mats, lo, hi, dt, mu_scale=None):
+    """16 blocks ``h^2 (K_dev + K_vol)`` per tet, rows/cols -1 for empty material (kernels.py:635-850)."""
+    T = len(tets)
+    rows = np.repeat(tets, 4, axis=1).astype(np.int64)  # row of block (a, b) = node a
+    cols = np.tile(tets, (1, 4)).astype(np.int64)  # col = node b
+    vals = np.zeros((T, 16, 3, 3))
+    if T == 0:
+        return rows.reshape(-1), cols.reshape(-1), vals.reshape(-1, 3, 3)
+    mu, lam = mats[:, 0].astype(np.float64), mats[:, 1].astype(np.float64)
+    if mu_scale is not None:
+        mu = mu * mu_scale
+    empty = (mu == 0.0) & (lam == 0.0) & (mats[:, 2] == 0.0)  # kernels.py:690-700
+    Dm = poses.astype(np.float64)
+    inv_rest_volume = np.linalg.det(Dm) * 6.0
+    degenerate = inv_rest_volume <= 0.0  # kernels.py:716-727: zero blocks, valid rows
+    ok = ~empty & ~degenerate
+    xs = x[tets].astype(np.float64)
+    x10, x20, x30 = xs[:, 1] - xs[:, 0], xs[:, 2] - xs[:, 0], xs[:, 3] - xs[:, 0]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rest_volume = np.where(ok, 1.0 / np.where(ok, inv_rest_volume, 1.0), 0.0)
+    k_mu, k_lam = mu * rest_volume, lam * rest_volume
+    F = _cols(x10, x20, x30) @ Dm
+    F[ok] = clamp_stretch(F[ok], lo, hi)
+    Ic1 = np.maximum(np.sum(F * F, axis=(1, 2)) + 1.0, 1e-6)
+    s = 1.0 - 1.0 / Ic1
+    coef = k_mu * 2.0 / (Ic1 * Ic1)
+    sv = (inv_rest_volume / 6.0)[:, None]
+    d1, d2, d3 = np.cross(x20, x30) * sv, np.cross(x30, x10) * sv, np.cross(x10, x20) * sv
+    dJ = np.stack([-(d1 + d2 + d3), d1, d2, d3], axis=1)  # [T,4,3]
+    dm = np.swapaxes(Dm, 1, 2)  # columns = rows of Dm
+    dm_rows = np.stack([-(Dm[:, 0] + Dm[:, 1] + Dm[:, 2]), Dm[:, 0], Dm[:, 1], Dm[:, 2]], axis=1)
+    del dm
+    Fdm = np.einsum("tij,taj->tai", F, dm_rows)
+    dots = np.einsum("tai,tbi->tab", dm_rows, dm_rows)
+    eye = np.eye(3)
+    K = (
+        (k_mu * s)[:, None, None, None, None] * dots[..., None, None] * eye
+        + coef[:, None, None, None, None] * np.einsum("tai,tbj->tabij", Fdm, Fdm)
+        + k_lam[:, None, None, None, None] * np.einsum("tai,tbj->tabij", dJ, dJ)
+    ) * (dt * dt)
+    K[~ok] = 0.0
+    vals[:] = K.reshape(T, 16, 3, 3)
+    rows[empty] = -1
+    cols[empty] = -1
+    return rows.reshape(-1), cols.reshape(-1), vals.reshape(-1, 3, 3)
+
+
+def hex_tangent(x, hexes, inv_J0, det_J0_w, mats, lo, hi, dt):
+    """64 PSD blocks per hex summed over the Gauss rule (kernels.py:1609-1747)."""
+    Hn = len(hexes)
+    rows = np.repeat(hexes, 8, axis=1).astype(np.int64)
+    cols = np.tile(hexes, (1, 8)).astype(np.int64)
+    if Hn == 0:
+        return rows.reshape(-1), cols.reshape(-1), np.zeros((0, 3, 3))
+    mu, lam = mats[:, 0].astype(np.float64), mats[:, 1].astype(np.float64)
+    dN = hex_shape_gradients(inv_J0.astype(np.float64))
+    xe = x[hexes].astype(np.float64)
+    F = clamp_stretch(_hex_F(xe, dN).reshape(-1, 3, 3), lo, hi).reshape(Hn, 8, 3, 3)
+    Ic1 = np.maximum(np.sum(F * F, axis=(2, 3)) + 1.0, 1e-6)
+    s = 1.0 - 1.0 / Ic1
+    coef = mu[:, None] * 2.0 / (Ic1 * Ic1)
+    c0, c1, c2 = F[..., :, 0], F[..., :, 1], F[..., :, 2]
+    cof = _cols(np.cross(c1, c2), np.cross(c2, c0), np.cross(c0, c1))
+    Fd = np.einsum("hgij,hgaj->hgai", F, dN)
+    dJ = np.einsum("hgij,hgaj->hgai", cof, dN)
+    dots = np.einsum("hgai,hgbi->hgab", dN, dN)
+    w = det_J0_w.astype(np.float64)
+    K = (
+        np.einsum("hg,hgab,ij->habij", w * mu[:, None] * s, dots, np.eye(3))
+        + np.einsum("hg,hgai,hgbj->habij", w * coef, Fd, Fd)
+        + np.einsum("hg,hgai,hgbj->habij", w * lam[:, None], dJ, dJ)
+    ) * (dt * dt)
+    return rows.reshape(-1), cols.reshape(-1), K.reshape(-1, 3, 3)
+
+
+def constant_triplets(mass, springs, ke, kd, dt):
+    """Mass + spring diagonal and spring off-diagonal triplets (solver.py:1015-1060; kernels.py:141-153, 294-366)."""
+    P = len(mass)
+    diag = mass.astype(np.float64).copy()
+    S = len(springs)
+    if S:
+        c = dt * kd.astype(np.float64) + dt * dt * ke.astype(np.float64)
+        for col in (0, 1):
+            idx = springs[:, col]
+            ok = idx >= 0
+            np.add.at(diag, idx[ok], c[ok])
+    rows = [np.arange(P)]
+    cols = [np.arange(P)]
+    vals = [diag[:, None, None] * np.eye(3)]
+    if S:
+        off = -(dt * kd.astype(np.float64) + dt * dt * ke.astype(np.float64))
+        r = np.stack([springs[:, 0], springs[:, 1]], axis=1).reshape(-1)
+        cc = np.stack([springs[:, 1], springs[:, 0]], axis=1).reshape(-1)
+        rows.append(r)
+        cols.append(cc)
+        vals.append(np.repeat(off, 2)[:, None, None] * np.eye(3))
+    return np.concatenate(rows), np.concatenate(cols), np.concatenate(vals)
+
+
+def assemble_bsr(rows, cols, vals, n):
+    """COO -> BSR with sorted columns, duplicates summed, negative indices dropped.
+
+    Restates the behaviour the reference relies on from Warp's
+    ``bsr_set_from_triplets(prune_numerical_zeros=False)`` (solver.py:677-683;
+    the pattern is pinned by tests/test_solver.py:542-545).
+    """
+    ok = (rows >= 0) & (cols >= 0)
+    rows, cols, vals = rows[ok], cols[ok], vals[ok]
+    key = rows.astype(np.int64) * n + cols
+    order = np.argsort(key, kind="stable")
+    key = key[order]
+    uniq, start = np.unique(key, return_index=True)
+    summed = np.add.reduceat(vals[order], start, axis=0) if len(key) else np.zeros((0, 3, 3))
+    r = (uniq // n).astype(np.int64)
+    c = (uniq % n).astype(np.int32)
+    offsets = np.zeros(n + 1, np.int64)
+    np.add.at(offsets, r + 1, 1)
+    offsets = np.cumsum(offsets)
+    return offsets, c, summed
+
+
+def bsr_to_scipy(offsets, columns, values, n):
+    return sp.bsr_matrix((values, columns, offsets), shape=(3 * n, 3 * n))
+
+
+def dense(offsets, columns, values, n):
+    out = np.zeros((3 * n, 3 * n))
+    for row in range(n):
+        for k in range(offsets[row], offsets[row + 1]):
+            c = columns[k]
+            out[3 * row : 3 * row + 3, 3 * c : 3 * c + 3] += values[k]
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Preconditioner, predictor, normalisation, CG
+# ---------------------------------------------------------------------------
+
+
+def inverse_diagonal_block(blocks: np.ndarray, dtype=np.float64) -> np.ndarray:
+    """Scale-normalised 3x3 inverse with point-Jacobi fallback (kernels.py:1817-1833)."""
+    blocks = np.asarray(blocks, dtype)
+    out = np.zeros_like(blocks)
+    scale = np.max(np.abs(np.diagonal(blocks, axis1=1, axis2=2)), axis=1)
+    good = np.zeros(len(blocks), bool)
+    pos = scale > 0
+    if np.any(pos):
+        nrm = blocks[pos] / scale[pos, None, None]
+        tr = np.trace(nrm, axis1=1, axis2=2) / dtype(3.0)
+        det = np.linalg.det(nrm)
+        ok = (tr > 0) & (np.abs(det) > dtype(1.0e-9) * tr * tr * tr)
+        idx = np.nonzero(pos)[0][ok]
+        out[idx] = np.linalg.inv(nrm[ok]) / scale[idx, None, None]
+        good[idx] = True
+    bad = ~good
+    if np.any(bad):
+        d = np.diagonal(blocks[bad], axis1=1, axis2=2)
+        rec = np.where(d > 0, 1.0 / np.where(d > 0, d, 1.0), 1.0)
+        out[bad] = rec[:, :, None] * np.eye(3)
+    return out
+
+
+def block_jacobi(offsets, columns, values, n):
+    """Minv[i] = inverse_diagonal_block(A_ii), identity when the row has no diagonal (kernels.py:1836-1849)."""
+    diag = np.tile(np.eye(3), (n, 1, 1))
+    for_row = np.repeat(np.arange(n), np.diff(offsets))
+    hit = columns == for_row
+    diag[for_row[hit]] = values[hit]
+    return inverse_diagonal_block(diag)
+
+
+def point_jacobi(offsets, columns, values, n):
+    """Inverse of the scalar diagonal, 1 where it is zero (Warp ``preconditioner(A, "diag")``)."""
+    out = np.zeros((n, 3, 3))
+    for_row = np.repeat(np.arange(n), np.diff(offsets))
+    hit = columns == for_row
+    d = np.ones((n, 3))
+    d[for_row[hit]] = np.diagonal(values[hit], axis1=1, axis2=2)
+    out[:, [0, 1, 2], [0, 1, 2]] = np.where(d == 0, 1.0, 1.0 / np.where(d == 0, 1.0, d))
+    return out
+
+
+def elastic_predictor(offsets, columns, values, v):
+    """``correction_i = sum_j A_ij (v_j - v_i)`` (implicit_predictor.py:9-23)."""
+    n = len(offsets) - 1
+    for_row = np.repeat(np.arange(n), np.diff(offsets))
+    diff = v[columns].astype(np.float64) - v[for_row]
+    contrib = np.einsum("kij,kj->ki", values, diff)
+    out = np.zeros((n, 3))
+    np.add.at(out, for_row, contrib)
+    return out
+
+
+def spring_damping_restore(springs, kd, dt, v, rhs):
+    """rhs_a += h d (v_a - v_b), rhs_b -= ... (implicit_predictor.py:26-41)."""
+    if len(springs) == 0:
+        return rhs
+    a, b = springs[:, 0], springs[:, 1]
+    ok = (a >= 0) & (b >= 0)
+    corr = dt * kd[ok, None].astype(np.float64) * (v[a[ok]].astype(np.float64) - v[b[ok]])
+    np.add.at(rhs, a[ok], corr)
+    np.subtract.at(rhs, b[ok], corr)
+    return rhs
+
+
+def rhs_scale(maximum: float) -> float:
+    """RHS normalisation factor (kernels.py:1785-1793)."""
+    if 0.0 < maximum < 1.0e-12:
+        return min(1.0 / maximum, 1.0e30)
+    return 1.0
+
+
+def pcg(apply_A, apply_M, b, x, tol, maxiter):
+    """Preconditioned CG with warm start, ``atol = 0`` and a relative stop.
+
+    Restates the semantics the reference relies on from Warp's ``cg`` (solver.py:1219-1252):
+    stop once ``||r||^2 <= tol^2 ||b||^2`` (unpreconditioned residual),
+    at most ``maxiter`` updates, iterate frozen after convergence.
+    Returns (x, iterations, ||r||^2, ||b||^2).
+    """
+    x = x.copy()
+    r = b - apply_A(x)
+    rr = float(np.dot(r.ravel(), r.ravel()))
+    bb = float(np.dot(b.ravel(), b.ravel()))
+    atol_sq = tol * tol * bb
+    z = apply_M(r)
+    rz = float(np.dot(r.ravel(), z.ravel()))
+    p = z.copy()
+    it = 0
+    while it < maxiter and rr > atol_sq:
+        Ap = apply_A(p)
+        pAp = float(np.dot(p.ravel(), Ap.ravel()))
+        alpha = rz / pAp
+        x += alpha * p
+        r -= alpha * Ap
+        rr = float(np.dot(r.ravel(), r.ravel()))
+        z = apply_M(r)
+        rz_new = float(np.dot(r.ravel(), z.ravel()))
+        beta = rz_new / rz
+        rz = rz_new
+        p = z + beta * p
+        it += 1
+    return x, it, rr, bb
+
+
+# ---------------------------------------------------------------------------
+# Whole solver (solver.py:212-415, 942-1002, 1254-1351)
+# ---------------------------------------------------------------------------
+
+
+class OracleFEM:
+    """CPU restatement of ``SolverFEM`` on the hot-path configuration (CG, block Jacobi)."""
+
+    def __init__(
+        self,
+        x,
+        mass,
+        *,
+        tets=None,
+        tet_poses=None,
+        tet_materials=None,
+        hexes=None,
+        hex_inv_J0=None,
+        hex_det_J0_w=None,
+        hex_materials=None,
+        springs=None,
+        spring_rest=None,
+        spring_ke=None,
+        spring_kd=None,
+        radius=None,
+        flags=None,
+        gravity=(0.0, 0.0, -9.81),
+        dt=1.0 / 60.0,
+        min_stretch=0.05,
+        max_stretch=20.0,
+        ground_plane=None,
+        ground_ke=1.0e5,
+        ground_kd=1.0e2,
+        ground_kf=1.0e3,
+        ground_mu=0.5,
+        linear_damping=0.0,
+        fixed=None,
+        maxiter=50,
+        tolerance=1.0e-2,
+        preconditioner="block_diag",
+        mu_scale=None,
+        scene_offsets=None,
+    ):
+        self.rest = np.asarray(x, np.float64).copy()
+        self.n = len(self.rest)
+        self.mass = np.asarray(mass, np.float64)
+        self.inv_mass = np.where(self.mass > 0, 1.0 / np.where(self.mass > 0, self.mass, 1.0), 0.0)
+        z4, z8 = np.zeros((0, 4), np.int32), np.zeros((0, 8), np.int32)
+        self.tets = z4 if tets is None else np.asarray(tets, np.int64)
+        self.tet_poses = np.zeros((0, 3, 3)) if tet_poses is None else np.asarray(tet_poses)
+        self.tet_materials = np.zeros((0, 3)) if tet_materials is None else np.asarray(tet_materials)
+        self.hexes = z8 if hexes is None else np.asarray(hexes, np.int64)
+        self.hex_inv_J0 = hex_inv_J0
+        self.hex_det_J0_w = hex_det_J0_w
+        self.hex_materials = np.zeros((0, 3)) if hex_materials is None else np.asarray(hex_materials)
+        self.springs = np.zeros((0, 2), np.int64) if springs is None else np.asarray(springs, np.int64)
+        S = len(self.springs)
+        self.spring_rest = np.zeros(S) if spring_rest is None else np.asarray(spring_rest, np.float64)
+        self.spring_ke = np.zeros(S) if spring_ke is None else np.asarray(spring_ke, np.float64)
+        self.spring_kd = np.zeros(S) if spring_kd is None else np.asarray(spring_kd, np.float64)
+        self.radius = np.zeros(self.n) if radius is None else np.broadcast_to(np.asarray(radius, np.float64), (self.n,))
+        self.flags = np.ones(self.n, np.int32) if flags is None else np.asarray(flags, np.int32)
+        self.gravity = np.asarray(gravity, np.float64)
+        self.dt = float(dt)
+        self.min_stretch, self.max_stretch = float(min_stretch), float(max_stretch)
+        self.ground_plane = None if ground_plane is None else np.asarray(ground_plane, np.float64)
+        self.ground = (ground_ke, ground_kd, ground_kf, ground_mu)
+        self.linear_damping = float(linear_damping)
+        self.fixed = np.zeros(0, np.int64) if fixed is None else np.unique(np.asarray(fixed, np.int64))
+        self.fixed_mask = np.zeros(self.n, bool)
+        self.fixed_mask[self.fixed] = True
+        self.maxiter, self.tolerance = int(maxiter), float(tolerance)
+        self.preconditioner = preconditioner
+        self.mu_scale = mu_scale
+        self.scene_offsets = (
+            np.array([0, self.n], np.int64) if scene_offsets is None else np.asarray(scene_offsets, np.int64)
+        )
+        self.dv = np.zeros((self.n, 3))
+        self.last_iterations = []
+        self.last_rr_bb = []
+        self._assemble(self.rest, self.dt)
+
+    # -- assembly -----------------------------------------------------------
+    def triplets(self, q, dt):
+        """All triplets in the reference layout [P | 2S | 16T | 64H] (solver.py:312-321)."""
+        parts = [constant_triplets(self.mass, self.springs, self.spring_ke, self.spring_kd, dt)]
+        parts.append(
+            tet_tangent(q, self.tets, self.tet_poses, self.tet_materials, self.min_stretch, self.max_stretch, dt,
+                        self.mu_scale)
+        )
+        if len(self.hexes):
+            parts.append(
+                hex_tangent(q, self.hexes, self.hex_inv_J0, self.hex_det_J0_w, self.hex_materials, self.min_stretch,
+                            self.max_stretch, dt)
+            )
+        rows = np.concatenate([p[0] for p in parts])
+        cols = np.concatenate([p[1] for p in parts])
+        vals = np.concatenate([p[2] for p in parts])
+        return rows, cols, vals
+
+    def _assemble(self, q, dt):
+        self.offsets, self.columns, self.values = assemble_bsr(*self.triplets(q, dt), self.n)
+        if self.preconditioner == "block_diag":
+            self.minv = block_jacobi(self.offsets, self.columns, self.values, self.n)
+        else:
+            self.minv = point_jacobi(self.offsets, self.columns, self.values, self.n)
+        self._A = bsr_to_scipy(self.offsets, self.columns, self.values, self.n).tocsr()
+
+    def refresh_tangent(self, q, dt=None):
+        """Refresh the tangent at q; a dt change clears the warm start (solver.py:769-857)."""
+        dt = self.dt if dt is None else float(dt)
+        q = np.asarray(q, np.float64).copy()
+        q[self.fixed] = self.rest[self.fixed]
+        if dt != self.dt:
+            self.dv[:] = 0.0
+        self._assemble(q, dt)
+        self.dt = dt
+        return q
+
+    def dense(self):
+        return dense(self.offsets, self.columns, self.values, self.n)
+
+    # -- forces --------------------------------------------------------------
+    def forces(self, q, v, *, activation=None, terms=("spring", "tet", "hex", "ground", "gravity", "damping")):
+        """Per-term forces in the reference's accumulation order (solver.py:571-582)."""
+        out = {}
+        if "spring" in terms:
+            out["spring"] = spring_forces(q, v, self.springs, self.spring_rest, self.spring_ke, self.spring_kd)
+        if "tet" in terms:
+            out["tet"] = tet_forces(q, v, self.tets, self.tet_poses, self.tet_materials, self.min_stretch,
+                                    self.max_stretch, activation, self.mu_scale)
+        if "hex" in terms:
+            out["hex"] = hex_forces(q, v, self.hexes, self.hex_inv_J0, self.hex_det_J0_w, self.hex_materials,
+                                    self.min_stretch, self.max_stretch) if len(self.hexes) else np.zeros((self.n, 3))
+        if "ground" in terms:
+            if self.ground_plane is None:
+                out["ground"] = np.zeros((self.n, 3))
+            else:
+                ke, kd, kf, mu = self.ground
+                out["ground"] = ground_forces(q, v, self.radius, self.inv_mass, self.flags, ke, kd, kf, mu,
+                                              self.ground_plane, self.gravity)
+        if "gravity" in terms:
+            out["gravity"] = gravity_forces(self.mass, self.flags, self.gravity)
+        if "damping" in terms:
+            out["damping"] = damping_forces(v, self.mass, self.flags, self.linear_damping) if self.linear_damping > 0 \
+                else np.zeros((self.n, 3))
+        return out
+
+    # -- step ----------------------------------------------------------------
+    def apply_A_projected(self, x):
+        y = (self._A @ x.reshape(-1)).reshape(-1, 3)
+        if len(self.fixed):
+            xf = x.copy()
+            xf[self.fixed] = 0.0
+            y = (self._A @ xf.reshape(-1)).reshape(-1, 3)
+            y[self.fixed] = x[self.fixed]
+        return y
+
+    def apply_M(self, r):
+        return np.einsum("nij,nj->ni", self.minv, r)
+
+    def step(self, q, v, dt, *, external=None, activation=None, fixed_iterations=None):
+        """One substep: returns (q_out, v_out, rhs) (solver.py:942-1002, 1254-1351).
+
+        ``fixed_iterations`` runs exactly that many CG updates (tolerance 0),
+        the reference semantics used for iterate-level parity.
+        """
+        q = np.asarray(q, np.float64).copy()
+        v = np.asarray(v, np.float64).copy()
+        q[self.fixed] = self.rest[self.fixed]  # fixed_particles.py:11-15
+        v[self.fixed] = 0.0
+        terms = self.forces(q, v, activation=activation)
+        f = np.zeros((self.n, 3))
+        for key in ("spring", "tet", "hex", "ground", "gravity", "damping"):
+            f += dt * terms[key]
+        if external is not None:
+            f += dt * np.asarray(external, np.float64)
+        rhs = f - elastic_predictor(self.offsets, self.columns, self.values, v)
+        rhs = spring_damping_restore(self.springs, self.spring_kd, dt, v, rhs)
+        rhs[self.fixed] = 0.0  # fixed_particles.py:159-160
+        dv = self.dv.copy()
+        dv[self.fixed] = 0.0
+        self.last_iterations, self.last_rr_bb = [], []
+        out_dv = np.zeros_like(dv)
+        for s in range(len(self.scene_offsets) - 1):
+            lo, hi = self.scene_offsets[s], self.scene_offsets[s + 1]
+            sl = slice(lo, hi)
+            maximum = float(np.max(np.abs(rhs[sl]))) if hi > lo else 0.0
+            scale = rhs_scale(maximum)
+            b = np.zeros_like(rhs)
+            b[sl] = scale * rhs[sl]
+            x0 = np.zeros_like(rhs)
+            if maximum != 0.0:
+                x0[sl] = scale * dv[sl]
+
+            def A_s(p, sl=sl):
+                full = np.zeros_like(rhs)
+                full[sl] = p[sl]
+                y = self.apply_A_projected(full)
+                out = np.zeros_like(rhs)
+                out[sl] = y[sl]
+                return out
+
+            tol = 0.0 if fixed_iterations is not None else self.tolerance
+            maxiter = self.maxiter if fixed_iterations is None else fixed_iterations
+            x, it, rr, bb = pcg(A_s, self.apply_M, b, x0, tol, maxiter)
+            out_dv[sl] = x[sl] / scale
+            self.last_iterations.append(it)
+            self.last_rr_bb.append((rr, bb))
+        self.dv = out_dv
+        v_out = v + self.dv
+        q_out = q + v_out * dt
+        q_out[self.fixed] = self.rest[self.fixed]
+        v_out[self.fixed] = 0.0
+        return q_out, v_out, rhs

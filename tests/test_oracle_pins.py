@@ -1,0 +1,214 @@
+"""Pin the CPU oracle to the reference's own known-answer tests (no GPU needed).
+
+Each test restates one hot-path check of the reference's test suite on the same
+fixture meshes (read from ``tests/golden/fixture_meshes.npz``) with the same
+tolerances; the reference file:line is in each docstring.
+"""
+
+import numpy as np
+import pytest
+from fixtures import DT, cube_arrays, energy, one_tet, oracle_cube
+
+from newton_solver_fem_gb300 import scenes
+from oracle import fem_oracle as O
+
+
+def test_hex_box_quadrature_and_one_step_fall():
+    """Hex 2x3x4 box: det_J0_w = 3, inv_J0 = diag(1, 2/3, 1/2), dv_z = -0.00981 (tests/test_reference_builder.py:35-54)."""
+    nodes = np.asarray([(0, 0, 0), (2, 0, 0), (2, 3, 0), (0, 3, 0), (0, 0, 4), (2, 0, 4), (2, 3, 4), (0, 3, 4)], float)
+    inv, det = O.hex_builder_data(nodes, np.arange(8).reshape(1, 8))
+    np.testing.assert_allclose(det, 3.0)
+    np.testing.assert_allclose(inv.astype(np.float32), np.broadcast_to(np.diag([1.0, 2 / 3, 0.5]), (1, 8, 3, 3)),
+                               atol=2e-7)
+    solver = O.OracleFEM(nodes, np.full(8, 3.0), hexes=np.arange(8).reshape(1, 8), hex_inv_J0=inv.astype(np.float32),
+                         hex_det_J0_w=det.astype(np.float32), hex_materials=np.array([[10, 20, 0]], np.float32),
+                         dt=0.001, gravity=(0, 0, -9.81))
+    _, v, _ = solver.step(nodes, np.zeros((8, 3)), 0.001)
+    np.testing.assert_allclose(v[:, 2], -0.00981, atol=1e-7)
+
+
+def test_grid_volume_and_mass():
+    """Hex grid sums to 0.1^3 and mass 100*0.1^3 (tests/test_solver.py:505-512)."""
+    x, el, mass, _ = cube_arrays("hex")
+    _, det = O.hex_builder_data(x, el)
+    assert abs(float(det.astype(np.float32).sum()) - 0.1**3) < 1e-8
+    assert abs(float(mass.sum()) - 100 * 0.1**3) < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["tet", "hex"])
+def test_rigid_motion_symmetry_and_spd(kind):
+    """Rest forces vanish under rigid motion; A symmetric and SPD (tests/test_solver.py:336-348)."""
+    rotation = np.array([[0.8, -0.6, 0.0], [0.6, 0.8, 0.0], [0.0, 0.0, 1.0]])
+    solver = oracle_cube(kind)
+    q = solver.rest @ rotation.T + [0.1, 0.2, -0.15]
+    f = solver.forces(q, np.zeros_like(q), terms=("tet", "hex"))
+    np.testing.assert_allclose(f["tet"] + f["hex"], 0, atol=3e-4)
+    A = solver.dense()
+    np.testing.assert_allclose(A, A.T, atol=2e-8)
+    assert np.linalg.eigvalsh(A).min() > 0
+
+
+@pytest.mark.parametrize("kind", ["tet", "hex"])
+def test_force_is_energy_gradient(kind):
+    """f = -grad(energy) by central differences, sum f = 0 (tests/test_solver.py:350-368)."""
+    rng = np.random.default_rng(7)
+    solver = oracle_cube(kind)
+    x, el, _, mats = cube_arrays(kind)
+    q = x.copy()
+    q[:, 0] *= 1.08
+    q[:, 1] += 0.04 * q[:, 2]
+    f = solver.forces(q, np.zeros_like(q), terms=("tet", "hex"))
+    force = f["tet"] + f["hex"]
+    direction = rng.normal(size=q.shape)
+    direction /= np.linalg.norm(direction)
+    if kind == "tet":
+        kw = dict(tets=el, poses=scenes.tet_poses(x, el), tet_mats=mats)
+    else:
+        kw = dict(hexes=el, hex_mats=mats)
+    for eps in (1e-4, 5e-5):
+        diff = (energy(x, q + eps * direction, **kw) - energy(x, q - eps * direction, **kw)) / (2 * eps)
+        np.testing.assert_allclose(float(-(force * direction).sum()), diff, rtol=0.001, atol=3e-5)
+    np.testing.assert_allclose(force.sum(axis=0), 0, atol=2e-5)
+
+
+def test_step_matches_dense_solve():
+    """One step equals the dense solve of A dv = h f - (A - M) v (tests/test_solver.py:232-262)."""
+    solver = oracle_cube("tet", tolerance=1e-12)
+    q = solver.rest.copy()
+    q[-1, 2] -= 0.001
+    velocity = np.random.default_rng(2).normal(0, 0.03, q.shape).astype(np.float32).astype(np.float64)
+    force = np.zeros_like(q)
+    force[-1] = (0.1, 0.05, -0.2)
+    mass = np.repeat(solver.mass, 3)
+    A = solver.dense()
+    elastic = solver.forces(q, velocity, terms=("tet",))["tet"]
+    rhs = DT * (force + elastic).ravel() - A @ velocity.ravel() + mass * velocity.ravel()
+    increment = np.linalg.solve(A, rhs).reshape(q.shape)
+    q_out, v_out, _ = solver.step(q, velocity, DT, external=force)
+    np.testing.assert_allclose(v_out, velocity + increment, rtol=3e-4, atol=3e-6)
+    np.testing.assert_allclose(q_out, q + DT * (velocity + increment), rtol=1e-6, atol=1e-7)
+
+
+@pytest.mark.parametrize("density", [0.1, 1000.0])
+def test_freefall_across_mass_scales(density):
+    """Zero RHS keeps the state; gravity gives dv_z = -g h (tests/test_solver.py:440-450).
+
+    The reference's ``make_solver`` defaults to ``differentiable=True``, whose checked solve uses tol 1e-8.
+    """
+    solver = oracle_cube("tet", density=density, tolerance=1e-8)
+    q0 = solver.rest.copy()
+    q, _, _ = solver.step(q0, np.zeros_like(q0), DT)
+    np.testing.assert_allclose(q, q0, atol=2e-7)
+    solver.gravity = np.array([0.0, 0.0, -9.81])
+    _, v, _ = solver.step(q0, np.zeros_like(q0), DT)
+    np.testing.assert_allclose(v[:, 2], -DT * 9.81, atol=2e-5)
+
+
+@pytest.mark.parametrize("mass", [1e-25, 1e-18, 1e-14, 1.0])
+def test_tiny_mass_falls_and_zero_rhs_clears_warm_start(mass):
+    """RHS normalisation keeps tiny masses falling; b = 0 clears dv (tests/test_reference_block_preconditioner.py:71-91)."""
+    dt = 1 / 240
+    solver = O.OracleFEM(np.array([[0.0, 0.0, 1.0]]), np.array([mass]), gravity=(0, 0, -9.81), dt=dt, maxiter=8)
+    q, v = solver.rest.copy(), np.zeros((1, 3))
+    for step in range(1, 4):
+        q, v, rhs = solver.step(q, v, dt)
+        np.testing.assert_allclose(v[0], (0, 0, -step * 9.81 * dt), atol=1e-7)
+        np.testing.assert_allclose(solver.dv[0], (0, 0, -9.81 * dt), atol=1e-7)
+        np.testing.assert_allclose(rhs[0], (0, 0, -mass * 9.81 * dt), rtol=3e-7, atol=0)
+    solver.gravity = np.zeros(3)
+    q2, v2, _ = solver.step(q, v, dt)
+    np.testing.assert_allclose(v2, v, atol=1e-7)
+    np.testing.assert_array_equal(solver.dv, np.zeros((1, 3)))
+
+
+def test_dirichlet_matches_reduced_system():
+    """Fixed nodes: the free block solves the reduced dense system (tests/test_fixed_particles.py:50-79)."""
+    x, tets, mass, mats = one_tet()
+    solver = O.OracleFEM(x, mass, tets=tets, tet_poses=scenes.tet_poses(x, tets), tet_materials=mats, gravity=(0, 0, 0),
+                         dt=DT, fixed=[0, 1], maxiter=64, tolerance=1e-12)
+    q = x.copy()
+    q[2] += (0.002, 0.001, -0.001)
+    velocity = np.array(((0, 0, 0), (0, 0, 0), (0.02, -0.03, 0.01), (-0.01, 0.01, 0.02)), np.float64)
+    external = np.array(((20, 30, 40), (10, -30, 60), (0.02, 0.04, 0.03), (-0.01, 0.03, 0.02)), np.float64)
+    for refresh in (False, True, True):
+        if refresh:
+            q = solver.refresh_tangent(q)
+        A = solver.dense()
+        elastic = solver.forces(q, velocity, terms=("tet",))["tet"]
+        m = np.repeat(solver.mass, 3)
+        rhs = DT * (elastic + external).ravel() - (A - np.diag(m)) @ velocity.ravel()
+        expected = np.zeros(12)
+        expected[6:] = np.linalg.solve(A[6:, 6:], rhs[6:])
+        q_out, v_out, _ = solver.step(q, velocity, DT, external=external)
+        np.testing.assert_allclose(solver.dv.ravel(), expected, rtol=3e-4, atol=2e-6)
+        np.testing.assert_array_equal(q_out[:2], x[:2])
+        np.testing.assert_array_equal(v_out[:2], np.zeros((2, 3)))
+        q, velocity = q_out, v_out
+
+
+def test_block_inverse_scale_invariance_and_fallback():
+    """Scale-normalised inverse over 1e-20..1e20, singular fallback (tests/test_reference_block_preconditioner.py:48-69)."""
+    base = np.asarray(((4, 0.7, -0.3), (0.7, 2, 0.4), (-0.3, 0.4, 1)), dtype=np.float64)
+    scales = np.power(10.0, np.arange(-20, 21, dtype=float))
+    blocks = (scales[:, None, None] * base).astype(np.float32)
+    expected = np.linalg.inv(blocks.astype(np.float64))
+    inverse = O.inverse_diagonal_block(blocks, dtype=np.float32)
+    assert np.isfinite(inverse).all()
+    np.testing.assert_allclose(inverse, expected, rtol=6e-7, atol=0)
+    singular = (scales[:, None, None] * np.diag((1, 0, 2))).astype(np.float32)
+    want = np.zeros_like(singular)
+    want[:, 0, 0] = 1 / singular[:, 0, 0]
+    want[:, 1, 1] = 1
+    want[:, 2, 2] = 1 / singular[:, 2, 2]
+    np.testing.assert_allclose(O.inverse_diagonal_block(singular, dtype=np.float32), want, rtol=2e-7, atol=0)
+
+
+def test_tolerance_semantics():
+    """True relative residual < 0.0101 at tol 1e-2 and < 2e-5 at 1e-5 with more iterations (tests/test_solver.py:281-316)."""
+    external = np.random.default_rng(13).normal(0, 0.03, (27, 3)).astype(np.float32).astype(np.float64)
+    residuals, iterations = [], []
+    for tol in (1e-2, 1e-5):
+        solver = oracle_cube("tet", tolerance=tol)
+        q0 = solver.rest.copy()
+        _, _, rhs = solver.step(q0, np.zeros_like(q0), DT, external=external)
+        A = solver.dense()
+        residuals.append(np.linalg.norm(A @ solver.dv.ravel() - rhs.ravel()) / np.linalg.norm(rhs))
+        iterations.append(solver.last_iterations[0])
+    assert residuals[0] < 0.0101
+    assert residuals[1] < 2e-5
+    assert iterations[1] > iterations[0]
+
+
+def test_unique_edge_springs():
+    """Two tets sharing a face give 9 unique edges (tests/test_reference_builder.py:15-33)."""
+    x = np.array([(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (0, 0, -1)], float)
+    tets = np.array([[0, 1, 2, 3], [0, 2, 1, 4]], np.int32)
+    assert len(scenes.unique_edges(x, tets)) == 9
+
+
+def test_external_force_derivative_is_half_dt():
+    """A free 2 kg particle has d v_x / d f_ext = h/2 (tests/test_solver.py:452-464), by linearity."""
+    solver = O.OracleFEM(np.array([[0.0, 0.0, 1.0]]), np.array([2.0]), gravity=(0, 0, 0), dt=DT, maxiter=128,
+                         tolerance=1e-12)
+    eps = 1e-3
+    _, vp, _ = solver.step(solver.rest, np.zeros((1, 3)), DT, external=np.array([[eps, 0, 0]]))
+    _, vm, _ = solver.step(solver.rest, np.zeros((1, 3)), DT, external=np.array([[-eps, 0, 0]]))
+    np.testing.assert_allclose((vp[0, 0] - vm[0, 0]) / (2 * eps), DT / 2, atol=1e-8)
+
+
+def test_synthetic_config_sizes():
+    """Workload sizes: Tet4 8x2x2 -> 81 nodes / 192 tets / nnzb 769; 16x4x4 -> 425 / 1536 / 4921."""
+    c1 = scenes.tet_cantilever()
+    assert (c1.particle_count, len(c1.tets), len(c1.fixed)) == (81, 192, 9)
+    assert np.all(scenes.tet_volumes(c1.x, c1.tets) > 0)
+    r, c, v = O.constant_triplets(c1.mass, np.zeros((0, 2), np.int64), np.zeros(0), np.zeros(0), c1.dt)
+    rt, ct, vt = O.tet_tangent(c1.x, c1.tets, scenes.tet_poses(c1.x, c1.tets), c1.tet_materials, 0.05, 20.0, c1.dt)
+    offsets, _, _ = O.assemble_bsr(np.concatenate([r, rt]), np.concatenate([c, ct]), np.concatenate([v, vt]), 81)
+    assert offsets[-1] == 769
+    c4 = scenes.tet_beam()
+    assert (c4.particle_count, len(c4.tets)) == (425, 1536)
+    hx = scenes.hex_cells(2, 2, 2)
+    xg = scenes.grid_nodes(2, 2, 2, 0.05)
+    assert hx.shape == (8, 8)
+    _, det = O.hex_builder_data(xg, hx)
+    np.testing.assert_allclose(det.sum(), 0.1**3)
