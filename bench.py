@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Benchmark of the SolverFEM hot path on GB300: DOF-substeps/s of the Hex8 64^3 block.
+
+Workload (the single-GPU configuration the metric is quoted on): a 64^3 Q1
+Hex8 grid of 1 cm cells (262,144 elements, 274,625 nodes, 823,875 DOF),
+E = 5e5 Pa, nu = 0.4, rho = 1100, resting on the analytic ground (mu = 0.5),
+velocities seeded N(0, 0.05 m/s); 60 Hz frames of 10 substeps; CG with
+block-Jacobi at relative residual 1e-2, at most 50 iterations; float32.
+
+One bench step = one frame = tangent refresh + 10 linearly implicit substeps,
+replayed from a captured CUDA graph.  ``value`` = 3 * nodes * substeps / frame
+time with inputs resident in HBM.  ``e2e`` = the same metric through the
+public ``SolverFEM`` API with the frame's positions/velocities copied from
+pinned host memory and the result read back every frame.  ``roofline`` = the
+persistent PCG kernel's algorithmic bytes per launch over its CUDA-event launch
+time.  ``cpu_baseline`` = the CPU oracle (NumPy/SciPy restatement of the
+reference algorithm) on a bounded sample of the same workload.
+
+``--impl reference`` times that CPU restatement alone on the same metric and
+config (the reference itself needs Warp and Newton, which cannot be installed
+in this image).  Multi-GPU: the single mesh does not shard, so N GPUs run N
+independent replicas ("replicas only"); value = all replicas' DOF-substeps / max
+time over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "DOF-substeps/s at rel-res 1e-2: batched/adjoint vs plain on 1 GB300; SpMV GB/s"
+UNIT = "DOF-substeps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    p.add_argument("--cells", type=int, default=64, help="Hex8 cells per axis (64 = the benchmark workload)")
+    p.add_argument("--cpu-sample", type=float, default=20.0, help="seconds budget for the CPU baseline sample")
+    p.add_argument("--cpu-cells", type=int, default=24, help="Hex8 cells per axis of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dram_traffic_per_launch():
+    """Per-launch DRAM bytes of the PCG kernel from the committed ncu summary, if present."""
+    path = ROOT / "profiles" / "pcg_kernel_hex8_64.md"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_launch_full_size:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [c.strip() for c in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(cells: int, device: str):
+    import numpy as np
+
+    from newton_solver_fem_gb300 import SolverFEM, model_from_arrays, scenes
+
+    sc = scenes.hex_block_64(n=cells)
+    model = model_from_arrays(sc.x, sc.mass, hexes=sc.hexes, hex_materials=sc.hex_materials, velocity=sc.velocity,
+                              radius=0.0, gravity=sc.gravity, device=device)
+    solver = SolverFEM(model, dt=sc.dt, solver_type="cg", preconditioner_type="block_diag",
+                       linear_solver_maxiter=sc.maxiter, linear_solver_tolerance=sc.tolerance,
+                       ground_plane=sc.ground_plane, self_contact_ke=0.0)
+    return sc, model, solver, np
+
+
+def spmv_bytes(nnzb: int, n: int) -> int:
+    """Algorithmic bytes of one 3x3-BSR SpMV: 36 B values + 4 B column per block, offsets, x read, y write."""
+    return 40 * nnzb + 4 * (n + 1) + 24 * n
+
+
+def pcg_launch_bytes(nnzb: int, n: int, iterations: float) -> float:
+    """Algorithmic bytes of one persistent PCG launch.
+
+    Per CG iteration: one SpMV plus 120 B/node (Minv 36, read x r p Ap 48, write x r p 36).
+    Prologue (predictor and initial residual in one pass over A): one SpMV plus
+    read v, dv, f and write f, r (60 B/node) plus read x, r, f, Minv and write x, r, z (108 B/node).
+    Epilogue: read x, v, q and write dv, q, v (72 B/node).
+    """
+    return iterations * (spmv_bytes(nnzb, n) + 120 * n) + spmv_bytes(nnzb, n) + (60 + 108 + 72) * n
+
+
+def cpu_baseline(cells: int, budget_s: float) -> dict:
+    """Oracle port on the host cores: one tangent refresh and substeps of the same workload until the budget."""
+    import numpy as np
+
+    from newton_solver_fem_gb300 import scenes
+    from oracle import fem_oracle as O
+
+    sc = scenes.hex_block_64(n=cells)
+    x = sc.x.astype(np.float32).astype(np.float64)
+    inv, det = O.hex_builder_data(x, sc.hexes)
+    orc = O.OracleFEM(x, sc.mass.astype(np.float32), hexes=sc.hexes, hex_inv_J0=inv.astype(np.float32),
+                      hex_det_J0_w=det.astype(np.float32), hex_materials=sc.hex_materials, dt=sc.dt,
+                      ground_plane=sc.ground_plane, maxiter=sc.maxiter, tolerance=sc.tolerance)
+    q, v = x.copy(), sc.velocity.astype(np.float64)
+    t0 = time.perf_counter()
+    q = orc.refresh_tangent(q)
+    t_refresh = time.perf_counter() - t0
+    subs, t_sub = 0, 0.0
+    while subs < sc.substeps and (subs == 0 or t_refresh + t_sub < budget_s):
+        t1 = time.perf_counter()
+        q, v, _ = orc.step(q, v, sc.dt)
+        t_sub += time.perf_counter() - t1
+        subs += 1
+    frame_s = t_refresh + t_sub / subs * sc.substeps
+    value = 3 * len(x) * sc.substeps / frame_s
+    return {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"NumPy/SciPy oracle, Hex8 {cells}^3: 1 tangent refresh + {subs} substep(s) "
+                      f"({t_refresh + t_sub:.1f} s), frame = refresh + 10 x mean substep"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    base = cpu_baseline(min(args.cells, args.cpu_cells), args.cpu_sample)
+    value = base["value"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 3 * (args.cells + 1) ** 3 * 10 / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"hex8_block_{args.cells}^3", "substeps": 10, "cg_tol": 1e-2, "cg_maxiter": 50},
+        "cpu_baseline": base,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference needs Warp 1.17 + Newton 1.7 (not installable here); this times the CPU restatement",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args) -> None:
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    device = f"cuda:{local}"
+    from newton_solver_fem_gb300 import _lib, build
+
+    build.build()
+    sc, model, solver, np = build_workload(args.cells, device)
+    lib = _lib.load()
+    P = model.particle_count
+    info = solver.matrix_info()
+    s0, s1 = model.state(), model.state()
+    substeps = sc.substeps
+    stream = torch.cuda.Stream(device)
+
+    def frame(a, b):
+        solver.refresh_tangent(a.particle_q)
+        for k in range(substeps):
+            solver.step(a, b, None, None, sc.dt)
+            a, b = b, a
+
+    with torch.cuda.stream(stream):
+        frame(s0, s1)  # eager warm-up (first refresh, lazy setup)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            frame(s0, s1)
+    for _ in range(max(3, args.warmup)):
+        graph.replay()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(args.steps):
+            graph.replay()
+        end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = start.elapsed_time(end) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t)
+    value = world * 3 * P * substeps / (ms / 1e3)
+
+    # ---- roofline of the dominant kernel: eager frames with per-launch CUDA events
+    stats0 = solver.stats()
+    _lib.check(lib.fem_set_timing(solver._handle, 1))
+    with torch.cuda.stream(stream):
+        for _ in range(max(1, min(args.steps, 3))):
+            frame(s0, s1)
+    total_ms, launches = torch.tensor(0.0), 0
+    import ctypes
+
+    t_ms, n_l = ctypes.c_double(), ctypes.c_int64()
+    _lib.check(lib.fem_get_timing(solver._handle, ctypes.byref(t_ms), ctypes.byref(n_l)))
+    _lib.check(lib.fem_set_timing(solver._handle, 0))
+    stats1 = solver.stats()
+    launches = n_l.value
+    iters = (stats1["total_iterations"] - stats0["total_iterations"]) / max(1, launches)
+    launch_ms = t_ms.value / max(1, launches)
+    bytes_launch = pcg_launch_bytes(info["nnzb"], P, iters)
+    achieved = bytes_launch / (launch_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = dram_traffic_per_launch()
+
+    # ---- end to end through the public API with host buffers
+    host_q = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
+    host_v = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
+    host_q.copy_(s0.particle_q.cpu())
+    host_v.copy_(s0.particle_qd.cpu())
+    torch.cuda.synchronize()
+    e2e_steps = max(1, args.steps)
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(e2e_steps):
+            s0.particle_q.copy_(host_q, non_blocking=True)
+            s0.particle_qd.copy_(host_v, non_blocking=True)
+            frame(s0, s1)
+            host_q.copy_(s0.particle_q, non_blocking=True)
+            host_v.copy_(s0.particle_qd, non_blocking=True)
+        stream.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = world * 3 * P * substeps / e2e_s
+    finite = bool(torch.isfinite(s0.particle_q).all())
+
+    if rank == 0:
+        cpu = None if args.no_cpu_baseline else cpu_baseline(min(args.cells, args.cpu_cells), args.cpu_sample)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"hex8_block_{args.cells}^3", "nodes": P, "hexes": int(model.fem.hex_count),
+                       "dof": 3 * P, "substeps_per_step": substeps, "cg_tol": sc.tolerance,
+                       "cg_maxiter": sc.maxiter, "preconditioner": "block_diag", "parallelism": "replicas",
+                       "nnzb": info["nnzb"], "mean_cg_iterations": iters,
+                       "l2": "inputs larger than L2 (A values 259 MB, element blocks 614 MB at 64^3)"},
+            "roofline": {"kernel": "pcg_kernel", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "bytes_per_launch": bytes_launch, "launch_ms": launch_ms, "launches": launches},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 12 * P,
+                    "d2h_bytes_per_step": 2 * 12 * P},
+            "gpu_launches": args.steps * (3 + 4 * substeps),
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "finite": finite,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

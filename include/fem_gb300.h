@@ -1,0 +1,176 @@
+/*
+ * fem_gb300.h -- C ABI of libfemgb300.so, the GB300 (sm_103a) implementation of
+ * SolverFEM's per-substep hot path: Stable Neo-Hookean Tet4/Hex8 forces and
+ * approximate PSD tangent, deterministic 3x3-block BSR assembly of
+ * A = M + h^2 K~ + h C_s, and block-Jacobi preconditioned CG with the fixed-node
+ * projection PAP + I - P.
+ *
+ * Reference interfaces replaced (paths inside the reference project,
+ * src/newton_solver_fem/_src/solvers/fem/):
+ *   fem_create / fem_destroy     SolverFEM.__init__                  solver.py:212-415
+ *   fem_step                     SolverFEM.step                      solver.py:942-1002
+ *   fem_refresh_tangent          SolverFEM.refresh_tangent           solver.py:769-857
+ *   fem_rebuild_element_blocks   SolverFEM.rebuild_element_blocks    solver.py:506-508, 591-687
+ *   fem_refresh_preconditioner   SolverFEM.refresh_preconditioner    solver.py:502-504
+ *   fem_set_tolerance            SolverFEM.linear_solver_tolerance   solver.py:241-243, 1203-1217
+ *   fem_set_maxiter              SolverFEM.linear_solver_maxiter     solver.py:273
+ *   fem_reset                    SolverFEM.reset                     solver.py:436-443
+ *   fem_velocity_increment_ptr   SolverFEM.velocity_increment        solver.py:478-481
+ *   fem_get_stats                SolverFEM.last_cg_iters             solver.py:279, 1333-1335
+ *   fem_eval_forces              SolverFEM.eval_*_forces             solver.py:1357-1600
+ *   fem_export_bsr               SolverFEM.A_bsr (Warp BsrMatrix)    solver.py:322-337
+ *   fem_export_preconditioner    SolverFEM._pc_inv_diag              solver.py:1142-1201
+ *   fem_matrix_info              A_bsr.nnz / nrow                    solver.py:322-328
+ *
+ * Conventions.  All vectors are contiguous float32 [n, 3] (x, y, z per node), all
+ * index arrays int32.  Pointers passed to fem_step / fem_refresh_tangent /
+ * fem_eval_forces / fem_export_* are DEVICE pointers; FemDesc pointers are HOST
+ * pointers that fem_create copies (the handle owns every device buffer it
+ * allocates).  Every entry point enqueues work on the given CUDA stream
+ * (cudaStream_t passed as void*; NULL = legacy default stream) and returns
+ * without host synchronisation, except fem_create, fem_get_stats and
+ * fem_matrix_info.  fem_step, fem_refresh_tangent (after its first call) and
+ * fem_refresh_preconditioner allocate nothing and may be captured in a CUDA
+ * graph.  A handle is not thread-safe; use one handle per stream.
+ */
+#ifndef FEM_GB300_H
+#define FEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes (int return of every entry point). */
+#define FEM_OK 0
+#define FEM_ERR_BAD_ARG 1      /* reference: ValueError */
+#define FEM_ERR_NOT_CONVERGED 2 /* informational: CG hit maxiter above tolerance */
+#define FEM_ERR_NON_FINITE 3    /* NaN/Inf in the solve */
+#define FEM_ERR_TIMEOUT 4       /* a bounded device wait gave up (grid barrier) */
+#define FEM_ERR_CUDA 5          /* CUDA runtime error */
+#define FEM_ERR_UNSUPPORTED 6   /* option outside the implemented hot path */
+
+/* Preconditioner kinds (SolverFEM preconditioner_type). */
+#define FEM_PRECOND_BLOCK_DIAG 0 /* "block_diag": 3x3 block Jacobi, kernels.py:1817-1868 */
+#define FEM_PRECOND_DIAG 1       /* "diag": point Jacobi of the scalar diagonal */
+
+/* Force-term bits for fem_eval_forces (solver.py:571-582 order). */
+#define FEM_TERM_SPRING 1
+#define FEM_TERM_TET 2
+#define FEM_TERM_HEX 4
+#define FEM_TERM_GROUND 8
+#define FEM_TERM_GRAVITY 16
+#define FEM_TERM_DAMPING 32
+
+typedef struct FemHandle FemHandle;
+
+/* Construction data: Newton Model fields plus SolverFEM keyword arguments. */
+typedef struct FemDesc {
+    int32_t particle_count; /* P */
+    int32_t tet_count;      /* T */
+    int32_t hex_count;      /* H */
+    int32_t spring_count;   /* S */
+    const float* particle_q;        /* [P,3] construction positions (Dirichlet anchors, initial tangent) */
+    const float* particle_mass;     /* [P] */
+    const float* particle_inv_mass; /* [P] */
+    const float* particle_radius;   /* [P] or NULL (= 0) */
+    const int32_t* particle_flags;  /* [P] or NULL (= all ACTIVE); bit 0 = ACTIVE */
+    const int32_t* tet_indices;     /* [T,4] */
+    const float* tet_poses;         /* [T,3,3] row-major inverse rest edge matrices */
+    const float* tet_materials;     /* [T,3] (mu, lambda, damping) */
+    const int32_t* hex_indices;     /* [H,8] VTK order */
+    const float* hex_materials;     /* [H,3] */
+    const float* hex_inv_J0;        /* [H,8,3,3] */
+    const float* hex_det_J0_w;      /* [H,8] */
+    const int32_t* spring_indices;  /* [2S] */
+    const float* spring_rest_length; /* [S] */
+    const float* spring_stiffness;   /* [S] */
+    const float* spring_damping;     /* [S] */
+    const int32_t* fixed_indices;    /* [fixed_count] unique, in range */
+    int32_t fixed_count;
+    const int64_t* scene_offsets;    /* [scene_count+1] node ranges of independent scenes, NULL = one scene */
+    int32_t scene_count;
+    float gravity[3];          /* model gravity, used when fem_step gets no gravity pointer */
+    float dt;                  /* assembly timestep */
+    float min_stretch;         /* < 0 disables the clamp */
+    float max_stretch;
+    int32_t has_ground;
+    float ground_plane[4];     /* n.x + d = 0 */
+    float ground_ke, ground_kd, ground_kf, ground_mu;
+    float linear_damping;
+    int32_t enable_tet_activations;
+    int32_t preconditioner;    /* FEM_PRECOND_* */
+    int32_t maxiter;
+    float tolerance;
+    float* velocity_increment; /* optional caller-owned DEVICE [P,3] buffer for dv; NULL = handle-owned */
+} FemDesc;
+
+/* Per-solve statistics (one entry per scene, plus the sticky device status). */
+typedef struct FemStats {
+    int32_t status;        /* FEM_OK or FEM_ERR_TIMEOUT / FEM_ERR_NON_FINITE bits (sticky until fem_reset) */
+    int32_t scene_count;
+    int32_t max_iterations; /* maximum CG iterations over scenes in the last solve */
+    int32_t min_iterations;
+    float max_relative_residual; /* max over scenes of ||r||/||b|| (recurrence residual) */
+    int32_t unconverged_scenes;
+    int64_t total_iterations;    /* CG iterations summed over scenes and launches since creation */
+} FemStats;
+
+int fem_create(const FemDesc* desc, FemHandle** out);
+int fem_destroy(FemHandle* handle);
+
+/* One linearly implicit substep.  q_in / v_in are restored in place at fixed
+ * nodes (reference semantics), f_workspace receives the final RHS
+ * h*sum(f) - h^2 K v (projected), q_out / v_out the new state.
+ * external_forces, activations and gravity may be NULL (gravity NULL = the
+ * construction-time value; activations only with enable_tet_activations). */
+int fem_step(FemHandle* handle, float* q_in, float* v_in, float* q_out, float* v_out, float* f_workspace,
+             const float* external_forces, const float* activations, const float* gravity, float dt, void* stream);
+
+/* Refresh the deformation-dependent tangent at q (fixed nodes restored in q
+ * first) and the block-Jacobi inverse.  A changed dt also rebuilds the
+ * mass/spring blocks and zeroes the warm start. */
+int fem_refresh_tangent(FemHandle* handle, float* q, float dt, void* stream);
+/* Rewrite only the Tet4/Hex8 blocks at q and dt (mass/spring blocks keep the
+ * assembly dt), then the preconditioner. */
+int fem_rebuild_element_blocks(FemHandle* handle, float* q, float dt, void* stream);
+int fem_refresh_preconditioner(FemHandle* handle, void* stream);
+
+int fem_set_tolerance(FemHandle* handle, float tolerance);
+/* Time limit of every bounded device wait (grid barrier) in nanoseconds,
+ * default 2e9.  A wait that runs out makes the kernel return early and sets the
+ * sticky FEM_ERR_TIMEOUT status that fem_get_stats reports. */
+int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
+int fem_set_maxiter(FemHandle* handle, int32_t maxiter);
+int fem_reset(FemHandle* handle, void* stream);
+float* fem_velocity_increment_ptr(FemHandle* handle);
+int fem_get_stats(FemHandle* handle, FemStats* stats, int32_t* scene_iterations, void* stream);
+
+/* Measurement support: when enabled, every eager (not graph-captured)
+ * fem_step brackets its PCG launch with CUDA events on the launch stream;
+ * fem_get_timing synchronises, returns the summed launch time and count, and
+ * clears the record. */
+int fem_set_timing(FemHandle* handle, int32_t enable);
+int fem_get_timing(FemHandle* handle, double* pcg_ms_total, int64_t* launches);
+
+/* Selected force terms (FEM_TERM_* bits), unscaled, summed into out[P,3]. */
+int fem_eval_forces(FemHandle* handle, const float* q, const float* v, const float* activations,
+                    const float* gravity, int32_t terms, float* out, void* stream);
+
+/* Sparse matrix in the reference's BSR form: offsets [P+1], columns [nnzb],
+ * values [nnzb,3,3]; any pointer may be NULL. */
+int fem_matrix_info(FemHandle* handle, int64_t* nnzb, int64_t* triplet_count, int64_t* stored_blocks);
+int fem_export_bsr(FemHandle* handle, int32_t* offsets, int32_t* columns, float* values, void* stream);
+int fem_export_preconditioner(FemHandle* handle, float* inverse_blocks, void* stream);
+/* Raw element/constant blocks in the reference's triplet layout [P | 2S | 16T | 64H] (bsr_values). */
+int fem_export_triplets(FemHandle* handle, int32_t* rows, int32_t* columns, float* values, void* stream);
+
+const char* fem_status_string(int status);
+const char* fem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FEM_GB300_H */

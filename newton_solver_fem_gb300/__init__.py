@@ -1,0 +1,23 @@
+"""GB300 (sm_103a) implementation of SolverFEM's per-substep hot path.
+
+Public names follow the reference package (``newton_solver_fem/__init__.py``):
+``SolverFEM`` (alias ``SolverLinearFEM``), ``FEMBuilder`` and ``LinearFEMData``,
+plus the minimal ``Model`` / ``State`` / ``Control`` containers the solver reads.
+The numerical work runs in ``libfemgb300.so`` (``include/fem_gb300.h``).
+"""
+
+from .builder import FEMBuilder, LinearFEMData, Model, State, Control, hex_gauss_data, model_from_arrays
+from .solver import BsrMatrix, SolverFEM, SolverLinearFEM
+
+__all__ = [
+    "BsrMatrix",
+    "Control",
+    "FEMBuilder",
+    "LinearFEMData",
+    "Model",
+    "SolverFEM",
+    "SolverLinearFEM",
+    "State",
+    "hex_gauss_data",
+    "model_from_arrays",
+]

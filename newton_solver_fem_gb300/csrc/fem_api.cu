@@ -1,0 +1,765 @@
+// C ABI of libfemgb300.so: handle construction (pattern, SELL layout,
+// incidence lists, launch configuration) and the per-substep entry points.
+// Host-side setup replaces SolverFEM.__init__ (solver.py:212-415) and Warp's
+// bsr_set_from_triplets / map_triplet_blocks (solver.py:331-337, 823-846;
+// sparse_update.py:9-30): the sparsity pattern is the set of valid triplet
+// (row, col) pairs of the reference layout, columns sorted per row, and each
+// slot keeps its contributing triplets in ascending order.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "fem_internal.cuh"
+
+namespace fem {
+void upload_hex_reference_table();
+size_t pcg_smem_bytes(int L, int S);
+}  // namespace fem
+
+struct FemHandle {
+    fem::Handle h;
+    int device = 0;
+};
+
+namespace {
+
+using fem::Handle;
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <class F>
+void parallel_for(int64_t n, F&& fn) {
+    unsigned hw = std::thread::hardware_concurrency();
+    int nt = (int)std::max(1u, std::min(hw == 0 ? 1u : hw, 32u));
+    if (n < 4096 || nt == 1) {
+        fn(0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    int64_t chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t) {
+        int64_t lo = t * chunk, hi = std::min(n, lo + chunk);
+        if (lo >= hi) break;
+        pool.emplace_back([&fn, lo, hi] { fn(lo, hi); });
+    }
+    for (auto& th : pool) th.join();
+}
+
+struct Builder {
+    Handle& h;
+    int status = FEM_OK;
+    explicit Builder(Handle& hh) : h(hh) {}
+
+    template <class T>
+    T* alloc(size_t n) {
+        if (n == 0 || status != FEM_OK) return nullptr;
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e != cudaSuccess) {
+            fail(FEM_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return nullptr;
+        }
+        h.allocations.push_back(p);
+        cudaMemset(p, 0, n * sizeof(T));
+        return (T*)p;
+    }
+    template <class T>
+    T* upload(const T* src, size_t n) {
+        T* d = alloc<T>(n);
+        if (d && src) {
+            cudaError_t e = cudaMemcpy(d, src, n * sizeof(T), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) fail(FEM_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+        }
+        return d;
+    }
+    template <class T>
+    T* upload(const std::vector<T>& v) {
+        return upload(v.data(), v.size());
+    }
+    void fail(int code, const std::string& msg) {
+        if (status == FEM_OK) {
+            status = code;
+            h.last_error = msg;
+        }
+    }
+};
+
+thread_local std::string g_error;
+
+int set_error(int code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+
+int cuda_status(cudaError_t e, Handle* h = nullptr) {
+    if (e == cudaSuccess) return FEM_OK;
+    std::string msg = std::string("CUDA error: ") + cudaGetErrorString(e);
+    if (h) h->last_error = msg;
+    return set_error(FEM_ERR_CUDA, msg);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fem_version(void) { return "fem_gb300 0.1 (sm_103a)"; }
+
+const char* fem_status_string(int status) {
+    switch (status) {
+        case FEM_OK: return "ok";
+        case FEM_ERR_BAD_ARG: return g_error.empty() ? "bad argument" : g_error.c_str();
+        case FEM_ERR_NOT_CONVERGED: return "linear solve reached maxiter above tolerance";
+        case FEM_ERR_NON_FINITE: return "non-finite value in the linear solve";
+        case FEM_ERR_TIMEOUT: return "a bounded device wait timed out";
+        case FEM_ERR_CUDA: return g_error.empty() ? "CUDA error" : g_error.c_str();
+        case FEM_ERR_UNSUPPORTED: return g_error.empty() ? "unsupported option" : g_error.c_str();
+        default: return "unknown status";
+    }
+}
+
+int fem_create(const FemDesc* d, FemHandle** out) {
+    if (d == nullptr || out == nullptr) return set_error(FEM_ERR_BAD_ARG, "null descriptor or output");
+    *out = nullptr;
+    const int P = d->particle_count, T = d->tet_count, Hn = d->hex_count, S = d->spring_count;
+    if (P < 0 || T < 0 || Hn < 0 || S < 0) return set_error(FEM_ERR_BAD_ARG, "negative element count");
+    if (P > 0 && (d->particle_q == nullptr || d->particle_mass == nullptr || d->particle_inv_mass == nullptr))
+        return set_error(FEM_ERR_BAD_ARG, "particle arrays are required");
+    if (T > 0 && (d->tet_indices == nullptr || d->tet_poses == nullptr || d->tet_materials == nullptr))
+        return set_error(FEM_ERR_BAD_ARG, "tet arrays are required");
+    if (Hn > 0 && (d->hex_indices == nullptr || d->hex_materials == nullptr || d->hex_inv_J0 == nullptr ||
+                   d->hex_det_J0_w == nullptr))
+        return set_error(FEM_ERR_BAD_ARG, "hex arrays are required");
+    if (S > 0 && (d->spring_indices == nullptr || d->spring_rest_length == nullptr ||
+                  d->spring_stiffness == nullptr || d->spring_damping == nullptr))
+        return set_error(FEM_ERR_BAD_ARG, "spring arrays are required");
+    if (!(d->tolerance > 0.0f) || !std::isfinite(d->tolerance))
+        return set_error(FEM_ERR_BAD_ARG, "linear_solver_tolerance must be finite and positive");
+    if (d->maxiter < 0) return set_error(FEM_ERR_BAD_ARG, "linear_solver_maxiter must be non-negative");
+    if (d->preconditioner != FEM_PRECOND_BLOCK_DIAG && d->preconditioner != FEM_PRECOND_DIAG)
+        return set_error(FEM_ERR_UNSUPPORTED, "preconditioner must be block_diag or diag");
+    const int64_t ntrip = (int64_t)P + 2 * (int64_t)S + 16 * (int64_t)T + 64 * (int64_t)Hn;
+    if (ntrip >= (int64_t)INT32_MAX) return set_error(FEM_ERR_BAD_ARG, "problem too large for int32 triplet ids");
+    for (int64_t k = 0; k < 4 * (int64_t)T; ++k)
+        if (d->tet_indices[k] < 0 || d->tet_indices[k] >= P) return set_error(FEM_ERR_BAD_ARG, "tet index out of range");
+    for (int64_t k = 0; k < 8 * (int64_t)Hn; ++k)
+        if (d->hex_indices[k] < 0 || d->hex_indices[k] >= P) return set_error(FEM_ERR_BAD_ARG, "hex index out of range");
+    for (int64_t k = 0; k < 2 * (int64_t)S; ++k)
+        if (d->spring_indices[k] >= P || d->spring_indices[k] < -1)
+            return set_error(FEM_ERR_BAD_ARG, "spring index out of range");
+    std::vector<unsigned char> fixed_mask(P, 0);
+    for (int k = 0; k < d->fixed_count; ++k) {
+        int i = d->fixed_indices[k];
+        if (i < 0 || i >= P) return set_error(FEM_ERR_BAD_ARG, "fixed_particle_indices contains an out-of-range node");
+        fixed_mask[i] = 1;
+    }
+    std::vector<int64_t> scenes;
+    if (d->scene_offsets != nullptr && d->scene_count > 0) {
+        scenes.assign(d->scene_offsets, d->scene_offsets + d->scene_count + 1);
+        if (scenes.front() != 0 || scenes.back() != P) return set_error(FEM_ERR_BAD_ARG, "scene offsets must span [0, P]");
+        for (int s = 0; s < d->scene_count; ++s)
+            if (scenes[s + 1] <= scenes[s]) return set_error(FEM_ERR_BAD_ARG, "scene offsets must increase");
+    } else {
+        scenes = {0, (int64_t)P};
+    }
+    const int nscenes = (int)scenes.size() - 1;
+    if (nscenes > 1024) return set_error(FEM_ERR_UNSUPPORTED, "at most 1024 scenes per handle");
+    if (P > 0) {
+        // elements and springs may not couple scenes
+        std::vector<int> scene_of(P);
+        for (int s = 0; s < nscenes; ++s)
+            for (int64_t i = scenes[s]; i < scenes[s + 1]; ++i) scene_of[i] = s;
+        auto same = [&](const int32_t* idx, int width, int64_t count) {
+            for (int64_t e = 0; e < count; ++e) {
+                int s0 = -1;
+                for (int k = 0; k < width; ++k) {
+                    int n = idx[e * width + k];
+                    if (n < 0) continue;
+                    if (s0 < 0) s0 = scene_of[n];
+                    else if (scene_of[n] != s0) return false;
+                }
+            }
+            return true;
+        };
+        if (!same(d->tet_indices, 4, T) || !same(d->hex_indices, 8, Hn) || !same(d->spring_indices, 2, S))
+            return set_error(FEM_ERR_BAD_ARG, "an element or spring couples two scenes");
+    }
+
+    int device = 0;
+    cudaError_t ce = cudaGetDevice(&device);
+    if (ce != cudaSuccess) return cuda_status(ce);
+    auto* H = new FemHandle();
+    H->device = device;
+    Handle& h = H->h;
+    Builder b(h);
+    h.P = P;
+    h.T = T;
+    h.H = Hn;
+    h.S = S;
+    h.nscenes = nscenes;
+    h.ntrip = ntrip;
+    h.dt = d->dt;
+    h.min_stretch = d->min_stretch;
+    h.max_stretch = d->max_stretch;
+    h.has_ground = d->has_ground;
+    for (int k = 0; k < 4; ++k) h.ground[k] = d->ground_plane[k];
+    h.gke = d->ground_ke;
+    h.gkd = d->ground_kd;
+    h.gkf = d->ground_kf;
+    h.gmu = d->ground_mu;
+    h.linear_damping = d->linear_damping;
+    h.enable_act = d->enable_tet_activations;
+    h.precond = d->preconditioner;
+    h.maxiter = d->maxiter;
+    h.tol = d->tolerance;
+    h.nfixed = d->fixed_count;
+    fem::upload_hex_reference_table();
+
+    // ---- empty-material tets produce no triplets (kernels.py:690-700)
+    std::vector<unsigned char> tet_empty(T, 0);
+    for (int t = 0; t < T; ++t)
+        tet_empty[t] = d->tet_materials[3 * t] == 0.0f && d->tet_materials[3 * t + 1] == 0.0f &&
+                       d->tet_materials[3 * t + 2] == 0.0f;
+    const int64_t off_spring = P, off_tet = (int64_t)P + 2 * (int64_t)S, off_hex = off_tet + 16 * (int64_t)T;
+    auto trip_rc = [&](int64_t t, int& r, int& c) {
+        if (t < off_spring) {
+            r = c = (int)t;
+        } else if (t < off_tet) {
+            int64_t k = t - off_spring;
+            int s = (int)(k >> 1);
+            int a = d->spring_indices[2 * s], bb = d->spring_indices[2 * s + 1];
+            if (k & 1) { r = bb; c = a; } else { r = a; c = bb; }
+            if (r < 0 || c < 0) r = c = -1;
+        } else if (t < off_hex) {
+            int64_t k = t - off_tet;
+            int e = (int)(k >> 4), ab = (int)(k & 15);
+            if (tet_empty[e]) { r = c = -1; return; }
+            r = d->tet_indices[4 * e + (ab >> 2)];
+            c = d->tet_indices[4 * e + (ab & 3)];
+        } else {
+            int64_t k = t - off_hex;
+            int e = (int)(k >> 6), ab = (int)(k & 63);
+            r = d->hex_indices[8 * e + (ab >> 3)];
+            c = d->hex_indices[8 * e + (ab & 7)];
+        }
+    };
+
+    // ---- pattern: bucket triplets by row (ascending id), sort each row by column
+    std::vector<int> trip_rows(ntrip), trip_cols(ntrip);
+    std::vector<int64_t> row_ptr(P + 1, 0);
+    for (int64_t t = 0; t < ntrip; ++t) {
+        int r, c;
+        trip_rc(t, r, c);
+        trip_rows[t] = r;
+        trip_cols[t] = c;
+        if (r >= 0) row_ptr[r + 1]++;
+    }
+    for (int i = 0; i < P; ++i) row_ptr[i + 1] += row_ptr[i];
+    const int64_t nvalid = P > 0 ? row_ptr[P] : 0;
+    std::vector<int> contrib(nvalid);
+    {
+        std::vector<int64_t> pos(row_ptr.begin(), row_ptr.end() - 1);
+        for (int64_t t = 0; t < ntrip; ++t)
+            if (trip_rows[t] >= 0) contrib[pos[trip_rows[t]]++] = (int)t;
+    }
+    std::vector<int> row_nnz(P, 0);
+    parallel_for(P, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            int* beg = contrib.data() + row_ptr[i];
+            int* end = contrib.data() + row_ptr[i + 1];
+            std::stable_sort(beg, end, [&](int x, int y) { return trip_cols[x] < trip_cols[y]; });
+            int n = 0, prev = -1;
+            for (int* p = beg; p != end; ++p)
+                if (trip_cols[*p] != prev) { ++n; prev = trip_cols[*p]; }
+            row_nnz[i] = n;
+        }
+    });
+    std::vector<int> bsr_offsets(P + 1, 0);
+    for (int i = 0; i < P; ++i) bsr_offsets[i + 1] = bsr_offsets[i] + row_nnz[i];
+    const int64_t nnzb = bsr_offsets[P];
+    h.nnzb = nnzb;
+    std::vector<int> bsr_columns(nnzb), slot_cptr(nnzb + 1);
+    slot_cptr[nnzb] = (int)nvalid;
+    parallel_for(P, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            int slot = bsr_offsets[i] - 1, prev = -1;
+            for (int64_t p = row_ptr[i]; p < row_ptr[i + 1]; ++p) {
+                int c = trip_cols[contrib[p]];
+                if (c != prev) {
+                    ++slot;
+                    bsr_columns[slot] = c;
+                    slot_cptr[slot] = (int)p;
+                    prev = c;
+                }
+            }
+        }
+    });
+
+    // ---- SELL-32 layout, sliced per scene
+    std::vector<int> slice_ptr(1, 0), slice_scene, scene_slice0(nscenes + 1, 0);
+    std::vector<int2> slice_meta;
+    for (int s = 0; s < nscenes; ++s) {
+        scene_slice0[s] = (int)slice_meta.size();
+        for (int64_t r0 = scenes[s]; r0 < scenes[s + 1]; r0 += fem::kSlice) {
+            int n = (int)std::min<int64_t>(fem::kSlice, scenes[s + 1] - r0);
+            int w = 0;
+            for (int l = 0; l < n; ++l) w = std::max(w, row_nnz[r0 + l]);
+            slice_meta.push_back(make_int2((int)r0, n));
+            slice_scene.push_back(s);
+            slice_ptr.push_back(slice_ptr.back() + w);
+        }
+    }
+    scene_slice0[nscenes] = (int)slice_meta.size();
+    h.nslices = (int)slice_meta.size();
+    const int64_t nsell = (int64_t)slice_ptr.back() * fem::kSlice;
+    h.nsell = nsell;
+    std::vector<int> sell_slot(nsell, -1), sell_row(nsell, -1), scol(nsell, 0), slot_sell(nnzb);
+    std::vector<unsigned> row_info(P);
+    parallel_for(h.nslices, [&](int64_t lo, int64_t hi) {
+        for (int64_t sl = lo; sl < hi; ++sl) {
+            int w = slice_ptr[sl + 1] - slice_ptr[sl];
+            for (int l = 0; l < fem::kSlice; ++l) {
+                int r = slice_meta[sl].x + l;
+                bool live = l < slice_meta[sl].y;
+                for (int k = 0; k < w; ++k) {
+                    int64_t e = ((int64_t)slice_ptr[sl] + k) * fem::kSlice + l;
+                    if (!live) continue;
+                    sell_row[e] = r;
+                    scol[e] = r;
+                    if (k < row_nnz[r]) {
+                        int slot = bsr_offsets[r] + k;
+                        sell_slot[e] = slot;
+                        slot_sell[slot] = (int)e;
+                        scol[e] = bsr_columns[slot];
+                    }
+                }
+                if (live) row_info[r] = (unsigned)row_nnz[r] | (fixed_mask[r] ? fem::kFixedBit : 0u);
+            }
+        }
+    });
+
+    // ---- node incidence (element-force slots, springs), ascending order
+    std::vector<int> elem_ptr(P + 1, 0), spring_ptr(P + 1, 0);
+    for (int64_t k = 0; k < 4 * (int64_t)T; ++k) elem_ptr[d->tet_indices[k] + 1]++;
+    for (int64_t k = 0; k < 8 * (int64_t)Hn; ++k) elem_ptr[d->hex_indices[k] + 1]++;
+    for (int s = 0; s < S; ++s) {
+        int a = d->spring_indices[2 * s], bb = d->spring_indices[2 * s + 1];
+        if (a >= 0) spring_ptr[a + 1]++;
+        if (bb >= 0 && bb != a) spring_ptr[bb + 1]++;
+    }
+    for (int i = 0; i < P; ++i) {
+        elem_ptr[i + 1] += elem_ptr[i];
+        spring_ptr[i + 1] += spring_ptr[i];
+    }
+    std::vector<int> elem_ent(elem_ptr[P]), spring_ent(spring_ptr[P]);
+    {
+        std::vector<int> pos(elem_ptr.begin(), elem_ptr.end() - 1);
+        for (int64_t k = 0; k < 4 * (int64_t)T; ++k) elem_ent[pos[d->tet_indices[k]]++] = (int)k;
+        for (int64_t k = 0; k < 8 * (int64_t)Hn; ++k) elem_ent[pos[d->hex_indices[k]]++] = (int)(4 * (int64_t)T + k);
+        std::vector<int> sp(spring_ptr.begin(), spring_ptr.end() - 1);
+        for (int s = 0; s < S; ++s) {
+            int a = d->spring_indices[2 * s], bb = d->spring_indices[2 * s + 1];
+            if (a >= 0) spring_ent[sp[a]++] = 2 * s;
+            if (bb >= 0 && bb != a) spring_ent[sp[bb]++] = 2 * s + 1;
+        }
+    }
+
+    // ---- device data
+    std::vector<float> radius(P, 0.0f);
+    if (d->particle_radius) std::copy(d->particle_radius, d->particle_radius + P, radius.begin());
+    std::vector<int> flags(P, 1);
+    if (d->particle_flags) std::copy(d->particle_flags, d->particle_flags + P, flags.begin());
+    h.rest = b.upload(d->particle_q, 3 * (size_t)P);
+    h.mass = b.upload(d->particle_mass, P);
+    h.inv_mass = b.upload(d->particle_inv_mass, P);
+    h.radius = b.upload(radius);
+    h.flags = b.upload(flags);
+    h.fixed_mask = b.upload(fixed_mask);
+    h.fixed_idx = b.upload(d->fixed_indices, (size_t)std::max(0, d->fixed_count));
+    h.gravity_dev = b.alloc<float>(3);
+    h.tet_idx = reinterpret_cast<int4*>(b.upload(d->tet_indices, 4 * (size_t)T));
+    h.tet_pose = b.upload(d->tet_poses, 9 * (size_t)T);
+    h.tet_mat = b.upload(d->tet_materials, 3 * (size_t)T);
+    h.hex_idx = b.upload(d->hex_indices, 8 * (size_t)Hn);
+    h.hex_invJ = b.upload(d->hex_inv_J0, 72 * (size_t)Hn);
+    h.hex_detw = b.upload(d->hex_det_J0_w, 8 * (size_t)Hn);
+    h.hex_mat = b.upload(d->hex_materials, 3 * (size_t)Hn);
+    h.spring_idx = b.upload(d->spring_indices, 2 * (size_t)S);
+    h.spring_rest = b.upload(d->spring_rest_length, S);
+    h.spring_ke = b.upload(d->spring_stiffness, S);
+    h.spring_kd = b.upload(d->spring_damping, S);
+    h.node_elem_ptr = b.upload(elem_ptr);
+    h.node_elem_ent = b.upload(elem_ent);
+    h.node_spring_ptr = b.upload(spring_ptr);
+    h.node_spring_ent = b.upload(spring_ent);
+    h.elem_force = b.alloc<float4>(4 * (size_t)T + 8 * (size_t)Hn);
+    h.q4 = b.alloc<float4>(P);
+    h.v4 = b.alloc<float4>(P);
+    h.trip_vals = b.alloc<float>(9 * (size_t)ntrip);
+    h.trip_rows = b.upload(trip_rows);
+    h.trip_cols = b.upload(trip_cols);
+    h.sell_slot = b.upload(sell_slot);
+    h.sell_row = b.upload(sell_row);
+    h.slot_cptr = b.upload(slot_cptr);
+    h.slot_contrib = b.upload(contrib);
+    h.bsr_offsets = b.upload(bsr_offsets);
+    h.bsr_columns = b.upload(bsr_columns);
+    h.slot_sell = b.upload(slot_sell);
+    h.valA = b.alloc<float4>(nsell);
+    h.valB = b.alloc<float4>(nsell);
+    h.valC = b.alloc<float>(nsell);
+    h.scol = b.upload(scol);
+    h.slice_ptr = b.upload(slice_ptr);
+    h.slice_meta = b.upload(slice_meta);
+    h.slice_scene = b.upload(slice_scene);
+    h.scene_slice0 = b.upload(scene_slice0);
+    h.row_info = b.upload(row_info);
+    h.minv = b.alloc<float>(9 * (size_t)P);
+    h.x = b.alloc<float4>(P);
+    h.r = b.alloc<float4>(P);
+    h.z = b.alloc<float4>(P);
+    h.p0 = b.alloc<float4>(P);
+    h.p1 = b.alloc<float4>(P);
+    h.y = b.alloc<float4>(P);
+    if (d->velocity_increment != nullptr) {
+        h.dv = d->velocity_increment;
+        h.dv_owned = false;
+        if (P > 0) cudaMemset(h.dv, 0, sizeof(float) * 3 * (size_t)P);
+    } else {
+        h.dv = b.alloc<float>(3 * (size_t)P);
+    }
+    h.barrier = b.alloc<unsigned>(1);
+    h.status = b.alloc<int>(1);
+    h.scene_stats = b.alloc<fem::SceneStats>(nscenes);
+    h.cum_iters = b.alloc<long long>(nscenes);
+    if (b.status != FEM_OK) {
+        int code = b.status;
+        g_error = h.last_error;
+        fem_destroy(H);
+        return code;
+    }
+    if (P > 0) {
+        cudaError_t ge = cudaMemcpy(h.gravity_dev, d->gravity, sizeof(float) * 3, cudaMemcpyHostToDevice);
+        if (ge != cudaSuccess) {
+            fem_destroy(H);
+            return cuda_status(ge);
+        }
+    }
+
+    // ---- launch configuration and deterministic-reduction segment tables
+    cudaError_t err = P > 0 ? fem::pcg_configure(h) : cudaSuccess;
+    if (err != cudaSuccess) {
+        int code = cuda_status(err);
+        fem_destroy(H);
+        return code;
+    }
+    if (P > 0) {
+        std::vector<int> cta_seg_base(h.grid, 0), cta_first_scene(h.grid, nscenes), scene_seg0(nscenes + 1, 0);
+        int nseg = 0, L = h.slices_per_cta;
+        std::vector<int> seg_scene;
+        for (int c = 0; c < h.grid; ++c) {
+            int first = c * L, last = std::min(first + L, h.nslices);
+            cta_seg_base[c] = nseg;
+            if (first >= last) continue;
+            cta_first_scene[c] = slice_scene[first];
+            for (int s = slice_scene[first]; s <= slice_scene[last - 1]; ++s) {
+                seg_scene.push_back(s);
+                ++nseg;
+            }
+        }
+        // segments are ordered by (cta, scene), which is also scene-major
+        std::vector<int> count(nscenes, 0);
+        for (int s : seg_scene) count[s]++;
+        for (int s = 0; s < nscenes; ++s) scene_seg0[s + 1] = scene_seg0[s] + count[s];
+        h.nseg = nseg;
+        h.cta_seg_base = b.upload(cta_seg_base);
+        h.cta_first_scene = b.upload(cta_first_scene);
+        h.scene_seg0 = b.upload(scene_seg0);
+        h.seg_part = b.alloc<double>(3 * (size_t)std::max(1, nseg));
+    }
+    if (b.status != FEM_OK) {
+        int code = b.status;
+        g_error = h.last_error;
+        fem_destroy(H);
+        return code;
+    }
+
+    // ---- initial assembly at the construction positions (solver.py:330-341)
+    cudaStream_t s0 = nullptr;
+    err = fem::launch_node_prepare(h, h.rest, nullptr, false, false, false, s0);
+    if (err == cudaSuccess) err = fem::launch_constant_blocks(h, h.dt, s0);
+    if (err == cudaSuccess) err = fem::launch_element_tangent(h, h.dt, s0);
+    if (err == cudaSuccess) err = fem::launch_gather(h, s0);
+    if (err == cudaSuccess) err = cudaDeviceSynchronize();
+    if (err != cudaSuccess) {
+        int code = cuda_status(err);
+        fem_destroy(H);
+        return code;
+    }
+    *out = H;
+    return FEM_OK;
+}
+
+int fem_destroy(FemHandle* H) {
+    if (H == nullptr) return FEM_OK;
+    DeviceGuard g(H->device);
+    for (cudaEvent_t e : H->h.timing_events) cudaEventDestroy(e);
+    for (void* p : H->h.allocations) cudaFree(p);
+    delete H;
+    return FEM_OK;
+}
+
+int fem_step(FemHandle* H, float* q_in, float* v_in, float* q_out, float* v_out, float* f_ws,
+             const float* external_forces, const float* activations, const float* gravity, float dt, void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    if (h.P == 0) return FEM_OK;
+    if (!q_in || !v_in || !q_out || !v_out || !f_ws) return set_error(FEM_ERR_BAD_ARG, "null state pointer");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return set_error(FEM_ERR_BAD_ARG, "dt must be finite and positive");
+    if (h.enable_act && h.T > 0 && activations == nullptr)
+        return set_error(FEM_ERR_BAD_ARG, "tet activations are enabled but none were passed");
+    DeviceGuard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = fem::launch_node_prepare(h, q_in, v_in, true, true, true, s);
+    if (err == cudaSuccess) err = fem::launch_element_forces(h, activations, s);
+    if (err == cudaSuccess)
+        err = fem::launch_node_forces(h, external_forces, gravity, dt, 0x3f, true, f_ws, s);
+    bool timed = false;
+    if (err == cudaSuccess && h.timing) {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cap);
+        if (cap == cudaStreamCaptureStatusNone) {
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            h.timing_events.push_back(e0);
+            h.timing_events.push_back(e1);
+            cudaEventRecord(e0, s);
+            timed = true;
+        }
+    }
+    if (err == cudaSuccess) err = fem::launch_pcg(h, dt, 1, q_out, v_out, f_ws, s);
+    if (timed) cudaEventRecord(h.timing_events.back(), s);
+    return cuda_status(err, &h);
+}
+
+int fem_set_timing(FemHandle* H, int32_t enable) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    H->h.timing = enable != 0;
+    return FEM_OK;
+}
+
+int fem_get_timing(FemHandle* H, double* pcg_ms_total, int64_t* launches) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    DeviceGuard g(H->device);
+    double total = 0.0;
+    int64_t n = 0;
+    cudaError_t err = cudaSuccess;
+    for (size_t k = 0; k + 1 < h.timing_events.size(); k += 2) {
+        cudaEvent_t e0 = h.timing_events[k], e1 = h.timing_events[k + 1];
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        total += ms;
+        ++n;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    h.timing_events.clear();
+    if (pcg_ms_total) *pcg_ms_total = total;
+    if (launches) *launches = n;
+    return cuda_status(err, &h);
+}
+
+int fem_refresh_tangent(FemHandle* H, float* q, float dt, void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return set_error(FEM_ERR_BAD_ARG, "refresh_tangent dt must be finite and positive");
+    if (h.P == 0) {
+        h.dt = dt;
+        return FEM_OK;
+    }
+    if (q == nullptr) return set_error(FEM_ERR_BAD_ARG, "null positions");
+    DeviceGuard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = cudaSuccess;
+    if (dt != h.dt) {  // solver.py:816-822: rebuild the dt-dependent blocks, clear the warm start
+        err = cudaMemsetAsync(h.dv, 0, sizeof(float) * 3 * (size_t)h.P, s);
+        if (err == cudaSuccess) err = fem::launch_constant_blocks(h, dt, s);
+    }
+    if (err == cudaSuccess) err = fem::launch_node_prepare(h, q, nullptr, true, false, false, s);
+    if (err == cudaSuccess) err = fem::launch_element_tangent(h, dt, s);
+    if (err == cudaSuccess) err = fem::launch_gather(h, s);
+    if (err == cudaSuccess) h.dt = dt;
+    return cuda_status(err, &h);
+}
+
+int fem_rebuild_element_blocks(FemHandle* H, float* q, float dt, void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return set_error(FEM_ERR_BAD_ARG, "dt must be finite and positive");
+    if (h.P == 0) return FEM_OK;
+    if (q == nullptr) return set_error(FEM_ERR_BAD_ARG, "null positions");
+    DeviceGuard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = fem::launch_node_prepare(h, q, nullptr, true, false, false, s);
+    if (err == cudaSuccess) err = fem::launch_element_tangent(h, dt, s);
+    if (err == cudaSuccess) err = fem::launch_gather(h, s);
+    return cuda_status(err, &h);
+}
+
+int fem_refresh_preconditioner(FemHandle* H, void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    DeviceGuard g(H->device);
+    // The inverse blocks are written by the assembly epilogue; re-running the
+    // gather refreshes them in place from the current triplet values.
+    return cuda_status(fem::launch_gather(H->h, (cudaStream_t)stream), &H->h);
+}
+
+int fem_set_tolerance(FemHandle* H, float tolerance) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    if (!(tolerance > 0.0f) || !std::isfinite(tolerance))
+        return set_error(FEM_ERR_BAD_ARG, "linear_solver_tolerance must be finite and positive");
+    H->h.tol = tolerance;
+    return FEM_OK;
+}
+
+int fem_set_wait_limit(FemHandle* H, int64_t nanoseconds) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    if (nanoseconds < 0) return set_error(FEM_ERR_BAD_ARG, "wait limit must be non-negative");
+    H->h.wait_limit_ns = nanoseconds;
+    return FEM_OK;
+}
+
+int fem_set_maxiter(FemHandle* H, int32_t maxiter) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    if (maxiter < 0) return set_error(FEM_ERR_BAD_ARG, "linear_solver_maxiter must be non-negative");
+    H->h.maxiter = maxiter;
+    return FEM_OK;
+}
+
+int fem_reset(FemHandle* H, void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    DeviceGuard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = cudaSuccess;
+    if (h.P > 0) err = cudaMemsetAsync(h.dv, 0, sizeof(float) * 3 * (size_t)h.P, s);
+    if (err == cudaSuccess && h.status) err = cudaMemsetAsync(h.status, 0, sizeof(int), s);
+    return cuda_status(err, &h);
+}
+
+float* fem_velocity_increment_ptr(FemHandle* H) { return H ? H->h.dv : nullptr; }
+
+int fem_get_stats(FemHandle* H, FemStats* stats, int32_t* scene_iterations, void* stream) {
+    if (H == nullptr || stats == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle or stats");
+    Handle& h = H->h;
+    DeviceGuard g(H->device);
+    std::memset(stats, 0, sizeof(FemStats));
+    stats->scene_count = h.nscenes;
+    if (h.P == 0) return FEM_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) return cuda_status(err, &h);
+    std::vector<fem::SceneStats> sc(h.nscenes);
+    std::vector<long long> cum(h.nscenes);
+    int status = 0;
+    err = cudaMemcpy(sc.data(), h.scene_stats, sizeof(fem::SceneStats) * sc.size(), cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemcpy(&status, h.status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess)
+        err = cudaMemcpy(cum.data(), h.cum_iters, sizeof(long long) * cum.size(), cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_status(err, &h);
+    stats->status = status;
+    stats->total_iterations = 0;
+    for (long long c : cum) stats->total_iterations += c;
+    stats->max_iterations = 0;
+    stats->min_iterations = sc.empty() ? 0 : INT32_MAX;
+    float worst = 0.0f;
+    for (int k = 0; k < h.nscenes; ++k) {
+        stats->max_iterations = std::max(stats->max_iterations, sc[k].iterations);
+        stats->min_iterations = std::min(stats->min_iterations, sc[k].iterations);
+        float rel = sc[k].bb > 0.0f ? std::sqrt(sc[k].rr / sc[k].bb) : 0.0f;
+        worst = std::max(worst, rel);
+        if (!sc[k].converged) stats->unconverged_scenes++;
+        if (scene_iterations) scene_iterations[k] = sc[k].iterations;
+    }
+    stats->max_relative_residual = worst;
+    if (status & fem::kStatusTimeout) return FEM_ERR_TIMEOUT;
+    if (status & fem::kStatusNonFinite) return FEM_ERR_NON_FINITE;
+    return FEM_OK;
+}
+
+int fem_eval_forces(FemHandle* H, const float* q, const float* v, const float* activations, const float* gravity,
+                    int32_t terms, float* out, void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    if (h.P == 0) return FEM_OK;
+    if (!q || !v || !out) return set_error(FEM_ERR_BAD_ARG, "null pointer");
+    DeviceGuard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = fem::launch_node_prepare(h, const_cast<float*>(q), const_cast<float*>(v), false, true, false, s);
+    if (err == cudaSuccess) err = fem::launch_element_forces(h, activations, s);
+    if (err == cudaSuccess) err = fem::launch_node_forces(h, nullptr, gravity, 1.0f, terms, false, out, s);
+    return cuda_status(err, &h);
+}
+
+int fem_matrix_info(FemHandle* H, int64_t* nnzb, int64_t* triplet_count, int64_t* stored_blocks) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    if (nnzb) *nnzb = H->h.nnzb;
+    if (triplet_count) *triplet_count = H->h.ntrip;
+    if (stored_blocks) *stored_blocks = H->h.nsell;
+    return FEM_OK;
+}
+
+int fem_export_bsr(FemHandle* H, int32_t* offsets, int32_t* columns, float* values, void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    DeviceGuard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = cudaSuccess;
+    if (offsets && h.P > 0)
+        err = cudaMemcpyAsync(offsets, h.bsr_offsets, sizeof(int) * (h.P + 1), cudaMemcpyDeviceToDevice, s);
+    if (err == cudaSuccess && columns && h.nnzb > 0)
+        err = cudaMemcpyAsync(columns, h.bsr_columns, sizeof(int) * h.nnzb, cudaMemcpyDeviceToDevice, s);
+    if (err == cudaSuccess && values) err = fem::launch_export_bsr(h, values, s);
+    return cuda_status(err, &h);
+}
+
+int fem_export_preconditioner(FemHandle* H, float* inverse_blocks, void* stream) {
+    if (H == nullptr || inverse_blocks == nullptr) return set_error(FEM_ERR_BAD_ARG, "null pointer");
+    Handle& h = H->h;
+    DeviceGuard g(H->device);
+    if (h.P == 0) return FEM_OK;
+    return cuda_status(cudaMemcpyAsync(inverse_blocks, h.minv, sizeof(float) * 9 * (size_t)h.P,
+                                       cudaMemcpyDeviceToDevice, (cudaStream_t)stream),
+                       &h);
+}
+
+int fem_export_triplets(FemHandle* H, int32_t* rows, int32_t* columns, float* values, void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    DeviceGuard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = cudaSuccess;
+    if (rows && h.ntrip)
+        err = cudaMemcpyAsync(rows, h.trip_rows, sizeof(int) * h.ntrip, cudaMemcpyDeviceToDevice, s);
+    if (err == cudaSuccess && columns && h.ntrip)
+        err = cudaMemcpyAsync(columns, h.trip_cols, sizeof(int) * h.ntrip, cudaMemcpyDeviceToDevice, s);
+    if (err == cudaSuccess && values) err = fem::launch_export_triplets(h, values, s);
+    return cuda_status(err, &h);
+}
+
+}  // extern "C"

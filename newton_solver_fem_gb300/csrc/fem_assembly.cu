@@ -1,0 +1,86 @@
+// Deterministic BSR assembly of A = M + h^2 K~ + h C_s into the SELL-32 layout.
+//
+// The reference writes every element/constant block as a triplet and either
+// sorts them (bsr_set_from_triplets) or scatters them with float atomics into
+// precomputed slots (sparse_update.py:9-59).  Here the setup builds, once, the
+// list of contributing triplets of every matrix slot in ascending triplet order
+// (the reference layout [P | 2S | 16T | 64H]), and each refresh sums that list
+// in order: no atomics, bit-identical results run to run.  The thread that
+// owns a diagonal slot also writes that row's preconditioner block
+// (kernels.py:1836-1849 fused into the assembly epilogue).
+#include "fem_internal.cuh"
+#include "fem_math.cuh"
+
+namespace fem {
+namespace {
+
+__global__ void gather_kernel(int64_t nsell, const int* __restrict__ sell_slot, const int* __restrict__ sell_row,
+                              const int* __restrict__ scol, const int* __restrict__ cptr,
+                              const int* __restrict__ contrib, const float* __restrict__ trip,
+                              float4* __restrict__ valA, float4* __restrict__ valB, float* __restrict__ valC,
+                              float* __restrict__ minv, int precond) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nsell) return;
+    int slot = sell_slot[e];
+    if (slot < 0) return;  // padding: zero since setup
+    float b[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) b[k] = 0.0f;
+    for (int c = cptr[slot]; c < cptr[slot + 1]; ++c) {
+        const float* t = trip + 9 * (int64_t)contrib[c];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) b[k] += t[k];
+    }
+    valA[e] = make_float4(b[0], b[1], b[2], b[3]);
+    valB[e] = make_float4(b[4], b[5], b[6], b[7]);
+    valC[e] = b[8];
+    int row = sell_row[e];
+    if (scol[e] == row) {
+        float inv[9];
+        if (precond == FEM_PRECOND_DIAG) inverse_point_diagonal(b, inv);
+        else inverse_diagonal_block(b, inv);
+        float* o = minv + 9 * (int64_t)row;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) o[k] = inv[k];
+    }
+}
+
+__global__ void export_bsr_kernel(int64_t nnzb, const int* __restrict__ slot_sell, const float4* __restrict__ valA,
+                                  const float4* __restrict__ valB, const float* __restrict__ valC,
+                                  float* __restrict__ out) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nnzb) return;
+    int64_t e = slot_sell[j];
+    float4 a = valA[e], b = valB[e];
+    float* o = out + 9 * j;
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+    o[8] = valC[e];
+}
+
+}  // namespace
+
+cudaError_t launch_gather(Handle& h, cudaStream_t s) {
+    if (h.nsell == 0) return cudaSuccess;
+    int threads = 256;
+    int64_t blocks = (h.nsell + threads - 1) / threads;
+    gather_kernel<<<(unsigned)blocks, threads, 0, s>>>(h.nsell, h.sell_slot, h.sell_row, h.scol, h.slot_cptr,
+                                                       h.slot_contrib, h.trip_vals, h.valA, h.valB, h.valC, h.minv,
+                                                       h.precond);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_bsr(Handle& h, float* values, cudaStream_t s) {
+    if (h.nnzb == 0) return cudaSuccess;
+    int threads = 256;
+    int64_t blocks = (h.nnzb + threads - 1) / threads;
+    export_bsr_kernel<<<(unsigned)blocks, threads, 0, s>>>(h.nnzb, h.slot_sell, h.valA, h.valB, h.valC, values);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_triplets(Handle& h, float* values, cudaStream_t s) {
+    if (h.ntrip == 0) return cudaSuccess;
+    return cudaMemcpyAsync(values, h.trip_vals, sizeof(float) * 9 * (size_t)h.ntrip, cudaMemcpyDeviceToDevice, s);
+}
+
+}  // namespace fem

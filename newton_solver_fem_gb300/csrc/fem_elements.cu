@@ -1,0 +1,653 @@
+// Element and node kernels of the FEM hot path (sm_103a):
+//   node_prepare      fixed-node restore + float4 packing of q, v and the CG warm start
+//   tet_force         Stable Neo-Hookean Tet4 force + Rayleigh damping (+ activation), per element
+//   hex_force         Q1 Hex8 force, 8 lanes per element (one per Gauss point)
+//   node_forces       deterministic element->node gather + springs, ground, gravity, damping,
+//                     and the h-scaled sum in the reference's term order
+//   constant_blocks   mass + spring diagonal and spring off-diagonal triplet blocks
+//   tet_tangent       16 PSD blocks per tet (per-tet factors staged in shared memory)
+//   hex_tangent       64 PSD blocks per hex (Gauss-point data computed once per element)
+// No float atomics anywhere: every sum runs in a fixed order.
+#include "fem_internal.cuh"
+#include "fem_math.cuh"
+
+namespace fem {
+
+__constant__ float c_dNdxi[8][8][3];  // [gauss point][node][d/dxi, d/deta, d/dzeta]
+
+namespace {
+
+__device__ __forceinline__ float3 load3(const float* p, int i) { return f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+__device__ __forceinline__ void store3(float* p, int i, float3 v) {
+    p[3 * i] = v.x;
+    p[3 * i + 1] = v.y;
+    p[3 * i + 2] = v.z;
+}
+
+__global__ void node_prepare_kernel(int P, float* __restrict__ q, float* __restrict__ v,
+                                    const unsigned char* __restrict__ fixed_mask, const float* __restrict__ rest,
+                                    const float* __restrict__ dv, float4* __restrict__ q4, float4* __restrict__ v4,
+                                    float4* __restrict__ x4, int restore, int pack_v, int pack_x) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    bool fx = fixed_mask[i] != 0;
+    if (!restore) {  // plain packing, caller arrays untouched
+        q4[i] = f4(load3(q, i));
+        if (pack_v) v4[i] = f4(load3(v, i));
+        if (pack_x) x4[i] = fx ? make_float4(0.f, 0.f, 0.f, 0.f) : f4(load3(dv, i));
+        return;
+    }
+    float3 qi;
+    if (fx) {  // fixed_particles.py:11-21 restore q (and v) in place
+        qi = load3(rest, i);
+        store3(q, i, qi);
+    } else {
+        qi = load3(q, i);
+    }
+    q4[i] = f4(qi);
+    if (pack_v) {
+        float3 vi = f3(0.f, 0.f, 0.f);
+        if (fx) store3(v, i, vi);
+        else vi = load3(v, i);
+        v4[i] = f4(vi);
+    }
+    if (pack_x) x4[i] = fx ? make_float4(0.f, 0.f, 0.f, 0.f) : f4(load3(dv, i));
+}
+
+// Reference kernels.py:511-632 (force) and 484-508 (activation).  Writes the
+// restoring force of each corner into out[4 t + a].
+__global__ void tet_force_kernel(int T, const int4* __restrict__ idx, const float* __restrict__ pose,
+                                 const float* __restrict__ mat, const float4* __restrict__ q4,
+                                 const float4* __restrict__ v4, const float* __restrict__ act, float lo, float hi,
+                                 float4* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    int4 n = idx[t];
+    float k_mu = mat[3 * t], k_lambda = mat[3 * t + 1], k_damp = mat[3 * t + 2];
+    float4* o = out + 4 * t;
+    if (k_mu == 0.0f && k_lambda == 0.0f && k_damp == 0.0f) {
+        float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        o[0] = zero; o[1] = zero; o[2] = zero; o[3] = zero;
+        return;
+    }
+    float3 x0 = xyz(q4[n.x]), x1 = xyz(q4[n.y]), x2 = xyz(q4[n.z]), x3 = xyz(q4[n.w]);
+    float3 v0 = xyz(v4[n.x]), v1 = xyz(v4[n.y]), v2 = xyz(v4[n.z]), v3 = xyz(v4[n.w]);
+    float3 x10 = x1 - x0, x20 = x2 - x0, x30 = x3 - x0;
+    float3 v10 = v1 - v0, v20 = v2 - v0, v30 = v3 - v0;
+    M3 Dm;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Dm.m[k / 3][k % 3] = pose[9 * t + k];
+    float inv_rest_volume = det3(Dm) * 6.0f;
+    float rest_volume = 1.0f / inv_rest_volume;
+    float alpha = 1.0f + k_mu / k_lambda - k_mu / (4.0f * k_lambda);
+    float mu = k_mu * rest_volume, lam = k_lambda * rest_volume, damp = k_damp * rest_volume;
+    M3 F = clamp_stretch(matmul(from_cols(x10, x20, x30), Dm), lo, hi);
+    M3 dFdt = matmul(from_cols(v10, v20, v30), Dm);
+    float3 c0 = col(F, 0), c1 = col(F, 1), c2 = col(F, 2);
+    float Ic = dot3(c0, c0) + dot3(c1, c1) + dot3(c2, c2);
+    float sdev = mu * (1.0f - 1.0f / (Ic + 1.0f));
+    M3 P;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) P.m[i][j] = F.m[i][j] * sdev + dFdt.m[i][j] * damp;
+    M3 Hm = matmulT(P, Dm);
+    float3 f1 = col(Hm, 0), f2 = col(Hm, 1), f3v = col(Hm, 2);
+    float J = fmaxf(det3(F), 0.01f);
+    float s = inv_rest_volume / 6.0f;
+    float3 d1 = cross3(x20, x30) * s, d2 = cross3(x30, x10) * s, d3 = cross3(x10, x20) * s;
+    float f_volume = (J - alpha) * lam;
+    float f_damp = (dot3(d1, v10) + dot3(d2, v20) + dot3(d3, v30)) * damp;
+    float ft = f_volume + f_damp;
+    f1 = f1 + d1 * ft;
+    f2 = f2 + d2 * ft;
+    f3v = f3v + d3 * ft;
+    float3 f0 = -(f1 + f2 + f3v);
+    // restoring force = -f_a (the reference subtracts f_a from the buffer)
+    float3 r0 = -f0, r1 = -f1, r2 = -f2, r3 = -f3v;
+    if (act != nullptr) {
+        float sc = k_lambda * act[t] / 6.0f;
+        float3 fb = cross3(x2 - x0, x3 - x0) * sc;
+        float3 fc = cross3(x3 - x0, x1 - x0) * sc;
+        float3 fd = cross3(x1 - x0, x2 - x0) * sc;
+        r0 = r0 + (fb + fc + fd);
+        r1 = r1 - fb;
+        r2 = r2 - fc;
+        r3 = r3 - fd;
+    }
+    o[0] = f4(r0);
+    o[1] = f4(r1);
+    o[2] = f4(r2);
+    o[3] = f4(r3);
+}
+
+// Reference kernels.py:1481-1601.  Lane g of an 8-lane group evaluates Gauss
+// point g of one hex; the 8 per-point corner forces are then summed over the
+// group with a fixed butterfly, lane a keeping corner a.
+__global__ void hex_force_kernel(int H, const int* __restrict__ idx, const float* __restrict__ invJ,
+                                 const float* __restrict__ detw, const float* __restrict__ mat,
+                                 const float4* __restrict__ q4, const float4* __restrict__ v4, float lo, float hi,
+                                 float4* __restrict__ out) {
+    int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    int h = gid >> 3, g = gid & 7;
+    bool live = h < H;
+    int he = live ? h : H - 1;
+    int node = idx[8 * he + g];
+    float3 xg = xyz(q4[node]), vg = xyz(v4[node]);
+    float k_mu = mat[3 * he], k_lambda = mat[3 * he + 1], k_damp = mat[3 * he + 2];
+    float alpha = 1.0f + k_mu / k_lambda - k_mu / (4.0f * k_lambda);
+    M3 iJ;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) iJ.m[k / 3][k % 3] = invJ[(8 * he + g) * 9 + k];
+    float w = detw[8 * he + g];
+    int base = threadIdx.x & ~7 & 31;
+    float3 xa[8], va[8], dN[8];
+    M3 F, dFdt;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) F.m[i][j] = dFdt.m[i][j] = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        xa[a] = f3(__shfl_sync(0xffffffffu, xg.x, base + a), __shfl_sync(0xffffffffu, xg.y, base + a),
+                   __shfl_sync(0xffffffffu, xg.z, base + a));
+        va[a] = f3(__shfl_sync(0xffffffffu, vg.x, base + a), __shfl_sync(0xffffffffu, vg.y, base + a),
+                   __shfl_sync(0xffffffffu, vg.z, base + a));
+        float3 d = f3(c_dNdxi[g][a][0], c_dNdxi[g][a][1], c_dNdxi[g][a][2]);
+        dN[a] = mulT(iJ, d);  // inv_J0^T dN/dxi
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            float xi = i == 0 ? xa[a].x : (i == 1 ? xa[a].y : xa[a].z);
+            float vi = i == 0 ? va[a].x : (i == 1 ? va[a].y : va[a].z);
+            F.m[i][0] += xi * dN[a].x;
+            F.m[i][1] += xi * dN[a].y;
+            F.m[i][2] += xi * dN[a].z;
+            dFdt.m[i][0] += vi * dN[a].x;
+            dFdt.m[i][1] += vi * dN[a].y;
+            dFdt.m[i][2] += vi * dN[a].z;
+        }
+    }
+    F = clamp_stretch(F, lo, hi);
+    float3 fc0 = col(F, 0), fc1 = col(F, 1), fc2 = col(F, 2);
+    float Ic = dot3(fc0, fc0) + dot3(fc1, fc1) + dot3(fc2, fc2);
+    float sdev = k_mu * (1.0f - 1.0f / (Ic + 1.0f));
+    float J = fmaxf(det3(F), 0.01f);
+    M3 cof = from_cols(cross3(fc1, fc2), cross3(fc2, fc0), cross3(fc0, fc1));
+    float vol = k_lambda * (J - alpha);
+    M3 P;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) P.m[i][j] = (F.m[i][j] * sdev + dFdt.m[i][j] * k_damp) + cof.m[i][j] * vol;
+    float3 mine = f3(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        float3 fa = mul(P, dN[a]) * w;
+#pragma unroll
+        for (int off = 1; off < 8; off <<= 1) {
+            fa.x += __shfl_xor_sync(0xffffffffu, fa.x, off);
+            fa.y += __shfl_xor_sync(0xffffffffu, fa.y, off);
+            fa.z += __shfl_xor_sync(0xffffffffu, fa.z, off);
+        }
+        if (a == g) mine = fa;
+    }
+    if (live) out[8 * h + g] = f4(-mine);
+}
+
+struct NodeForceArgs {
+    int P, T;
+    const float4* q4;
+    const float4* v4;
+    const int* elem_ptr;
+    const int* elem_ent;
+    const float4* elem_force;
+    const int* spring_ptr;
+    const int* spring_ent;
+    const int* spring_idx;
+    const float* spring_rest;
+    const float* spring_ke;
+    const float* spring_kd;
+    const float* mass;
+    const float* inv_mass;
+    const float* radius;
+    const int* flags;
+    const float* gravity;
+    const float* ext;
+    float ground[4];
+    float gke, gkd, gkf, gmu;
+    int has_ground;
+    float linear_damping;
+    float dt;
+    int terms;
+    int scale_by_dt;
+    float* out;
+};
+
+// Reference solver.py:542-589 (term order), kernels.py:176-218 (springs),
+// 1132-1195 (ground), 1273-1307 (gravity, damping).
+__global__ void node_forces_kernel(NodeForceArgs a) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.P) return;
+    float3 xi = xyz(a.q4[i]), vi = xyz(a.v4[i]);
+    float3 zero = f3(0.f, 0.f, 0.f);
+    float3 fs = zero, ft = zero, fh = zero, fg = zero, fgr = zero, fd = zero;
+    if (a.terms & FEM_TERM_SPRING) {
+        for (int e = a.spring_ptr[i]; e < a.spring_ptr[i + 1]; ++e) {
+            int ent = a.spring_ent[e];
+            int s = ent >> 1;
+            int ia = a.spring_idx[2 * s], ib = a.spring_idx[2 * s + 1];
+            if (ia < 0 || ib < 0) continue;
+            float3 xij = xyz(a.q4[ia]) - xyz(a.q4[ib]);
+            float3 vij = xyz(a.v4[ia]) - xyz(a.v4[ib]);
+            float L = len3(xij);
+            if (L < 1.0e-6f) continue;
+            float3 dir = f3(xij.x / L, xij.y / L, xij.z / L);
+            float c = L - a.spring_rest[s];
+            float dcdt = dot3(dir, vij);
+            float3 f = dir * (a.spring_ke[s] * c + a.spring_kd[s] * dcdt);
+            fs = (ent & 1) ? fs + f : fs - f;
+        }
+    }
+    if (a.terms & (FEM_TERM_TET | FEM_TERM_HEX)) {
+        int tet_end = 4 * a.T;
+        for (int e = a.elem_ptr[i]; e < a.elem_ptr[i + 1]; ++e) {
+            int ent = a.elem_ent[e];
+            float3 f = xyz(a.elem_force[ent]);
+            if (ent < tet_end) {
+                if (a.terms & FEM_TERM_TET) ft = ft + f;
+            } else if (a.terms & FEM_TERM_HEX) {
+                fh = fh + f;
+            }
+        }
+    }
+    bool active = (a.flags[i] & 1) != 0;
+    float3 grav = f3(a.gravity[0], a.gravity[1], a.gravity[2]);
+    if ((a.terms & FEM_TERM_GROUND) && a.has_ground && active) {
+        float3 n = f3(a.ground[0], a.ground[1], a.ground[2]);
+        float c = fminf(dot3(n, xi) + a.ground[3] - a.radius[i], 0.0f);
+        if (c < 0.0f) {
+            float vn = dot3(n, vi);
+            float jn = c * a.gke;
+            float jd = fminf(vn, 0.0f) * a.gkd;
+            float fn = jn + jd;
+            float3 vt = vi - n * vn;
+            float vs = len3(vt);
+            if (vs > 0.0f) vt = f3(vt.x / vs, vt.y / vs, vt.z / vs);
+            float gmag = len3(grav);
+            float inv_m = a.inv_mass[i];
+            float inv_m_safe = fmaxf(inv_m, 1e-9f);
+            float m = inv_m > 0.0f ? 1.0f / inv_m_safe : 0.0f;
+            float fn_eff = fminf(fabsf(fn), m * gmag);
+            float ftan = fminf(vs * a.gkf, a.gmu * fn_eff);
+            fg = zero - n * fn - vt * ftan;
+        }
+    }
+    if ((a.terms & FEM_TERM_GRAVITY) && active) {
+        float m = a.mass[i];
+        fgr = f3(grav.x * m, grav.y * m, grav.z * m);
+    }
+    if ((a.terms & FEM_TERM_DAMPING) && active && a.linear_damping > 0.0f) {
+        fd = vi * (-a.linear_damping * a.mass[i]);
+    }
+    float3 f;
+    if (a.scale_by_dt) {
+        float h = a.dt;
+        f = fs * h;
+        f = f + ft * h;
+        f = f + fh * h;
+        f = f + fg * h;
+        f = f + fgr * h;
+        f = f + fd * h;
+        if (a.ext != nullptr) f = f + load3(a.ext, i) * h;
+    } else {
+        f = fs + ft + fh + fg + fgr + fd;
+    }
+    store3(a.out, i, f);
+}
+
+// Reference kernels.py:294-323 (diagonal with springs), 141-153 (mass only), 326-366 (off-diagonal).
+__global__ void constant_diag_kernel(int P, const float* __restrict__ mass, const int* __restrict__ sptr,
+                                     const int* __restrict__ sent, const float* __restrict__ ke,
+                                     const float* __restrict__ kd, float dt, float* __restrict__ vals) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    float dt2 = dt * dt;
+    float d = mass[i];
+    for (int e = sptr[i]; e < sptr[i + 1]; ++e) {
+        int s = sent[e] >> 1;
+        d = d + dt * kd[s] + dt2 * ke[s];
+    }
+    float* o = vals + 9 * (size_t)i;
+    o[0] = d; o[1] = 0.f; o[2] = 0.f;
+    o[3] = 0.f; o[4] = d; o[5] = 0.f;
+    o[6] = 0.f; o[7] = 0.f; o[8] = d;
+}
+
+__global__ void constant_offdiag_kernel(int P, int S, const float* __restrict__ ke, const float* __restrict__ kd,
+                                        float dt, float* __restrict__ vals) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    float neg_off = -(dt * kd[s] + dt * dt * ke[s]);
+    for (int k = 0; k < 2; ++k) {
+        float* o = vals + 9 * ((size_t)P + 2 * (size_t)s + k);
+        o[0] = neg_off; o[1] = 0.f; o[2] = 0.f;
+        o[3] = 0.f; o[4] = neg_off; o[5] = 0.f;
+        o[6] = 0.f; o[7] = 0.f; o[8] = neg_off;
+    }
+}
+
+constexpr int kTetTangentThreads = 128;
+constexpr int kTetFactor = 40;
+
+// Reference kernels.py:635-850.  Phase 1: one thread per tet computes the
+// per-tet factors (F dm_a, dJ/dx_a, dm_a and three coefficients) into shared
+// memory.  Phase 2: 16 consecutive threads write the 16 blocks of a tet, so
+// the 576-byte block run of each element is written contiguously.
+__global__ void __launch_bounds__(kTetTangentThreads) tet_tangent_kernel(
+    int T, const int4* __restrict__ idx, const float* __restrict__ pose, const float* __restrict__ mat,
+    const float4* __restrict__ q4, float lo, float hi, float dt, int64_t trip_off, float* __restrict__ vals) {
+    __shared__ float sm[kTetTangentThreads][kTetFactor + 1];
+    int lt = threadIdx.x;
+    int t = blockIdx.x * kTetTangentThreads + lt;
+    float* fct = sm[lt];
+    if (t < T) {
+        float k_mu = mat[3 * t], k_lambda = mat[3 * t + 1];
+        if (k_mu == 0.0f && k_lambda == 0.0f && mat[3 * t + 2] == 0.0f) {
+            fct[39] = 2.0f;  // empty material: rows/cols are -1, nothing to write
+        } else {
+            M3 Dm;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Dm.m[k / 3][k % 3] = pose[9 * t + k];
+            float inv_rest_volume = det3(Dm) * 6.0f;
+            if (inv_rest_volume <= 0.0f) {
+                fct[39] = 1.0f;  // degenerate rest pose: zero blocks at valid rows
+            } else {
+                int4 n = idx[t];
+                float3 x0 = xyz(q4[n.x]), x1 = xyz(q4[n.y]), x2 = xyz(q4[n.z]), x3 = xyz(q4[n.w]);
+                float3 x10 = x1 - x0, x20 = x2 - x0, x30 = x3 - x0;
+                float rest_volume = 1.0f / inv_rest_volume;
+                float mu = k_mu * rest_volume, lam = k_lambda * rest_volume;
+                M3 F = clamp_stretch(matmul(from_cols(x10, x20, x30), Dm), lo, hi);
+                float3 c0 = col(F, 0), c1 = col(F, 1), c2 = col(F, 2);
+                float Ic = dot3(c0, c0) + dot3(c1, c1) + dot3(c2, c2);
+                float Ic1 = fmaxf(Ic + 1.0f, 1e-6f);
+                float s = 1.0f - 1.0f / Ic1;
+                float coef = mu * 2.0f / (Ic1 * Ic1);
+                float sv = inv_rest_volume / 6.0f;
+                float3 d1 = cross3(x20, x30) * sv, d2 = cross3(x30, x10) * sv, d3 = cross3(x10, x20) * sv;
+                float3 d0 = -(d1 + d2 + d3);
+                float3 m1 = row(Dm, 0), m2 = row(Dm, 1), m3 = row(Dm, 2);
+                float3 m0 = -(m1 + m2 + m3);
+                float3 dJ[4] = {d0, d1, d2, d3};
+                float3 dm[4] = {m0, m1, m2, m3};
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    float3 fd = mul(F, dm[a]);
+                    fct[3 * a] = fd.x; fct[3 * a + 1] = fd.y; fct[3 * a + 2] = fd.z;
+                    fct[12 + 3 * a] = dJ[a].x; fct[13 + 3 * a] = dJ[a].y; fct[14 + 3 * a] = dJ[a].z;
+                    fct[24 + 3 * a] = dm[a].x; fct[25 + 3 * a] = dm[a].y; fct[26 + 3 * a] = dm[a].z;
+                }
+                fct[36] = mu * s;
+                fct[37] = coef;
+                fct[38] = lam;
+                fct[39] = 0.0f;
+            }
+        }
+    }
+    __syncthreads();
+    float scale = dt * dt;
+#pragma unroll 4
+    for (int m = 0; m < 16; ++m) {
+        int b = lt + kTetTangentThreads * m;
+        int le = b >> 4, ab = b & 15;
+        int te = blockIdx.x * kTetTangentThreads + le;
+        if (te >= T) continue;
+        const float* f = sm[le];
+        float mode = f[39];
+        if (mode == 2.0f) continue;
+        float* o = vals + 9 * (trip_off + 16 * (int64_t)te + ab);
+        if (mode == 1.0f) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) o[k] = 0.0f;
+            continue;
+        }
+        int a = ab >> 2, bb = ab & 3;
+        float3 Fa = f3(f[3 * a], f[3 * a + 1], f[3 * a + 2]);
+        float3 Fb = f3(f[3 * bb], f[3 * bb + 1], f[3 * bb + 2]);
+        float3 Ja = f3(f[12 + 3 * a], f[13 + 3 * a], f[14 + 3 * a]);
+        float3 Jb = f3(f[12 + 3 * bb], f[13 + 3 * bb], f[14 + 3 * bb]);
+        float3 ma = f3(f[24 + 3 * a], f[25 + 3 * a], f[26 + 3 * a]);
+        float3 mb = f3(f[24 + 3 * bb], f[25 + 3 * bb], f[26 + 3 * bb]);
+        float diag = f[36] * dot3(ma, mb);
+        float coef = f[37], lam = f[38];
+        float fa[3] = {Fa.x, Fa.y, Fa.z}, fb[3] = {Fb.x, Fb.y, Fb.z};
+        float ja[3] = {Ja.x, Ja.y, Ja.z}, jb[3] = {Jb.x, Jb.y, Jb.z};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                float kdev = (i == j ? diag : 0.0f) + fa[i] * fb[j] * coef;
+                float kvol = ja[i] * jb[j] * lam;
+                o[3 * i + j] = (kdev + kvol) * scale;
+            }
+    }
+}
+
+constexpr int kHexPerCta = 4;
+
+// Reference kernels.py:1609-1747 with F, the clamp and cof(F) computed once
+// per Gauss point instead of once per (a, b) block.
+__global__ void __launch_bounds__(256) hex_tangent_kernel(int H, const int* __restrict__ idx,
+                                                          const float* __restrict__ invJ,
+                                                          const float* __restrict__ detw,
+                                                          const float* __restrict__ mat,
+                                                          const float4* __restrict__ q4, float lo, float hi, float dt,
+                                                          int64_t trip_off, float* __restrict__ vals) {
+    __shared__ float s_dN[kHexPerCta][8][8][3];
+    __shared__ float s_Fd[kHexPerCta][8][8][3];
+    __shared__ float s_cd[kHexPerCta][8][8][3];
+    __shared__ float s_F[kHexPerCta][8][18];
+    __shared__ float s_c[kHexPerCta][8][4];
+    __shared__ float s_x[kHexPerCta][8][3];
+    int tid = threadIdx.x;
+    int hl = tid >> 6, g = (tid >> 3) & 7, a = tid & 7;
+    int h = blockIdx.x * kHexPerCta + hl;
+    bool live = h < H;
+    if (live) {
+        const float* iJ = invJ + (8 * (int64_t)h + g) * 9;
+        float3 d = f3(c_dNdxi[g][a][0], c_dNdxi[g][a][1], c_dNdxi[g][a][2]);
+        float3 dn = f3(iJ[0] * d.x + iJ[3] * d.y + iJ[6] * d.z, iJ[1] * d.x + iJ[4] * d.y + iJ[7] * d.z,
+                       iJ[2] * d.x + iJ[5] * d.y + iJ[8] * d.z);
+        s_dN[hl][g][a][0] = dn.x;
+        s_dN[hl][g][a][1] = dn.y;
+        s_dN[hl][g][a][2] = dn.z;
+        if (g == 0) {
+            float3 xa = xyz(q4[idx[8 * (int64_t)h + a]]);
+            s_x[hl][a][0] = xa.x;
+            s_x[hl][a][1] = xa.y;
+            s_x[hl][a][2] = xa.z;
+        }
+    }
+    __syncthreads();
+    if (tid < kHexPerCta * 8) {
+        int hh = tid >> 3, gg = tid & 7;
+        int he = blockIdx.x * kHexPerCta + hh;
+        if (he < H) {
+            M3 F;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) F.m[i][j] = 0.0f;
+#pragma unroll
+            for (int aa = 0; aa < 8; ++aa)
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) F.m[i][j] += s_x[hh][aa][i] * s_dN[hh][gg][aa][j];
+            F = clamp_stretch(F, lo, hi);
+            float3 fc0 = col(F, 0), fc1 = col(F, 1), fc2 = col(F, 2);
+            float Ic = dot3(fc0, fc0) + dot3(fc1, fc1) + dot3(fc2, fc2);
+            float Ic1 = fmaxf(Ic + 1.0f, 1.0e-6f);
+            float s = 1.0f - 1.0f / Ic1;
+            float k_mu = mat[3 * (int64_t)he], k_lambda = mat[3 * (int64_t)he + 1];
+            float coef = k_mu * 2.0f / (Ic1 * Ic1);
+            M3 cof = from_cols(cross3(fc1, fc2), cross3(fc2, fc0), cross3(fc0, fc1));
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                s_F[hh][gg][k] = F.m[k / 3][k % 3];
+                s_F[hh][gg][9 + k] = cof.m[k / 3][k % 3];
+            }
+            s_c[hh][gg][0] = k_mu * s;
+            s_c[hh][gg][1] = coef;
+            s_c[hh][gg][2] = k_lambda;
+            s_c[hh][gg][3] = detw[8 * (int64_t)he + gg];
+        }
+    }
+    __syncthreads();
+    if (live) {
+        const float* Fm = s_F[hl][g];
+        float3 dn = f3(s_dN[hl][g][a][0], s_dN[hl][g][a][1], s_dN[hl][g][a][2]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            s_Fd[hl][g][a][i] = Fm[3 * i] * dn.x + Fm[3 * i + 1] * dn.y + Fm[3 * i + 2] * dn.z;
+            s_cd[hl][g][a][i] = Fm[9 + 3 * i] * dn.x + Fm[9 + 3 * i + 1] * dn.y + Fm[9 + 3 * i + 2] * dn.z;
+        }
+    }
+    __syncthreads();
+    if (!live) return;
+    int ra = (tid >> 3) & 7, cb = tid & 7;
+    float K[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) K[k] = 0.0f;
+#pragma unroll
+    for (int gg = 0; gg < 8; ++gg) {
+        float kms = s_c[hl][gg][0], coef = s_c[hl][gg][1], lam = s_c[hl][gg][2], w = s_c[hl][gg][3];
+        float dot_ab = s_dN[hl][gg][ra][0] * s_dN[hl][gg][cb][0] + s_dN[hl][gg][ra][1] * s_dN[hl][gg][cb][1] +
+                       s_dN[hl][gg][ra][2] * s_dN[hl][gg][cb][2];
+        float diag = kms * dot_ab;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                float kdev = (i == j ? diag : 0.0f) + s_Fd[hl][gg][ra][i] * s_Fd[hl][gg][cb][j] * coef;
+                float kvol = s_cd[hl][gg][ra][i] * s_cd[hl][gg][cb][j] * lam;
+                K[3 * i + j] = K[3 * i + j] + (kdev + kvol) * w;
+            }
+    }
+    float scale = dt * dt;
+    float* o = vals + 9 * (trip_off + 64 * (int64_t)h + 8 * ra + cb);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) o[k] = K[k] * scale;
+}
+
+inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
+
+}  // namespace
+
+void upload_hex_reference_table() {
+    // dN_a/dxi at Gauss point g, evaluated in float32 exactly as the
+    // reference's _hex_dN_dxi (kernels.py:1356-1419).  Once per device.
+    static bool done[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    if (done[dev]) return;
+    const float gp = 0.5773502691896258f;
+    float table[8][8][3];
+    auto sgn_xi = [](int k) { return (k == 1 || k == 2 || k == 5 || k == 6) ? 1.0f : -1.0f; };
+    auto sgn_eta = [](int k) { return (k == 2 || k == 3 || k == 6 || k == 7) ? 1.0f : -1.0f; };
+    auto sgn_zeta = [](int k) { return (k >= 4) ? 1.0f : -1.0f; };
+    for (int g = 0; g < 8; ++g) {
+        float xi = sgn_xi(g) * gp, eta = sgn_eta(g) * gp, zeta = sgn_zeta(g) * gp;
+        for (int a = 0; a < 8; ++a) {
+            float xa = sgn_xi(a), ya = sgn_eta(a), za = sgn_zeta(a);
+            table[g][a][0] = xa * (1.0f + ya * eta) * (1.0f + za * zeta) * 0.125f;
+            table[g][a][1] = (1.0f + xa * xi) * ya * (1.0f + za * zeta) * 0.125f;
+            table[g][a][2] = (1.0f + xa * xi) * (1.0f + ya * eta) * za * 0.125f;
+        }
+    }
+    if (cudaMemcpyToSymbol(c_dNdxi, table, sizeof(table)) == cudaSuccess) done[dev] = true;
+}
+
+cudaError_t launch_node_prepare(Handle& h, float* q, float* v, bool restore_fixed, bool pack_v, bool pack_x,
+                                cudaStream_t s) {
+    if (h.P == 0) return cudaSuccess;
+    node_prepare_kernel<<<blocks_for(h.P, 256), 256, 0, s>>>(h.P, q, v, h.fixed_mask, h.rest, h.dv, h.q4, h.v4, h.x,
+                                                             restore_fixed ? 1 : 0, pack_v ? 1 : 0, pack_x ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_element_forces(Handle& h, const float* activations, cudaStream_t s) {
+    if (h.T > 0) {
+        tet_force_kernel<<<blocks_for(h.T, 128), 128, 0, s>>>(h.T, h.tet_idx, h.tet_pose, h.tet_mat, h.q4, h.v4,
+                                                              h.enable_act ? activations : nullptr, h.min_stretch,
+                                                              h.max_stretch, h.elem_force);
+    }
+    if (h.H > 0) {
+        hex_force_kernel<<<blocks_for(8 * (int64_t)h.H, 256), 256, 0, s>>>(
+            h.H, h.hex_idx, h.hex_invJ, h.hex_detw, h.hex_mat, h.q4, h.v4, h.min_stretch, h.max_stretch,
+            h.elem_force + 4 * (int64_t)h.T);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity, float dt, int terms, bool scale_by_dt,
+                               float* out, cudaStream_t s) {
+    if (h.P == 0) return cudaSuccess;
+    NodeForceArgs a;
+    a.P = h.P;
+    a.T = h.T;
+    a.q4 = h.q4;
+    a.v4 = h.v4;
+    a.elem_ptr = h.node_elem_ptr;
+    a.elem_ent = h.node_elem_ent;
+    a.elem_force = h.elem_force;
+    a.spring_ptr = h.node_spring_ptr;
+    a.spring_ent = h.node_spring_ent;
+    a.spring_idx = h.spring_idx;
+    a.spring_rest = h.spring_rest;
+    a.spring_ke = h.spring_ke;
+    a.spring_kd = h.spring_kd;
+    a.mass = h.mass;
+    a.inv_mass = h.inv_mass;
+    a.radius = h.radius;
+    a.flags = h.flags;
+    a.gravity = gravity != nullptr ? gravity : h.gravity_dev;
+    a.ext = ext;
+    for (int k = 0; k < 4; ++k) a.ground[k] = h.ground[k];
+    a.gke = h.gke;
+    a.gkd = h.gkd;
+    a.gkf = h.gkf;
+    a.gmu = h.gmu;
+    a.has_ground = h.has_ground;
+    a.linear_damping = h.linear_damping;
+    a.dt = dt;
+    a.terms = terms;
+    a.scale_by_dt = scale_by_dt ? 1 : 0;
+    a.out = out;
+    node_forces_kernel<<<blocks_for(h.P, 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_constant_blocks(Handle& h, float dt, cudaStream_t s) {
+    if (h.P > 0)
+        constant_diag_kernel<<<blocks_for(h.P, 256), 256, 0, s>>>(h.P, h.mass, h.node_spring_ptr, h.node_spring_ent,
+                                                                  h.spring_ke, h.spring_kd, dt, h.trip_vals);
+    if (h.S > 0)
+        constant_offdiag_kernel<<<blocks_for(h.S, 256), 256, 0, s>>>(h.P, h.S, h.spring_ke, h.spring_kd, dt,
+                                                                     h.trip_vals);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_element_tangent(Handle& h, float dt, cudaStream_t s) {
+    int64_t tet_off = (int64_t)h.P + 2 * (int64_t)h.S;
+    if (h.T > 0)
+        tet_tangent_kernel<<<blocks_for(h.T, kTetTangentThreads), kTetTangentThreads, 0, s>>>(
+            h.T, h.tet_idx, h.tet_pose, h.tet_mat, h.q4, h.min_stretch, h.max_stretch, dt, tet_off, h.trip_vals);
+    if (h.H > 0)
+        hex_tangent_kernel<<<blocks_for(h.H, kHexPerCta), 256, 0, s>>>(
+            h.H, h.hex_idx, h.hex_invJ, h.hex_detw, h.hex_mat, h.q4, h.min_stretch, h.max_stretch, dt,
+            tet_off + 16 * (int64_t)h.T, h.trip_vals);
+    return cudaGetLastError();
+}
+
+}  // namespace fem

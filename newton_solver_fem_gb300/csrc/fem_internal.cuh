@@ -1,0 +1,188 @@
+// Internal state of a FemHandle and the launchers shared between translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "fem_gb300.h"
+
+namespace fem {
+
+constexpr int kSlice = 32;          // rows per SELL slice (one warp, thread per row)
+constexpr int kPcgThreads = 256;    // persistent PCG block size (8 warps)
+constexpr unsigned kFixedBit = 0x80000000u;  // row_info: fixed-node flag; low bits = row length
+
+// Device-side status bits (FemStats.status).
+constexpr int kStatusTimeout = 1 << 2;
+constexpr int kStatusNonFinite = 1 << 1;
+
+// Per-scene persistent solver statistics written by the PCG epilogue.
+struct SceneStats {
+    int iterations;
+    float rr;
+    float bb;
+    int converged;
+};
+
+// Everything a PCG launch needs (plain pointers, passed by value).
+struct PcgArgs {
+    // SELL-32 matrix: entry e = (slice_ptr[sl] + k) * 32 + lane
+    const float4* __restrict__ valA;  // (a00 a01 a02 a10)
+    const float4* __restrict__ valB;  // (a11 a12 a20 a21)
+    const float* __restrict__ valC;   // a22
+    const int* __restrict__ scol;     // block column
+    const int* __restrict__ slice_ptr;   // [nslices+1]
+    const int2* __restrict__ slice_meta; // [nslices] (first row, row count)
+    const int* __restrict__ slice_scene; // [nslices]
+    const unsigned* __restrict__ row_info;  // [P] length | kFixedBit
+    const float* __restrict__ minv;  // [P*9]
+    int nslices;
+    int slices_per_cta;  // L
+    // segment tables for deterministic per-scene reductions
+    const int* __restrict__ cta_seg_base;     // [grid]
+    const int* __restrict__ cta_first_scene;  // [grid]
+    const int* __restrict__ scene_slice0;     // [S+1]
+    const int* __restrict__ scene_seg0;       // [S+1]
+    int nscenes;
+    double* seg_part;  // [nseg * 3]
+    // node data
+    const float4* __restrict__ v4;     // packed velocity (fixed zeroed)
+    const float4* __restrict__ q4;     // packed positions (fixed restored)
+    const float* __restrict__ rest;    // [P*3] anchors
+    const int* __restrict__ spring_ptr;   // node -> incident springs [P+1]
+    const int* __restrict__ spring_ent;   // 2*s + endpoint
+    const int* __restrict__ spring_idx;   // [2S]
+    const float* __restrict__ spring_kd;  // [S]
+    float* f_ws;       // [P*3] in: h*sum f, out: final rhs
+    float* dv;         // [P*3] warm start in, velocity increment out
+    float* q_out;      // [P*3]
+    float* v_out;      // [P*3]
+    // CG vectors
+    float4* x;
+    float4* r;
+    float4* z;
+    float4* p0;
+    float4* p1;
+    float4* y;
+    // control
+    unsigned* barrier;
+    int* status;
+    SceneStats* scene_stats;
+    long long* cum_iters;  // [S] CG iterations summed over launches
+    int maxiter;
+    float tol;
+    float dt;
+    long long limit_ns;  // give up a barrier wait after this many ns
+    int write_state;  // 1: integrate state (step); 0: solve only
+};
+
+struct Handle {
+    // sizes
+    int P = 0, T = 0, H = 0, S = 0, nfixed = 0, nscenes = 1;
+    int64_t ntrip = 0, nnzb = 0, nsell = 0;
+    int nslices = 0;
+    // options
+    float dt = 0.f, min_stretch = 0.f, max_stretch = 0.f;
+    int has_ground = 0;
+    float ground[4] = {0, 0, 1, 0};
+    float gke = 0, gkd = 0, gkf = 0, gmu = 0, linear_damping = 0;
+    float gravity_init[3] = {0, 0, 0};
+    int enable_act = 0, precond = 0, maxiter = 50;
+    float tol = 1e-2f;
+    long long wait_limit_ns = 2000000000LL;
+    bool tangent_prepared = false;
+    // node data
+    float* rest = nullptr;
+    float* mass = nullptr;
+    float* inv_mass = nullptr;
+    float* radius = nullptr;
+    int* flags = nullptr;
+    int* fixed_idx = nullptr;
+    unsigned char* fixed_mask = nullptr;
+    float* gravity_dev = nullptr;  // construction gravity (used when the step passes none)
+    // elements
+    int4* tet_idx = nullptr;
+    float* tet_pose = nullptr;  // [T*9]
+    float* tet_mat = nullptr;   // [T*3]
+    int* hex_idx = nullptr;     // [H*8]
+    float* hex_invJ = nullptr;  // [H*72]
+    float* hex_detw = nullptr;  // [H*8]
+    float* hex_mat = nullptr;   // [H*3]
+    int* spring_idx = nullptr;  // [2S]
+    float* spring_rest = nullptr;
+    float* spring_ke = nullptr;
+    float* spring_kd = nullptr;
+    // incidence
+    int* node_elem_ptr = nullptr;  // [P+1]
+    int* node_elem_ent = nullptr;  // element-force slots
+    int* node_spring_ptr = nullptr;
+    int* node_spring_ent = nullptr;
+    // per-step scratch
+    float4* elem_force = nullptr;  // [4T + 8H]
+    float4* q4 = nullptr;
+    float4* v4 = nullptr;
+    // assembly
+    float* trip_vals = nullptr;   // [ntrip*9]
+    int* sell_slot = nullptr;     // [nsell] canonical slot or -1
+    int* slot_cptr = nullptr;     // [nnzb+1]
+    int* slot_contrib = nullptr;  // triplet ids
+    int* bsr_offsets = nullptr;   // [P+1]
+    int* bsr_columns = nullptr;   // [nnzb]
+    int* slot_sell = nullptr;     // [nnzb] canonical slot -> SELL entry
+    int* trip_rows = nullptr;     // [ntrip] (export only)
+    int* trip_cols = nullptr;
+    // SELL matrix
+    float4* valA = nullptr;
+    float4* valB = nullptr;
+    float* valC = nullptr;
+    int* scol = nullptr;
+    int* slice_ptr = nullptr;
+    int2* slice_meta = nullptr;
+    int* slice_scene = nullptr;
+    int* sell_row = nullptr;  // [nsell] row of entry (or -1 for lanes past the slice)
+    unsigned* row_info = nullptr;
+    float* minv = nullptr;  // [P*9]
+    // CG
+    float4 *x = nullptr, *r = nullptr, *z = nullptr, *p0 = nullptr, *p1 = nullptr, *y = nullptr;
+    float* dv = nullptr;
+    bool dv_owned = true;
+    // reductions / control
+    int grid = 0;
+    size_t pcg_smem = 0;
+    int slices_per_cta = 0;
+    int* cta_seg_base = nullptr;
+    int* cta_first_scene = nullptr;
+    int* scene_slice0 = nullptr;
+    int* scene_seg0 = nullptr;
+    int nseg = 0;
+    double* seg_part = nullptr;
+    unsigned* barrier = nullptr;
+    int* status = nullptr;
+    SceneStats* scene_stats = nullptr;
+    long long* cum_iters = nullptr;
+    // optional timing of PCG launches (eager launches only)
+    bool timing = false;
+    std::vector<cudaEvent_t> timing_events;  // start/end pairs
+    std::vector<void*> allocations;
+    std::string last_error;
+};
+
+// --- launchers (fem_elements.cu) ---
+cudaError_t launch_node_prepare(Handle& h, float* q, float* v, bool restore_fixed, bool pack_v, bool pack_x,
+                                cudaStream_t s);
+cudaError_t launch_element_forces(Handle& h, const float* activations, cudaStream_t s);
+cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity, float dt, int terms, bool scale_by_dt,
+                               float* out, cudaStream_t s);
+cudaError_t launch_constant_blocks(Handle& h, float dt, cudaStream_t s);
+cudaError_t launch_element_tangent(Handle& h, float dt, cudaStream_t s);
+// --- launchers (fem_assembly.cu) ---
+cudaError_t launch_gather(Handle& h, cudaStream_t s);
+cudaError_t launch_export_bsr(Handle& h, float* values, cudaStream_t s);
+cudaError_t launch_export_triplets(Handle& h, float* values, cudaStream_t s);
+// --- launchers (fem_pcg.cu) ---
+cudaError_t pcg_configure(Handle& h);
+cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s);
+
+}  // namespace fem

@@ -1,0 +1,582 @@
+// Persistent block-Jacobi PCG for A dv = h f - h^2 K v with the fixed-node
+// projection PAP + I - P (sm_103a, one cooperative launch per substep).
+//
+// Reference path (solver.py:1254-1351; implicit_predictor.py:9-41;
+// fixed_particles.py:56-73, 159-168; kernels.py:1779-1868; Warp cg):
+//   phase 0   rhs = f - sum_j A_ij (v_j - v_i) + spring damping, projected;
+//             u = rhs - (PAP + I - P) dv           [one pass over A for both]
+//   phase 1   per-scene max|rhs| -> scale (RHS normalisation); x0 = s dv,
+//             r0 = s u, z0 = M r0, ||r0||^2, r0.z0, ||b||^2
+//   loop      A:  p = z + beta p (recomputed on the fly at every gathered column,
+//                 so no separate pass), y = (PAP + I - P) p, p.y
+//             B:  x += alpha p, r -= alpha y, z = M r, ||r||^2, r.z
+//   epilogue  dv = x / s; v' = v + dv; q' = q + h v'; fixed nodes restored.
+// Two grid barriers per iteration.  Every cross-CTA sum is a fixed-order
+// reduction of per-slice partials (no atomics on data), so results are
+// deterministic and identical in every CTA.  The projection needs no column
+// mask: fixed rows of r, z and p are exactly zero, so PAP p = P A p.
+// Matrix layout: SELL-32 (slice of 32 consecutive rows of one scene, thread
+// per row), the 9 block values split into two float4 planes and one float
+// plane so that a warp streams 512 + 512 + 128 contiguous bytes per block column.
+#include <cooperative_groups.h>
+
+#include "fem_internal.cuh"
+#include "fem_math.cuh"
+
+namespace fem {
+namespace {
+
+struct SceneState {
+    double rz;
+    double atol_sq;
+    double rr;
+    double bb;
+    float scale;
+    float alpha;
+    float beta;
+    int active;
+    int iters;
+    int zero;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int ld_relaxed_int(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded grid barrier over a monotone counter (zeroed before the launch).
+// Gives up after limit_ns nanoseconds, or as soon as another CTA has given up,
+// and reports false; the caller then leaves the kernel.
+__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned nblocks, unsigned& epoch, int* status,
+                                             long long limit_ns, int* s_ok) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        epoch += 1;
+        unsigned target = epoch * nblocks;
+        __threadfence();
+        atomicAdd(counter, 1u);
+        int ok = 1;
+        unsigned long long t0 = global_ns();
+        unsigned spins = 0;
+        while (ld_acquire(counter) < target) {
+            if ((++spins & 63u) == 1u) {  // first spin, then every 64th
+                if ((ld_relaxed_int(status) & kStatusTimeout) != 0 ||
+                    (long long)(global_ns() - t0) >= limit_ns) {
+                    ok = 0;
+                    atomicOr(status, kStatusTimeout);
+                    break;
+                }
+            }
+            __nanosleep(20);
+        }
+        __threadfence();
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+__device__ __forceinline__ double warp_max_d(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+
+__device__ __forceinline__ float3 bmul(float4 a, float4 b, float c, float3 p) {
+    return f3(a.x * p.x + a.y * p.y + a.z * p.z, a.w * p.x + b.x * p.y + b.y * p.z, b.z * p.x + b.w * p.y + c * p.z);
+}
+
+__device__ __forceinline__ float3 minv_mul(const float* __restrict__ m, int row, float3 r) {
+    const float* b = m + 9 * (size_t)row;
+    return f3(b[0] * r.x + b[1] * r.y + b[2] * r.z, b[3] * r.x + b[4] * r.y + b[5] * r.z,
+              b[6] * r.x + b[7] * r.y + b[8] * r.z);
+}
+
+__device__ __forceinline__ float3 load3(const float* p, int i) { return f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+__device__ __forceinline__ void store3(float* p, int i, float3 v) {
+    p[3 * i] = v.x;
+    p[3 * i + 1] = v.y;
+    p[3 * i + 2] = v.z;
+}
+
+// Same expression at the owner and at every gathering neighbour, so the
+// recomputed search direction is bit-identical everywhere.
+__device__ __forceinline__ float3 next_p(float4 z, float4 p, float beta) {
+    return f3(fmaf(beta, p.x, z.x), fmaf(beta, p.y, z.y), fmaf(beta, p.z, z.z));
+}
+
+struct Smem {
+    float* part;      // [L * 3]
+    SceneState* st;   // [S]
+    double* tot;      // [S * 3]
+    double* red;      // [32 * 3] block-reduce scratch
+};
+
+// Per-CTA segment partials: sum (or max) of the slice partials of each scene
+// this CTA covers, in slice order, written to seg_part.
+__device__ void write_segments(const PcgArgs& a, const Smem& sm, int nv, bool is_max, int first, int last) {
+    __syncthreads();
+    if (first >= last) return;
+    int s0 = a.cta_first_scene[blockIdx.x];
+    int nsc = a.slice_scene[last - 1] - s0 + 1;
+    for (int t = threadIdx.x; t < nsc; t += blockDim.x) {
+        int s = s0 + t;
+        int lo = max(a.scene_slice0[s], first), hi = min(a.scene_slice0[s + 1], last);
+        for (int k = 0; k < nv; ++k) {
+            double acc = 0.0;
+            for (int sl = lo; sl < hi; ++sl) {
+                double v = (double)sm.part[(sl - first) * 3 + k];
+                acc = is_max ? fmax(acc, v) : acc + v;
+            }
+            a.seg_part[(size_t)(a.cta_seg_base[blockIdx.x] + t) * 3 + k] = acc;
+        }
+    }
+}
+
+// After a grid barrier: every CTA forms the per-scene totals from the segment
+// partials in the same fixed order.
+__device__ void scene_totals(const PcgArgs& a, const Smem& sm, int nv, bool is_max) {
+    int S = a.nscenes;
+    if (S <= 4) {
+        int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int s = 0; s < S; ++s) {
+            int lo = a.scene_seg0[s], hi = a.scene_seg0[s + 1];
+            double acc[3] = {0.0, 0.0, 0.0};
+            for (int g = lo + threadIdx.x; g < hi; g += blockDim.x)
+                for (int k = 0; k < nv; ++k) {
+                    double v = a.seg_part[(size_t)g * 3 + k];
+                    acc[k] = is_max ? fmax(acc[k], v) : acc[k] + v;
+                }
+            for (int k = 0; k < nv; ++k) {
+                double v = is_max ? warp_max_d(acc[k]) : warp_sum_d(acc[k]);
+                if (lane == 0) sm.red[warp * 3 + k] = v;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int k = 0; k < nv; ++k) {
+                    double t = 0.0;
+                    for (int w = 0; w < nw; ++w) t = is_max ? fmax(t, sm.red[w * 3 + k]) : t + sm.red[w * 3 + k];
+                    sm.tot[s * 3 + k] = t;
+                }
+            }
+            __syncthreads();
+        }
+    } else {
+        for (int s = threadIdx.x; s < S; s += blockDim.x) {
+            int lo = a.scene_seg0[s], hi = a.scene_seg0[s + 1];
+            for (int k = 0; k < nv; ++k) {
+                double t = 0.0;
+                for (int g = lo; g < hi; ++g) {
+                    double v = a.seg_part[(size_t)g * 3 + k];
+                    t = is_max ? fmax(t, v) : t + v;
+                }
+                sm.tot[s * 3 + k] = t;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ float rhs_scale(float maximum) {
+    // kernels.py:1785-1793
+    float scale = 1.0f;
+    if (maximum > 0.0f && maximum < 1.0e-12f) scale = fminf(1.0f / maximum, 1.0e30f);
+    return scale;
+}
+
+__global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_ok;
+    __shared__ int s_any;
+    const int S = a.nscenes;
+    const int L = a.slices_per_cta;
+    Smem sm;
+    sm.part = reinterpret_cast<float*>(smem_raw);
+    size_t off = ((size_t)L * 3 * sizeof(float) + 15) & ~(size_t)15;
+    sm.st = reinterpret_cast<SceneState*>(smem_raw + off);
+    off += ((size_t)S * sizeof(SceneState) + 15) & ~(size_t)15;
+    sm.tot = reinterpret_cast<double*>(smem_raw + off);
+    off += (size_t)S * 3 * sizeof(double);
+    sm.red = reinterpret_cast<double*>(smem_raw + off);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+    const int first = blockIdx.x * L;
+    const int last = min(first + L, a.nslices);
+    const unsigned nblocks = gridDim.x;
+    unsigned epoch = 0;
+    const float h = a.dt;
+
+    // ---------------- phase 0: RHS (predictor, springs, projection) and u = rhs - A x0
+    for (int sl = first + warp; sl < last; sl += W) {
+        int2 meta = a.slice_meta[sl];
+        float mx = 0.0f;
+        if (lane < meta.y) {
+            int row = meta.x + lane;
+            unsigned info = a.row_info[row];
+            float3 rhs = f3(0.f, 0.f, 0.f), u = f3(0.f, 0.f, 0.f);
+            if (!(info & kFixedBit)) {
+                int len = (int)(info & ~kFixedBit);
+                float3 vi = xyz(a.v4[row]);
+                float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
+                int base = a.slice_ptr[sl];
+                for (int k = 0; k < len; ++k) {
+                    size_t e = (size_t)(base + k) * kSlice + lane;
+                    float4 A = a.valA[e], B = a.valB[e];
+                    float C = a.valC[e];
+                    int j = a.scol[e];
+                    float3 vj = xyz(a.v4[j]);
+                    float3 xj = xyz(a.x[j]);
+                    cv = cv + bmul(A, B, C, vj - vi);
+                    ax = ax + bmul(A, B, C, xj);
+                }
+                rhs = load3(a.f_ws, row) - cv;
+                for (int e = a.spring_ptr[row]; e < a.spring_ptr[row + 1]; ++e) {
+                    int ent = a.spring_ent[e];
+                    int s = ent >> 1;
+                    int ia = a.spring_idx[2 * s], ib = a.spring_idx[2 * s + 1];
+                    if (ia < 0 || ib < 0) continue;
+                    float3 corr = (xyz(a.v4[ia]) - xyz(a.v4[ib])) * (h * a.spring_kd[s]);
+                    rhs = (ent & 1) ? rhs - corr : rhs + corr;
+                }
+                u = rhs - ax;
+            }
+            store3(a.f_ws, row, rhs);
+            a.r[row] = f4(u);
+            mx = fmaxf(fabsf(rhs.x), fmaxf(fabsf(rhs.y), fabsf(rhs.z)));
+        }
+        mx = warp_max(mx);
+        if (lane == 0) sm.part[(sl - first) * 3] = mx;
+    }
+    write_segments(a, sm, 1, true, first, last);
+    if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
+    scene_totals(a, sm, 1, true);
+    for (int s = threadIdx.x; s < S; s += blockDim.x) {
+        float mxs = (float)sm.tot[s * 3];
+        sm.st[s].scale = rhs_scale(mxs);
+        sm.st[s].zero = mxs == 0.0f;
+    }
+    __syncthreads();
+
+    // ---------------- phase 1: normalise, initial residual and preconditioned residual
+    for (int sl = first + warp; sl < last; sl += W) {
+        int2 meta = a.slice_meta[sl];
+        const SceneState& st = sm.st[a.slice_scene[sl]];
+        float rr = 0.f, rz = 0.f, bb = 0.f;
+        if (lane < meta.y) {
+            int row = meta.x + lane;
+            float sc = st.scale;
+            float3 x = f3(0.f, 0.f, 0.f), r = f3(0.f, 0.f, 0.f);
+            if (!st.zero) {
+                x = xyz(a.x[row]) * sc;
+                r = xyz(a.r[row]) * sc;
+            }
+            float3 b = load3(a.f_ws, row) * sc;
+            float3 z = minv_mul(a.minv, row, r);
+            a.x[row] = f4(x);
+            a.r[row] = f4(r);
+            a.z[row] = f4(z);
+            rr = dot3(r, r);
+            rz = dot3(r, z);
+            bb = dot3(b, b);
+        }
+        rr = warp_sum(rr);
+        rz = warp_sum(rz);
+        bb = warp_sum(bb);
+        if (lane == 0) {
+            float* p = sm.part + (sl - first) * 3;
+            p[0] = rr; p[1] = rz; p[2] = bb;
+        }
+    }
+    write_segments(a, sm, 3, false, first, last);
+    if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
+    scene_totals(a, sm, 3, false);
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    for (int s = threadIdx.x; s < S; s += blockDim.x) {
+        SceneState& st = sm.st[s];
+        st.rr = sm.tot[s * 3];
+        st.rz = sm.tot[s * 3 + 1];
+        st.bb = sm.tot[s * 3 + 2];
+        st.atol_sq = (double)a.tol * (double)a.tol * st.bb;
+        st.iters = 0;
+        st.beta = 0.0f;
+        st.alpha = 0.0f;
+        st.active = (st.rr > st.atol_sq) && (a.maxiter > 0);
+        if (!isfinite(st.rr)) {
+            st.active = 0;
+            atomicOr(a.status, kStatusNonFinite);
+        }
+        if (st.active) atomicOr(&s_any, 1);
+    }
+    __syncthreads();
+
+    // ---------------- CG iterations
+    for (int it = 0; s_any; ++it) {
+        const float4* pold = (it & 1) ? a.p1 : a.p0;
+        float4* pnew = (it & 1) ? a.p0 : a.p1;
+        // phase A: p = z + beta p, y = (PAP + I - P) p, partial p.y
+        for (int sl = first + warp; sl < last; sl += W) {
+            int2 meta = a.slice_meta[sl];
+            const SceneState& st = sm.st[a.slice_scene[sl]];
+            float pap = 0.f;
+            if (st.active && lane < meta.y) {
+                int row = meta.x + lane;
+                unsigned info = a.row_info[row];
+                const bool firstit = st.iters == 0;
+                const float beta = st.beta;
+                float4 zi = a.z[row];
+                float3 pc = firstit ? xyz(zi) : next_p(zi, pold[row], beta);
+                float3 acc = pc;  // fixed rows: identity (their p is zero)
+                if (!(info & kFixedBit)) {
+                    int len = (int)(info & ~kFixedBit);
+                    int base = a.slice_ptr[sl];
+                    acc = f3(0.f, 0.f, 0.f);
+                    if (firstit) {
+                        for (int k = 0; k < len; ++k) {
+                            size_t e = (size_t)(base + k) * kSlice + lane;
+                            int j = a.scol[e];
+                            acc = acc + bmul(a.valA[e], a.valB[e], a.valC[e], xyz(a.z[j]));
+                        }
+                    } else {
+                        for (int k = 0; k < len; ++k) {
+                            size_t e = (size_t)(base + k) * kSlice + lane;
+                            int j = a.scol[e];
+                            acc = acc + bmul(a.valA[e], a.valB[e], a.valC[e], next_p(a.z[j], pold[j], beta));
+                        }
+                    }
+                }
+                pnew[row] = f4(pc);
+                a.y[row] = f4(acc);
+                pap = dot3(pc, acc);
+            }
+            pap = warp_sum(pap);
+            if (lane == 0) sm.part[(sl - first) * 3] = pap;
+        }
+        write_segments(a, sm, 1, false, first, last);
+        if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
+        scene_totals(a, sm, 1, false);
+        for (int s = threadIdx.x; s < S; s += blockDim.x) {
+            SceneState& st = sm.st[s];
+            if (st.active) st.alpha = (float)(st.rz / sm.tot[s * 3]);
+        }
+        __syncthreads();
+        // phase B: x += alpha p, r -= alpha y, z = M r, partial r.r and r.z
+        for (int sl = first + warp; sl < last; sl += W) {
+            int2 meta = a.slice_meta[sl];
+            const SceneState& st = sm.st[a.slice_scene[sl]];
+            float rr = 0.f, rz = 0.f;
+            if (st.active && lane < meta.y) {
+                int row = meta.x + lane;
+                float alpha = st.alpha;
+                float3 p = xyz(pnew[row]), yv = xyz(a.y[row]);
+                float3 x = xyz(a.x[row]), r = xyz(a.r[row]);
+                x = x + p * alpha;
+                r = r - yv * alpha;
+                float3 z = minv_mul(a.minv, row, r);
+                a.x[row] = f4(x);
+                a.r[row] = f4(r);
+                a.z[row] = f4(z);
+                rr = dot3(r, r);
+                rz = dot3(r, z);
+            }
+            rr = warp_sum(rr);
+            rz = warp_sum(rz);
+            if (lane == 0) {
+                float* p = sm.part + (sl - first) * 3;
+                p[0] = rr; p[1] = rz;
+            }
+        }
+        write_segments(a, sm, 2, false, first, last);
+        if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
+        scene_totals(a, sm, 2, false);
+        if (threadIdx.x == 0) s_any = 0;
+        __syncthreads();
+        for (int s = threadIdx.x; s < S; s += blockDim.x) {
+            SceneState& st = sm.st[s];
+            if (!st.active) continue;
+            double rr = sm.tot[s * 3], rz_new = sm.tot[s * 3 + 1];
+            st.iters += 1;
+            st.beta = (float)(rz_new / st.rz);
+            st.rz = rz_new;
+            st.rr = rr;
+            st.active = (rr > st.atol_sq) && (st.iters < a.maxiter);
+            if (!isfinite(rr)) {
+                st.active = 0;
+                atomicOr(a.status, kStatusNonFinite);
+            }
+            if (st.active) atomicOr(&s_any, 1);
+        }
+        __syncthreads();
+    }
+
+    // ---------------- epilogue: restore scale, integrate, fixed restore
+    for (int sl = first + warp; sl < last; sl += W) {
+        int2 meta = a.slice_meta[sl];
+        if (lane >= meta.y) continue;
+        const SceneState& st = sm.st[a.slice_scene[sl]];
+        int row = meta.x + lane;
+        float3 dv = xyz(a.x[row]);
+        float sc = st.scale;
+        dv = f3(dv.x / sc, dv.y / sc, dv.z / sc);
+        store3(a.dv, row, dv);
+        if (a.write_state) {
+            bool fixed = (a.row_info[row] & kFixedBit) != 0;
+            float3 v = xyz(a.v4[row]) + dv;
+            float3 q = xyz(a.q4[row]) + v * h;
+            if (fixed) {
+                q = load3(a.rest, row);
+                v = f3(0.f, 0.f, 0.f);
+            }
+            store3(a.q_out, row, q);
+            store3(a.v_out, row, v);
+        }
+    }
+    if (blockIdx.x == 0) {
+        for (int s = threadIdx.x; s < S; s += blockDim.x) {
+            const SceneState& st = sm.st[s];
+            SceneStats o;
+            o.iterations = st.iters;
+            o.rr = (float)st.rr;
+            o.bb = (float)st.bb;
+            o.converged = st.rr <= st.atol_sq;
+            a.scene_stats[s] = o;
+            a.cum_iters[s] += st.iters;
+        }
+    }
+}
+
+}  // namespace
+
+size_t pcg_smem_bytes(int L, int S) {
+    size_t off = ((size_t)L * 3 * sizeof(float) + 15) & ~(size_t)15;
+    off += ((size_t)S * sizeof(SceneState) + 15) & ~(size_t)15;
+    off += (size_t)S * 3 * sizeof(double);
+    off += 32 * 3 * sizeof(double);
+    return off;
+}
+
+cudaError_t pcg_configure(Handle& h) {
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    int sms = 0, coop = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return cudaErrorNotSupported;
+    int warps_per_cta = kPcgThreads / 32;
+    int needed = (h.nslices + warps_per_cta - 1) / warps_per_cta;
+    if (needed < 1) needed = 1;
+    // grid depends on shared memory, which depends on slices per CTA: iterate
+    int grid = needed;
+    for (int pass = 0; pass < 4; ++pass) {
+        int L = (h.nslices + grid - 1) / grid;
+        if (L < 1) L = 1;
+        size_t smem = pcg_smem_bytes(L, h.nscenes);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(pcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0;
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_kernel, kPcgThreads, smem);
+        if (err != cudaSuccess) return err;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+        int cap = per_sm * sms;
+        int g = needed < cap ? needed : cap;
+        if (g == grid && pass > 0) break;
+        grid = g;
+    }
+    h.grid = grid;
+    h.slices_per_cta = (h.nslices + grid - 1) / grid;
+    if (h.slices_per_cta < 1) h.slices_per_cta = 1;
+    h.pcg_smem = pcg_smem_bytes(h.slices_per_cta, h.nscenes);
+    if (h.pcg_smem > 48 * 1024)
+        cudaFuncSetAttribute(pcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h.pcg_smem);
+    return cudaSuccess;
+}
+
+cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s) {
+    PcgArgs a;
+    a.valA = h.valA;
+    a.valB = h.valB;
+    a.valC = h.valC;
+    a.scol = h.scol;
+    a.slice_ptr = h.slice_ptr;
+    a.slice_meta = h.slice_meta;
+    a.slice_scene = h.slice_scene;
+    a.row_info = h.row_info;
+    a.minv = h.minv;
+    a.nslices = h.nslices;
+    a.slices_per_cta = h.slices_per_cta;
+    a.cta_seg_base = h.cta_seg_base;
+    a.cta_first_scene = h.cta_first_scene;
+    a.scene_slice0 = h.scene_slice0;
+    a.scene_seg0 = h.scene_seg0;
+    a.nscenes = h.nscenes;
+    a.seg_part = h.seg_part;
+    a.v4 = h.v4;
+    a.q4 = h.q4;
+    a.rest = h.rest;
+    a.spring_ptr = h.node_spring_ptr;
+    a.spring_ent = h.node_spring_ent;
+    a.spring_idx = h.spring_idx;
+    a.spring_kd = h.spring_kd;
+    a.f_ws = f_ws;
+    a.dv = h.dv;
+    a.q_out = q_out;
+    a.v_out = v_out;
+    a.x = h.x;
+    a.r = h.r;
+    a.z = h.z;
+    a.p0 = h.p0;
+    a.p1 = h.p1;
+    a.y = h.y;
+    a.barrier = h.barrier;
+    a.status = h.status;
+    a.scene_stats = h.scene_stats;
+    a.cum_iters = h.cum_iters;
+    a.maxiter = h.maxiter;
+    a.tol = h.tol;
+    a.dt = dt;
+    a.limit_ns = h.wait_limit_ns;
+    a.write_state = write_state;
+    cudaError_t err = cudaMemsetAsync(h.barrier, 0, sizeof(unsigned), s);
+    if (err != cudaSuccess) return err;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(h.grid);
+    cfg.blockDim = dim3(kPcgThreads);
+    cfg.dynamicSmemBytes = h.pcg_smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, pcg_kernel, a);
+}
+
+}  // namespace fem

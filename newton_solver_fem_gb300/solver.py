@@ -1,0 +1,450 @@
+"""``SolverFEM``: the reference's solver interface over the GB300 C-ABI library.
+
+Keeps the reference constructor (``solver.py:212-240``), its validation
+(``solver.py:241-262``), ``step(state_in, state_out, control, contacts, dt, *,
+external_forces=)`` (``solver.py:942-1002``), the tangent-refresh calls
+(``refresh_tangent`` ``solver.py:769-857``, ``rebuild_element_blocks``
+``solver.py:506-508``, ``refresh_preconditioner`` ``solver.py:502-504``), the
+mutable ``linear_solver_tolerance`` / ``linear_solver_maxiter``, ``reset``,
+``velocity_increment``, ``last_cg_iters``, the per-term force evaluators and the
+volume telemetry.  Every numerical operation runs in ``libfemgb300.so`` on the
+model's CUDA device, enqueued on the current torch stream; tensors are only
+buffers.  There is no CPU path: a CPU model is rejected.
+
+Implemented hot-path options: ``solver_type="cg"`` with ``preconditioner_type``
+``"block_diag"`` or ``"diag"``; Tet4, Hex8, springs, analytic ground, gravity,
+linear damping, tet activations, fixed nodes, batched independent scenes
+(``model.scene_offsets``).  Other Krylov types, triangles, particle-particle
+contact, torque springs and soft/surface contacts are outside this path.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .builder import Model, State
+
+
+def _ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def _f32(t: torch.Tensor, shape, name: str, device) -> torch.Tensor:
+    if not isinstance(t, torch.Tensor) or t.dtype != torch.float32 or tuple(t.shape) != tuple(shape) or \
+            t.device != device or not t.is_contiguous():
+        raise ValueError(f"{name} must be a contiguous float32 tensor of shape {tuple(shape)} on {device}")
+    return t
+
+
+class BsrMatrix:
+    """Exported 3x3-block CSR matrix in the reference's Warp ``BsrMatrix`` layout."""
+
+    def __init__(self, offsets: torch.Tensor, columns: torch.Tensor, values: torch.Tensor, nrow: int):
+        self.offsets = offsets
+        self.columns = columns
+        self.values = values
+        self.nrow = nrow
+        self.ncol = nrow
+        self.nnz = int(columns.shape[0])
+
+    def dense(self) -> np.ndarray:
+        offsets, columns, values = self.offsets.cpu().numpy(), self.columns.cpu().numpy(), self.values.cpu().numpy()
+        out = np.zeros((3 * self.nrow, 3 * self.ncol))
+        rows = np.repeat(np.arange(self.nrow), np.diff(offsets))
+        for k in range(len(columns)):
+            r, c = rows[k], columns[k]
+            out[3 * r:3 * r + 3, 3 * c:3 * c + 3] += values[k]
+        return out
+
+
+class SolverFEM:
+    """Linearly implicit Backward-Euler FEM solver (reference ``SolverFEM``) on one GB300."""
+
+    def __init__(
+        self,
+        model: Model,
+        dt: float = 1.0 / 60.0,
+        mass: float = 1.0,
+        preconditioner_type: str = "diag",
+        solver_type: str = "bicgstab",
+        linear_solver_maxiter: int = 50,
+        min_stretch: float = 0.05,
+        max_stretch: float = 20.0,
+        ground_plane=None,
+        ground_ke: float = 1.0e5,
+        ground_kd: float = 1.0e2,
+        ground_kf: float = 1.0e3,
+        ground_mu: float = 0.5,
+        torque_stiffness: float = 0.0,
+        torque_damping: float = 0.0,
+        spring_rest_direction=None,
+        self_contact_ke: float = 1.0e3,
+        self_contact_kd: float = 1.0e2,
+        linear_damping: float = 0.0,
+        differentiable: bool = False,
+        enable_tet_activations: bool = False,
+        defer_differentiation_checks: bool = False,
+        tet_volume_weights=None,
+        fixed_particle_indices=None,
+        linear_solver_tolerance: float = 1.0e-2,
+        linear_solver_use_cuda_graph: bool = True,
+    ):
+        if not math.isfinite(linear_solver_tolerance) or linear_solver_tolerance <= 0:
+            raise ValueError("linear_solver_tolerance must be finite and positive")
+        fixed = np.asarray([] if fixed_particle_indices is None else fixed_particle_indices)
+        if fixed.ndim != 1 or (fixed.size and fixed.dtype.kind not in "iu"):
+            raise ValueError("fixed_particle_indices must be a one-dimensional integer sequence")
+        if fixed.size and (fixed.min() < 0 or fixed.max() >= model.particle_count):
+            raise ValueError("fixed_particle_indices contains an out-of-range node")
+        fixed = np.unique(fixed).astype(np.int32)
+        if fixed.size and differentiable:
+            raise ValueError("fixed_particle_indices is not supported with differentiable=True")
+        if not isinstance(model.particle_q, torch.Tensor) or model.particle_q.device.type != "cuda":
+            raise RuntimeError("SolverFEM on GB300 requires a model on a CUDA device (no CPU path)")
+        if solver_type not in ("cg", "bicgstab", "gmres", "cr"):
+            raise ValueError(f"Invalid solver type: {solver_type}")
+        if solver_type != "cg":
+            raise NotImplementedError(f"solver_type={solver_type!r}: the GB300 hot path implements 'cg'")
+        if preconditioner_type not in ("block_diag", "diag"):
+            raise NotImplementedError(f"preconditioner_type={preconditioner_type!r} is not implemented")
+        if torque_stiffness > 0.0 and spring_rest_direction is not None:
+            raise NotImplementedError("spring bend torque is outside the GB300 hot path")
+        if differentiable:
+            raise NotImplementedError("use newton_solver_fem_gb300.adjoint for differentiable rollouts")
+        if tet_volume_weights is not None:
+            w = torch.as_tensor(tet_volume_weights)
+            if tuple(w.shape) != (model.tet_count,) or not torch.isfinite(w).all() or (w < 0).any():
+                raise ValueError("tet_volume_weights must be finite and nonnegative with shape (tet_count,)")
+        self.model = model
+        self.device = model.particle_q.device
+        self.mass = float(mass)
+        self.preconditioner_type = preconditioner_type
+        self.solver_type = solver_type
+        self.min_stretch = float(min_stretch)
+        self.max_stretch = float(max_stretch)
+        self.linear_damping = float(linear_damping)
+        self.differentiable = False
+        self.enable_tet_activations = bool(enable_tet_activations)
+        self.linear_solver_use_cuda_graph = bool(linear_solver_use_cuda_graph)
+        self.linear_solver_check_every = 0
+        self.dt = float(dt)
+        self.hex_count = int(model.fem.hex_count) if getattr(model, "fem", None) is not None else 0
+        self.fixed_particle_indices = fixed
+        self._tet_volume_weights = tet_volume_weights
+        self._ground_plane = None if ground_plane is None else tuple(float(v) for v in ground_plane)
+        model.particle_ke = float(self_contact_ke)
+        model.particle_kd = float(self_contact_kd)
+        self._lib = _lib.load()
+        self._handle = ctypes.c_void_p()
+        P = model.particle_count
+        # persistent velocity increment, owned here so it is visible as a tensor
+        self.dv = torch.zeros((P, 3), dtype=torch.float32, device=self.device)
+        self._create(model, fixed, linear_solver_maxiter, linear_solver_tolerance, ground_ke, ground_kd, ground_kf,
+                     ground_mu)
+        self._tolerance = float(linear_solver_tolerance)
+        self._maxiter = int(linear_solver_maxiter)
+        self._initial_volume = self._compute_volume(model.particle_q)
+
+    # ------------------------------------------------------------------ setup
+    def _create(self, model, fixed, maxiter, tolerance, gke, gkd, gkf, gmu):
+        keep = []
+
+        def host(t, dtype):
+            if t is None:
+                return None
+            a = np.ascontiguousarray(t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else t, dtype=dtype)
+            keep.append(a)
+            return a.ctypes.data
+
+        d = _lib.FemDesc()
+        P = model.particle_count
+        fem = getattr(model, "fem", None)
+        H = self.hex_count
+        d.particle_count = P
+        d.tet_count = model.tet_count
+        d.hex_count = H
+        d.spring_count = model.spring_count
+        d.particle_q = host(model.particle_q, np.float32)
+        d.particle_mass = host(model.particle_mass, np.float32)
+        d.particle_inv_mass = host(model.particle_inv_mass, np.float32)
+        d.particle_radius = host(model.particle_radius, np.float32)
+        d.particle_flags = host(model.particle_flags, np.int32)
+        if model.tet_count:
+            d.tet_indices = host(model.tet_indices, np.int32)
+            d.tet_poses = host(model.tet_poses, np.float32)
+            d.tet_materials = host(model.tet_materials, np.float32)
+        if H:
+            d.hex_indices = host(fem.hex_indices, np.int32)
+            d.hex_materials = host(fem.hex_materials, np.float32)
+            d.hex_inv_J0 = host(fem.hex_inv_J0, np.float32)
+            d.hex_det_J0_w = host(fem.hex_det_J0_w, np.float32)
+        if model.spring_count:
+            d.spring_indices = host(model.spring_indices, np.int32)
+            d.spring_rest_length = host(model.spring_rest_length, np.float32)
+            d.spring_stiffness = host(model.spring_stiffness, np.float32)
+            d.spring_damping = host(model.spring_damping, np.float32)
+        d.fixed_indices = host(fixed, np.int32) if fixed.size else None
+        d.fixed_count = int(fixed.size)
+        offsets = getattr(model, "scene_offsets", None)
+        if offsets is not None:
+            d.scene_offsets = host(offsets, np.int64)
+            d.scene_count = len(offsets) - 1
+        g = model.gravity.detach().cpu().numpy().astype(np.float32)
+        d.gravity[:] = list(g)
+        d.dt = self.dt
+        d.min_stretch = self.min_stretch
+        d.max_stretch = self.max_stretch
+        d.has_ground = 1 if self._ground_plane is not None else 0
+        if self._ground_plane is not None:
+            d.ground_plane[:] = list(self._ground_plane)
+        d.ground_ke, d.ground_kd, d.ground_kf, d.ground_mu = gke, gkd, gkf, gmu
+        d.linear_damping = self.linear_damping
+        d.enable_tet_activations = int(self.enable_tet_activations)
+        d.preconditioner = _lib.FEM_PRECOND_BLOCK_DIAG if self.preconditioner_type == "block_diag" else \
+            _lib.FEM_PRECOND_DIAG
+        d.maxiter = int(maxiter)
+        d.tolerance = float(tolerance)
+        d.velocity_increment = self.dv.data_ptr()
+        with torch.cuda.device(self.device):
+            torch.cuda.current_stream(self.device).synchronize()
+            _lib.check(self._lib.fem_create(ctypes.byref(d), ctypes.byref(self._handle)), "SolverFEM")
+        del keep
+
+    def __del__(self):
+        handle = getattr(self, "_handle", None)
+        if handle is not None and handle.value:
+            try:
+                torch.cuda.synchronize(self.device)
+                self._lib.fem_destroy(handle)
+            except Exception:
+                pass
+            self._handle = ctypes.c_void_p()
+
+    def _stream(self) -> int:
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    # ------------------------------------------------------------------ settings
+    @property
+    def linear_solver_tolerance(self) -> float:
+        return self._tolerance
+
+    @linear_solver_tolerance.setter
+    def linear_solver_tolerance(self, value: float) -> None:
+        value = float(value)
+        _lib.check(self._lib.fem_set_tolerance(self._handle, value), "linear_solver_tolerance")
+        self._tolerance = value
+
+    @property
+    def linear_solver_maxiter(self) -> int:
+        return self._maxiter
+
+    @linear_solver_maxiter.setter
+    def linear_solver_maxiter(self, value: int) -> None:
+        _lib.check(self._lib.fem_set_maxiter(self._handle, int(value)), "linear_solver_maxiter")
+        self._maxiter = int(value)
+
+    @property
+    def velocity_increment(self) -> torch.Tensor:
+        """Persistent solved velocity increment (also the next solve's warm start)."""
+        return self.dv
+
+    # ------------------------------------------------------------------ step
+    def step(self, state_in: State, state_out: State, control, contacts, dt: float, *, external_forces=None,
+             observables=None):
+        """Advance one linearly implicit substep (reference ``solver.py:942-1002``).
+
+        ``state_in.particle_f`` is overwritten with the final right-hand side
+        ``h*sum(f) - h^2 K v`` (projected); fixed nodes of ``state_in`` are
+        restored in place, as in the reference.
+        """
+        P = self.model.particle_count
+        dev = self.device
+        ext = None
+        if external_forces is not None:
+            if not isinstance(external_forces, torch.Tensor) or tuple(external_forces.shape) != (P, 3) or \
+                    external_forces.dtype != torch.float32 or external_forces.device != dev:
+                raise ValueError("external_forces must be a model-sized wp.vec3 array on the model device")
+            ext = external_forces.contiguous()
+        for name, t in (("state_in.particle_q", state_in.particle_q), ("state_in.particle_qd", state_in.particle_qd),
+                        ("state_out.particle_q", state_out.particle_q),
+                        ("state_out.particle_qd", state_out.particle_qd), ("state_in.particle_f", state_in.particle_f)):
+            _f32(t, (P, 3), name, dev)
+        act = None
+        if self.enable_tet_activations and self.model.tet_count:
+            act = control.tet_activations if control is not None else self.model.tet_activations
+            _f32(act, (self.model.tet_count,), "tet_activations", dev)
+        code = self._lib.fem_step(
+            self._handle, state_in.particle_q.data_ptr(), state_in.particle_qd.data_ptr(),
+            state_out.particle_q.data_ptr(), state_out.particle_qd.data_ptr(), state_in.particle_f.data_ptr(),
+            _ptr(ext), _ptr(act), self.model.gravity.data_ptr(), float(dt), self._stream())
+        _lib.check(code, "step")
+        if self.linear_solver_check_every > 0:
+            stats = self.stats()
+            self.last_cg_iters = stats["max_iterations"]
+        return state_out
+
+    def stats(self) -> dict:
+        """Synchronise and return the last solve's statistics (raises on a device timeout / NaN)."""
+        s = _lib.FemStats()
+        iters = (ctypes.c_int32 * max(1, self.model.scene_count))()
+        code = self._lib.fem_get_stats(self._handle, ctypes.byref(s), iters, self._stream())
+        _lib.check(code, "linear solve")
+        return {
+            "status": s.status,
+            "max_iterations": s.max_iterations,
+            "min_iterations": s.min_iterations,
+            "max_relative_residual": s.max_relative_residual,
+            "unconverged_scenes": s.unconverged_scenes,
+            "scene_iterations": list(iters)[: self.model.scene_count],
+        }
+
+    @property
+    def last_cg_iters(self) -> int:
+        return self.stats()["max_iterations"]
+
+    @last_cg_iters.setter
+    def last_cg_iters(self, value) -> None:
+        pass
+
+    # ------------------------------------------------------------------ tangent
+    def refresh_tangent(self, particle_q: torch.Tensor, dt: float | None = None) -> None:
+        """Refresh the element stiffness in place; a changed dt rebuilds all blocks and clears dv."""
+        dt = self.dt if dt is None else float(dt)
+        if not math.isfinite(dt) or dt <= 0:
+            raise ValueError("refresh_tangent dt must be finite and positive")
+        _f32(particle_q, (self.model.particle_count, 3), "particle_q", self.device)
+        _lib.check(self._lib.fem_refresh_tangent(self._handle, particle_q.data_ptr(), dt, self._stream()),
+                   "refresh_tangent")
+        self.dt = dt
+
+    def rebuild_element_blocks(self, particle_q: torch.Tensor, dt: float, *, update_preconditioner=True) -> None:
+        """Reassemble the Tet4/Hex8 blocks at particle_q and dt (the preconditioner refreshes in place)."""
+        _f32(particle_q, (self.model.particle_count, 3), "particle_q", self.device)
+        _lib.check(self._lib.fem_rebuild_element_blocks(self._handle, particle_q.data_ptr(), float(dt),
+                                                        self._stream()), "rebuild_element_blocks")
+
+    def refresh_preconditioner(self) -> None:
+        _lib.check(self._lib.fem_refresh_preconditioner(self._handle, self._stream()), "refresh_preconditioner")
+
+    def reset(self, state=None, world_mask=None, flags=None) -> None:
+        """Clear the warm start and the sticky device status."""
+        _lib.check(self._lib.fem_reset(self._handle, self._stream()), "reset")
+
+    def notify_model_changed(self, flags) -> None:
+        """Gravity is read live from ``model.gravity``; topology edits need a new solver."""
+
+    # ------------------------------------------------------------------ matrix views
+    def matrix_info(self) -> dict:
+        nnzb, ntrip, stored = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(self._lib.fem_matrix_info(self._handle, ctypes.byref(nnzb), ctypes.byref(ntrip),
+                                             ctypes.byref(stored)))
+        return {"nnzb": nnzb.value, "triplets": ntrip.value, "stored_blocks": stored.value}
+
+    @property
+    def A_bsr(self) -> BsrMatrix:
+        """Copy of the assembled A in BSR form (offsets [P+1], columns [nnzb], values [nnzb,3,3])."""
+        info = self.matrix_info()
+        P = self.model.particle_count
+        offsets = torch.empty(P + 1, dtype=torch.int32, device=self.device)
+        columns = torch.empty(info["nnzb"], dtype=torch.int32, device=self.device)
+        values = torch.empty((info["nnzb"], 3, 3), dtype=torch.float32, device=self.device)
+        _lib.check(self._lib.fem_export_bsr(self._handle, offsets.data_ptr(), columns.data_ptr(), values.data_ptr(),
+                                            self._stream()))
+        return BsrMatrix(offsets, columns, values, P)
+
+    @property
+    def _pc_inv_diag(self) -> torch.Tensor:
+        out = torch.empty((self.model.particle_count, 3, 3), dtype=torch.float32, device=self.device)
+        _lib.check(self._lib.fem_export_preconditioner(self._handle, out.data_ptr(), self._stream()))
+        return out
+
+    def _triplets(self):
+        n = self.matrix_info()["triplets"]
+        rows = torch.empty(n, dtype=torch.int32, device=self.device)
+        cols = torch.empty(n, dtype=torch.int32, device=self.device)
+        vals = torch.empty((n, 3, 3), dtype=torch.float32, device=self.device)
+        _lib.check(self._lib.fem_export_triplets(self._handle, rows.data_ptr(), cols.data_ptr(), vals.data_ptr(),
+                                                 self._stream()))
+        return rows, cols, vals
+
+    @property
+    def bsr_values(self) -> torch.Tensor:
+        return self._triplets()[2]
+
+    @property
+    def bsr_rows(self) -> torch.Tensor:
+        return self._triplets()[0]
+
+    @property
+    def bsr_cols(self) -> torch.Tensor:
+        return self._triplets()[1]
+
+    # ------------------------------------------------------------------ force evaluators
+    def _forces(self, state, terms: int, activations=None) -> torch.Tensor:
+        P = self.model.particle_count
+        out = torch.empty((P, 3), dtype=torch.float32, device=self.device)
+        q = state.particle_q.detach().contiguous()
+        v = state.particle_qd.detach().contiguous()
+        _lib.check(self._lib.fem_eval_forces(self._handle, q.data_ptr(), v.data_ptr(), _ptr(activations),
+                                             self.model.gravity.data_ptr(), terms, out.data_ptr(), self._stream()))
+        return out
+
+    def eval_tetrahedral_forces(self, model, control, state) -> torch.Tensor:
+        act = None
+        if self.enable_tet_activations and model.tet_count:
+            act = (control.tet_activations if control is not None else model.tet_activations).contiguous()
+        return self._forces(state, _lib.FEM_TERM_TET, act)
+
+    def eval_hexahedral_forces(self, model, control, state) -> torch.Tensor:
+        return self._forces(state, _lib.FEM_TERM_HEX)
+
+    def eval_spring_forces(self, model, state) -> torch.Tensor:
+        return self._forces(state, _lib.FEM_TERM_SPRING)
+
+    def eval_particle_ground_contact_forces(self, model, control, state) -> torch.Tensor:
+        return self._forces(state, _lib.FEM_TERM_GROUND)
+
+    def eval_gravity_forces(self, model) -> torch.Tensor:
+        st = model.state()
+        return self._forces(st, _lib.FEM_TERM_GRAVITY)
+
+    def eval_linear_damping_forces(self, model, state) -> torch.Tensor:
+        return self._forces(state, _lib.FEM_TERM_DAMPING)
+
+    # ------------------------------------------------------------------ volume telemetry (not on the hot path)
+    def _compute_volume(self, positions: torch.Tensor | None) -> float:
+        total = 0.0
+        m = self.model
+        if m.tet_count and positions is not None:
+            idx = m.tet_indices.long()
+            p = positions.detach().double()
+            e = p[idx[:, 1:]] - p[idx[:, :1]]
+            vol = torch.linalg.det(e.transpose(1, 2)).abs() / 6.0
+            if self._tet_volume_weights is not None:
+                vol = vol * torch.as_tensor(self._tet_volume_weights, device=vol.device).double()
+            total += float(vol.sum())
+        if self.hex_count:
+            total += float(m.fem.hex_det_J0_w.double().sum())
+        return total
+
+    def compute_volume(self, state=None) -> float:
+        return self._compute_volume(None if state is None else state.particle_q)
+
+    def get_initial_volume(self, state=None) -> float:
+        return self._initial_volume if self._initial_volume > 1e-12 else 1.0
+
+    def get_volume_ratio(self, state=None) -> float:
+        initial = self.get_initial_volume(state)
+        current = self.compute_volume(state)
+        if not math.isfinite(current) or current <= 0.0:
+            return 1.0
+        ratio = current / initial
+        return ratio if math.isfinite(ratio) else 1.0
+
+
+SolverLinearFEM = SolverFEM

@@ -1,0 +1,83 @@
+"""Build matching (GPU solver, CPU oracle) pairs from identical float32 inputs."""
+
+import numpy as np
+import torch
+
+from newton_solver_fem_gb300 import SolverFEM, model_from_arrays, scenes
+from oracle import fem_oracle as O
+
+DEVICE = "cuda:0"
+
+
+def rounded(a):
+    return np.asarray(a, np.float32).astype(np.float64)
+
+
+def make_pair(x, mass, *, tets=None, tet_materials=None, hexes=None, hex_materials=None, springs=None, spring_ke=None,
+              spring_kd=None, velocity=None, radius=0.0, gravity=(0.0, 0.0, -9.81), fixed=None, dt=1.0 / 600.0,
+              scene_offsets=None, solver_type="cg", preconditioner_type="block_diag", with_oracle=True, **kw):
+    """Return (model, solver, oracle) over the same float32 data."""
+    x32 = rounded(x)
+    m32 = rounded(mass)
+    model = model_from_arrays(x32, m32, tets=tets, tet_materials=tet_materials, hexes=hexes,
+                              hex_materials=hex_materials, springs=springs, spring_ke=spring_ke, spring_kd=spring_kd,
+                              velocity=velocity, radius=radius, gravity=gravity, scene_offsets=scene_offsets,
+                              device=DEVICE)
+    args = dict(dt=dt, solver_type=solver_type, preconditioner_type=preconditioner_type, self_contact_ke=0.0)
+    args.update(kw)
+    solver = SolverFEM(model, fixed_particle_indices=fixed, **args)
+    if not with_oracle:
+        return model, solver, None
+    okw = dict(
+        dt=dt, gravity=gravity, radius=radius, fixed=fixed,
+        min_stretch=args.get("min_stretch", 0.05), max_stretch=args.get("max_stretch", 20.0),
+        maxiter=args.get("linear_solver_maxiter", 50), tolerance=args.get("linear_solver_tolerance", 1e-2),
+        ground_plane=args.get("ground_plane"), ground_ke=args.get("ground_ke", 1.0e5),
+        ground_kd=args.get("ground_kd", 1.0e2), ground_kf=args.get("ground_kf", 1.0e3),
+        ground_mu=args.get("ground_mu", 0.5), linear_damping=args.get("linear_damping", 0.0),
+        preconditioner=preconditioner_type, scene_offsets=scene_offsets,
+    )
+    if tets is not None and len(tets):
+        okw.update(tets=tets, tet_poses=model.tet_poses.cpu().numpy(), tet_materials=np.asarray(tet_materials,
+                                                                                             np.float32))
+    if hexes is not None and len(hexes):
+        okw.update(hexes=hexes, hex_inv_J0=model.fem.hex_inv_J0.cpu().numpy(),
+                   hex_det_J0_w=model.fem.hex_det_J0_w.cpu().numpy(),
+                   hex_materials=np.asarray(hex_materials, np.float32))
+    if springs is not None and len(springs):
+        okw.update(springs=springs, spring_rest=model.spring_rest_length.cpu().numpy(),
+                   spring_ke=np.asarray(spring_ke, np.float32), spring_kd=np.asarray(spring_kd, np.float32))
+    oracle = O.OracleFEM(x32, m32, **okw)
+    return model, solver, oracle
+
+
+def scene_pair(scene, **kw):
+    args = dict(tets=scene.tets if len(scene.tets) else None, tet_materials=scene.tet_materials,
+                hexes=scene.hexes if len(scene.hexes) else None, hex_materials=scene.hex_materials,
+                springs=scene.springs if len(scene.springs) else None, spring_ke=scene.spring_ke,
+                spring_kd=scene.spring_kd, velocity=scene.velocity, radius=scene.radius, gravity=scene.gravity,
+                fixed=scene.fixed if len(scene.fixed) else None, dt=scene.dt, scene_offsets=scene.scene_offsets,
+                linear_solver_maxiter=scene.maxiter, linear_solver_tolerance=scene.tolerance)
+    if scene.ground_plane is not None:
+        args["ground_plane"] = scene.ground_plane
+    args.update(kw)
+    return make_pair(scene.x, scene.mass, **args)
+
+
+def to_np(t):
+    return t.detach().cpu().numpy().astype(np.float64)
+
+
+def tensor(a):
+    return torch.tensor(np.asarray(a, np.float32), device=DEVICE)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def small_batch(count=6, seed=11):
+    return scenes.batched_scenes(count=count, seed=seed, dims=(2, 5))

@@ -1,0 +1,72 @@
+"""The C-ABI library loads and exports every symbol ``include/fem_gb300.h`` declares (no GPU calls)."""
+
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from newton_solver_fem_gb300 import _lib, build
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "fem_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(fem_\w+)\s*\(", text, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def library():
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_reference_boundary():
+    names = declared_functions()
+    for required in ("fem_create", "fem_destroy", "fem_step", "fem_refresh_tangent", "fem_set_tolerance",
+                     "fem_get_stats", "fem_export_bsr"):
+        assert required in names
+
+
+def test_every_declared_symbol_is_exported_and_bound(library):
+    names = declared_functions()
+    bound = {name for name, _, _ in _lib.SIGNATURES}
+    for name in names:
+        assert hasattr(library, name), name
+        assert name in bound, f"{name} missing from _lib.SIGNATURES"
+    assert library.fem_version().decode().startswith("fem_gb300")
+
+
+def test_ctypes_struct_layout_matches_c(tmp_path):
+    """sizeof/offsetof of FemDesc and FemStats as gcc lays them out equal the ctypes mirrors."""
+    fields = [name for name, _ in _lib.FemDesc._fields_]
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {",
+             'printf("%zu %zu\\n", sizeof(FemDesc), sizeof(FemStats));']
+    lines += [f'printf("%zu\\n", offsetof(FemDesc, {f}));' for f in fields]
+    lines += ["return 0; }"]
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert int(out[0]) == ctypes.sizeof(_lib.FemDesc)
+    assert int(out[1]) == ctypes.sizeof(_lib.FemStats)
+    for f, off in zip(fields, out[2:]):
+        assert getattr(_lib.FemDesc, f).offset == int(off), f
+
+
+def test_bad_arguments_are_rejected_without_a_gpu(library):
+    """Argument validation happens on the host before any device call."""
+    d = _lib.FemDesc()
+    d.particle_count = 4
+    d.tolerance = 0.0  # invalid
+    h = ctypes.c_void_p()
+    code = library.fem_create(ctypes.byref(d), ctypes.byref(h))
+    assert code == _lib.FEM_ERR_BAD_ARG
+    assert library.fem_create(None, ctypes.byref(h)) == _lib.FEM_ERR_BAD_ARG
+    with pytest.raises(ValueError):
+        _lib.check(code)
