@@ -348,7 +348,8 @@ def model_from_arrays(
         poses = np.zeros((0, 3, 3), np.float32)
     m.tet_indices = torch.tensor(tets, **i32)
     m.tet_poses = torch.tensor(poses, **f32)
-    m.tet_materials = torch.tensor(np.asarray(tet_materials, np.float32).reshape(-1, 3), **f32)
+    mats = np.zeros((0, 3), np.float32) if tet_materials is None or not len(tets) else tet_materials
+    m.tet_materials = torch.tensor(np.asarray(mats, np.float32).reshape(-1, 3), **f32)
     m.tet_activations = torch.zeros(len(tets), **f32)
     springs = np.zeros((0, 2), np.int32) if springs is None else np.asarray(springs, np.int32).reshape(-1, 2)
     m.spring_indices = torch.tensor(springs.reshape(-1), **i32)

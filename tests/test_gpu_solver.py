@@ -183,7 +183,7 @@ def test_step_matches_dense_solve_and_preserves_inputs():
     np.testing.assert_allclose(to_np(s1.particle_qd), velocity + inc, rtol=3e-4, atol=3e-6)
     np.testing.assert_allclose(to_np(s1.particle_q), q + DT * (velocity + inc), rtol=1e-6, atol=1e-7)
     np.testing.assert_array_equal(to_np(s0.particle_q), rounded(q))
-    np.testing.assert_array_equal(to_np(ext), force)
+    np.testing.assert_array_equal(to_np(ext), rounded(force))
 
 
 @pytest.mark.parametrize("tol", [1e-2, 1e-5])
