@@ -134,9 +134,11 @@ def build_workload(cells: int, device: str):
     sc = scenes.hex_block_64(n=cells)
     model = model_from_arrays(sc.x, sc.mass, hexes=sc.hexes, hex_materials=sc.hex_materials, velocity=sc.velocity,
                               radius=0.0, gravity=sc.gravity, device=device)
+    ke, kd, kf, mu = sc.ground
     solver = SolverFEM(model, dt=sc.dt, solver_type="cg", preconditioner_type="block_diag",
                        linear_solver_maxiter=sc.maxiter, linear_solver_tolerance=sc.tolerance,
-                       ground_plane=sc.ground_plane, self_contact_ke=0.0)
+                       ground_plane=sc.ground_plane, ground_ke=ke, ground_kd=kd, ground_kf=kf, ground_mu=mu,
+                       self_contact_ke=0.0)
     return sc, model, solver, np
 
 
@@ -169,7 +171,8 @@ def cpu_port(cells: int):
     inv, det = O.hex_builder_data(x, sc.hexes)
     port = fem_port.PortFEM(x, sc.mass.astype(np.float32), hexes=sc.hexes, hex_inv_J0=inv.astype(np.float32),
                             hex_det_J0_w=det.astype(np.float32), hex_materials=sc.hex_materials, dt=sc.dt,
-                            ground_plane=sc.ground_plane, maxiter=sc.maxiter, tolerance=sc.tolerance)
+                            ground_plane=sc.ground_plane, ground=sc.ground, maxiter=sc.maxiter,
+                            tolerance=sc.tolerance)
     return sc, port, x.astype(np.float32), sc.velocity.astype(np.float32), fem_port.threads()
 
 

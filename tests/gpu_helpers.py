@@ -60,6 +60,7 @@ def scene_pair(scene, **kw):
                 linear_solver_maxiter=scene.maxiter, linear_solver_tolerance=scene.tolerance)
     if scene.ground_plane is not None:
         args["ground_plane"] = scene.ground_plane
+        args.update(zip(("ground_ke", "ground_kd", "ground_kf", "ground_mu"), scene.ground))
     args.update(kw)
     return make_pair(scene.x, scene.mass, **args)
 

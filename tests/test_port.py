@@ -13,6 +13,7 @@ def _pair(sc, **kw):
     m = sc.mass.astype(np.float32).astype(np.float64)
     common = dict(gravity=sc.gravity, dt=sc.dt, ground_plane=sc.ground_plane, fixed=sc.fixed if len(sc.fixed) else None)
     common.update(kw)
+    ke, kd, kf, mu = sc.ground
     args = {}
     if len(sc.tets):
         args.update(tets=sc.tets, tet_poses=scenes.tet_poses(x, sc.tets), tet_materials=sc.tet_materials)
@@ -20,8 +21,8 @@ def _pair(sc, **kw):
         inv, det = O.hex_builder_data(x, sc.hexes)
         args.update(hexes=sc.hexes, hex_inv_J0=inv.astype(np.float32), hex_det_J0_w=det.astype(np.float32),
                     hex_materials=sc.hex_materials)
-    port = fem_port.PortFEM(x, m, **args, **common)
-    oracle = O.OracleFEM(x, m, **args, **common)
+    port = fem_port.PortFEM(x, m, ground=sc.ground, **args, **common)
+    oracle = O.OracleFEM(x, m, ground_ke=ke, ground_kd=kd, ground_kf=kf, ground_mu=mu, **args, **common)
     return x, port, oracle
 
 
