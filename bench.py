@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--cpu-sample", type=float, default=20.0, help="seconds budget for the CPU baseline sample")
     p.add_argument("--cpu-cells", type=int, default=None, help="Hex8 cells per axis of the CPU sample (default: same)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched vs plain measurement")
     return p.parse_args()
 
 
@@ -241,6 +242,75 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def scene_solver(sc, device, scene_offsets=None):
+    from newton_solver_fem_gb300 import SolverFEM, model_from_arrays
+
+    model = model_from_arrays(sc.x, sc.mass, tets=sc.tets if len(sc.tets) else None, tet_materials=sc.tet_materials,
+                              hexes=sc.hexes if len(sc.hexes) else None, hex_materials=sc.hex_materials,
+                              velocity=sc.velocity, radius=sc.radius, gravity=sc.gravity,
+                              scene_offsets=scene_offsets, device=device)
+    solver = SolverFEM(model, dt=sc.dt, solver_type="cg", preconditioner_type="block_diag",
+                       linear_solver_maxiter=sc.maxiter, linear_solver_tolerance=sc.tolerance, self_contact_ke=0.0,
+                       fixed_particle_indices=sc.fixed if len(sc.fixed) else None)
+    return model, solver
+
+
+def batched_measurement(device: str, steps: int, warmup: int) -> dict:
+    """256 uneven scenes: one batched handle vs each scene stepped alone (both as captured frame graphs)."""
+    import torch
+
+    from newton_solver_fem_gb300 import scenes
+
+    sc = scenes.batched_scenes()
+    model, batched = scene_solver(sc, device, sc.scene_offsets)
+    parts = [scene_solver(s, device) for s in scenes.split_batched(sc)]
+    P = model.particle_count
+    stream = torch.cuda.Stream(device)
+
+    def frame(pairs):
+        for mdl, slv, a, b in pairs:
+            slv.refresh_tangent(a.particle_q)
+            for _ in range(sc.substeps):
+                slv.step(a, b, None, None, sc.dt)
+                a, b = b, a
+
+    runs = {
+        "batched": [(model, batched, model.state(), model.state())],
+        "plain": [(m, s, m.state(), m.state()) for m, s in parts],
+    }
+    out = {}
+    for name, pairs in runs.items():
+        with torch.cuda.stream(stream):
+            frame(pairs)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            with torch.cuda.graph(graph, stream=stream):
+                frame(pairs)
+        for _ in range(max(3, warmup)):
+            graph.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                graph.replay()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        iters = [p[1].stats()["scene_iterations"] for p in pairs]
+        flat = [i for it in iters for i in it]
+        finite = all(bool(torch.isfinite(p[2].particle_q).all()) for p in pairs)
+        out[name] = {"ms_per_frame": ms, "value": 3 * P * sc.substeps / (ms / 1e3), "unit": UNIT,
+                     "mean_cg_iterations_last_substep": float(sum(flat) / len(flat)), "finite": finite}
+        del graph
+    out["scenes"] = len(sc.scene_offsets) - 1
+    out["nodes"] = P
+    out["speedup_batched_vs_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    out["workload"] = "256 scenes (128 Tet4, 128 Hex8), dims U{4..32}^3, cell 0.05 m, one face fixed, gravity"
+    return out
+
+
 def run_gb300(args) -> None:
     import torch
 
@@ -339,6 +409,9 @@ def run_gb300(args) -> None:
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_value = world * 3 * P * substeps / e2e_s
     finite = bool(torch.isfinite(s0.particle_q).all())
+    batched = None
+    if not args.no_batched and rank == 0:
+        batched = batched_measurement(device, args.steps, args.warmup)
 
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_baseline(args.cpu_cells or args.cells, args.cpu_sample)
@@ -360,6 +433,7 @@ def run_gb300(args) -> None:
             "clocks": clk,
             "cpu_baseline": cpu,
             "finite": finite,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -319,6 +319,26 @@ def batched_scenes(count: int = 256, seed: int = 5, cell: float = 0.05, dims=(4,
     )
 
 
+def split_batched(scene: Scene) -> list[Scene]:
+    """The independent scenes of a batched Scene, each re-indexed from node 0."""
+    out = []
+    offs = scene.scene_offsets
+    for s in range(len(offs) - 1):
+        lo, hi = int(offs[s]), int(offs[s + 1])
+        tsel = np.all((scene.tets >= lo) & (scene.tets < hi), axis=1) if len(scene.tets) else np.zeros(0, bool)
+        hsel = np.all((scene.hexes >= lo) & (scene.hexes < hi), axis=1) if len(scene.hexes) else np.zeros(0, bool)
+        fixed = scene.fixed[(scene.fixed >= lo) & (scene.fixed < hi)] - lo
+        out.append(Scene(
+            f"{scene.name}[{s}]", scene.x[lo:hi], scene.mass[lo:hi],
+            tets=(scene.tets[tsel] - lo).astype(np.int32) if tsel.any() else np.zeros((0, 4), np.int32),
+            tet_materials=scene.tet_materials[tsel] if tsel.any() else np.zeros((0, 3), np.float32),
+            hexes=(scene.hexes[hsel] - lo).astype(np.int32) if hsel.any() else np.zeros((0, 8), np.int32),
+            hex_materials=scene.hex_materials[hsel] if hsel.any() else np.zeros((0, 3), np.float32),
+            fixed=fixed.astype(np.int32), gravity=scene.gravity, substeps=scene.substeps, frames=scene.frames,
+            maxiter=scene.maxiter, tolerance=scene.tolerance, seed=scene.seed))
+    return out
+
+
 CONFIGS = {
     "tet4_cantilever": tet_cantilever,
     "hex8_block": hex_block_64,

@@ -300,6 +300,7 @@ class SolverFEM:
             "min_iterations": s.min_iterations,
             "max_relative_residual": s.max_relative_residual,
             "unconverged_scenes": s.unconverged_scenes,
+            "total_iterations": s.total_iterations,
             "scene_iterations": list(iters)[: self.model.scene_count],
         }
 
