@@ -487,7 +487,7 @@ int fem_create(const FemDesc* d, FemHandle** out) {
         h.cta_seg_base = b.upload(cta_seg_base);
         h.cta_first_scene = b.upload(cta_first_scene);
         h.scene_seg0 = b.upload(scene_seg0);
-        h.seg_part = b.alloc<double>(3 * (size_t)std::max(1, nseg));
+        h.seg_part = b.alloc<double>(2 * 3 * (size_t)std::max(1, nseg));
     }
     if (b.status != FEM_OK) {
         int code = b.status;

@@ -46,7 +46,8 @@ struct PcgArgs {
     const int* __restrict__ scene_slice0;     // [S+1]
     const int* __restrict__ scene_seg0;       // [S+1]
     int nscenes;
-    double* seg_part;  // [nseg * 3]
+    double* seg_part;  // [2][nseg * 3], alternating between consecutive reductions
+    int nseg;
     // node data
     const float4* __restrict__ v4;     // packed velocity (fixed zeroed)
     const float4* __restrict__ q4;     // packed positions (fixed restored)

@@ -141,8 +141,12 @@ struct Smem {
 };
 
 // Per-CTA segment partials: sum (or max) of the slice partials of each scene
-// this CTA covers, in slice order, written to seg_part.
-__device__ void write_segments(const PcgArgs& a, const Smem& sm, int nv, bool is_max, int first, int last) {
+// this CTA covers, in slice order, written to buf.  Consecutive reductions
+// alternate between two buffers: a CTA that races ahead can only write a
+// buffer again after the next grid barrier, which every CTA reaches only once
+// it has finished reading that buffer's previous contents.
+__device__ void write_segments(const PcgArgs& a, const Smem& sm, double* buf, int nv, bool is_max, int first,
+                               int last) {
     __syncthreads();
     if (first >= last) return;
     int s0 = a.cta_first_scene[blockIdx.x];
@@ -156,14 +160,14 @@ __device__ void write_segments(const PcgArgs& a, const Smem& sm, int nv, bool is
                 double v = (double)sm.part[(sl - first) * 3 + k];
                 acc = is_max ? fmax(acc, v) : acc + v;
             }
-            a.seg_part[(size_t)(a.cta_seg_base[blockIdx.x] + t) * 3 + k] = acc;
+            buf[(size_t)(a.cta_seg_base[blockIdx.x] + t) * 3 + k] = acc;
         }
     }
 }
 
 // After a grid barrier: every CTA forms the per-scene totals from the segment
 // partials in the same fixed order.
-__device__ void scene_totals(const PcgArgs& a, const Smem& sm, int nv, bool is_max) {
+__device__ void scene_totals(const PcgArgs& a, const Smem& sm, const double* buf, int nv, bool is_max) {
     int S = a.nscenes;
     if (S <= 4) {
         int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -172,7 +176,7 @@ __device__ void scene_totals(const PcgArgs& a, const Smem& sm, int nv, bool is_m
             double acc[3] = {0.0, 0.0, 0.0};
             for (int g = lo + threadIdx.x; g < hi; g += blockDim.x)
                 for (int k = 0; k < nv; ++k) {
-                    double v = a.seg_part[(size_t)g * 3 + k];
+                    double v = buf[(size_t)g * 3 + k];
                     acc[k] = is_max ? fmax(acc[k], v) : acc[k] + v;
                 }
             for (int k = 0; k < nv; ++k) {
@@ -195,7 +199,7 @@ __device__ void scene_totals(const PcgArgs& a, const Smem& sm, int nv, bool is_m
             for (int k = 0; k < nv; ++k) {
                 double t = 0.0;
                 for (int g = lo; g < hi; ++g) {
-                    double v = a.seg_part[(size_t)g * 3 + k];
+                    double v = buf[(size_t)g * 3 + k];
                     t = is_max ? fmax(t, v) : t + v;
                 }
                 sm.tot[s * 3 + k] = t;
@@ -275,9 +279,11 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
         mx = warp_max(mx);
         if (lane == 0) sm.part[(sl - first) * 3] = mx;
     }
-    write_segments(a, sm, 1, true, first, last);
+    double* const buf0 = a.seg_part;
+    double* const buf1 = a.seg_part + (size_t)a.nseg * 3;
+    write_segments(a, sm, buf0, 1, true, first, last);
     if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
-    scene_totals(a, sm, 1, true);
+    scene_totals(a, sm, buf0, 1, true);
     for (int s = threadIdx.x; s < S; s += blockDim.x) {
         float mxs = (float)sm.tot[s * 3];
         sm.st[s].scale = rhs_scale(mxs);
@@ -315,9 +321,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
             p[0] = rr; p[1] = rz; p[2] = bb;
         }
     }
-    write_segments(a, sm, 3, false, first, last);
+    write_segments(a, sm, buf1, 3, false, first, last);
     if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
-    scene_totals(a, sm, 3, false);
+    scene_totals(a, sm, buf1, 3, false);
     if (threadIdx.x == 0) s_any = 0;
     __syncthreads();
     for (int s = threadIdx.x; s < S; s += blockDim.x) {
@@ -380,9 +386,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
             pap = warp_sum(pap);
             if (lane == 0) sm.part[(sl - first) * 3] = pap;
         }
-        write_segments(a, sm, 1, false, first, last);
+        write_segments(a, sm, buf0, 1, false, first, last);
         if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
-        scene_totals(a, sm, 1, false);
+        scene_totals(a, sm, buf0, 1, false);
         for (int s = threadIdx.x; s < S; s += blockDim.x) {
             SceneState& st = sm.st[s];
             if (st.active) st.alpha = (float)(st.rz / sm.tot[s * 3]);
@@ -414,9 +420,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
                 p[0] = rr; p[1] = rz;
             }
         }
-        write_segments(a, sm, 2, false, first, last);
+        write_segments(a, sm, buf1, 2, false, first, last);
         if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
-        scene_totals(a, sm, 2, false);
+        scene_totals(a, sm, buf1, 2, false);
         if (threadIdx.x == 0) s_any = 0;
         __syncthreads();
         for (int s = threadIdx.x; s < S; s += blockDim.x) {
@@ -538,6 +544,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.scene_seg0 = h.scene_seg0;
     a.nscenes = h.nscenes;
     a.seg_part = h.seg_part;
+    a.nseg = h.nseg;
     a.v4 = h.v4;
     a.q4 = h.q4;
     a.rest = h.rest;
