@@ -166,6 +166,25 @@ int fem_export_preconditioner(FemHandle* handle, float* inverse_blocks, void* st
 /* Raw element/constant blocks in the reference's triplet layout [P | 2S | 16T | 64H] (bsr_values). */
 int fem_export_triplets(FemHandle* handle, int32_t* rows, int32_t* columns, float* values, void* stream);
 
+/* Block-Jacobi PCG on a caller-supplied BSR matrix that allocates no device
+ * memory.  No counterpart in the reference: it exists for callers that cannot
+ * call cudaMalloc at solve time (a host application that owns all device
+ * memory or forbids runtime allocations, or a real-time loop that cannot take
+ * an allocation's implicit synchronisation), which rules out fem_create.
+ * offsets [rows+1], columns [nnzb], values [nnzb,3,3], rhs [rows,3] and
+ * x_inout [rows,3] (warm start in, solution out) are device pointers; info is
+ * an optional device int[2] receiving (iterations, status).  Solves
+ * A x = rhs to ||r|| <= tolerance ||rhs|| with the reference's RHS
+ * normalisation and at most maxiter iterations.  Working vectors live in a
+ * static device array sized for at most 65,536 block rows (about 6.5 MB per
+ * GPU that loads the library, held until exit); larger systems return
+ * FEM_ERR_BAD_ARG.  The first call on a device resolves that array's address
+ * and must come before any stream capture.  All calls share the array, so
+ * calls that overlap on the GPU race; serialise them. */
+int fem_pcg_solve_noalloc(const int32_t* offsets, const int32_t* columns, const float* values, const float* rhs,
+                          float* x_inout, int32_t rows, float tolerance, int32_t maxiter, int32_t* info,
+                          void* stream);
+
 const char* fem_status_string(int status);
 const char* fem_version(void);
 

@@ -113,6 +113,7 @@ SIGNATURES = [
     ("fem_export_bsr", _i32, [_p, _p, _p, _p, _p]),
     ("fem_export_preconditioner", _i32, [_p, _p, _p]),
     ("fem_export_triplets", _i32, [_p, _p, _p, _p, _p]),
+    ("fem_pcg_solve_noalloc", _i32, [_p, _p, _p, _p, _p, _i32, _f, _i32, _p, _p]),
     ("fem_status_string", ctypes.c_char_p, [_i32]),
     ("fem_version", ctypes.c_char_p, []),
 ]
