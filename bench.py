@@ -54,6 +54,7 @@ def parse():
     p.add_argument("--cpu-cells", type=int, default=None, help="Hex8 cells per axis of the CPU sample (default: same)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched vs plain measurement")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-beam gradient measurement")
     return p.parse_args()
 
 
@@ -311,6 +312,102 @@ def batched_measurement(device: str, steps: int, warmup: int) -> dict:
     return out
 
 
+def adjoint_measurement(device: str, repeats: int) -> dict:
+    """Differentiable beam (16x4x4 cubes, 1,536 tets, 120 frames x 4 substeps, 30 CG): gradient vs plain rollout.
+
+    Times (a) the plain forward rollout through ``SolverFEM.step`` (frame
+    graphs), (b) the recorded differentiable forward, (c) its backward pass
+    (adjoint solves + VJPs), and (d) the checkpointed gradient (checkpoints
+    every 10 frames: forward, then per-segment recomputation and backward).
+    """
+    import torch
+
+    from newton_solver_fem_gb300 import scenes
+    from newton_solver_fem_gb300.adjoint import DifferentiableSolver, checkpointed_gradient
+
+    sc = scenes.tet_beam()
+    model, solver = scene_solver(sc, device)
+    solver.linear_solver_tolerance = 1.0e-8
+    P = model.particle_count
+    steps = sc.frames * sc.substeps
+    every = sc.extra["checkpoint_every"] * sc.substeps
+    diff = DifferentiableSolver(solver, tolerance=1.0e-8, maxiter=sc.maxiter)
+    scale = torch.tensor(sc.extra["mu_scale"], device=device).requires_grad_(True)
+    diff.set_mu_scale(scale)
+    solver.refresh_tangent(model.particle_q.clone())
+    tip = torch.as_tensor(sc.extra["tip_nodes"], device=device, dtype=torch.long)
+    target = torch.tensor(sc.extra["target"], device=device, dtype=torch.float32)
+    q0 = model.particle_q.clone()
+
+    def step(q, v, k):
+        return diff.step(q, v, sc.dt, mu_scale=scale)
+
+    def loss_fn(q, v):
+        return ((q[tip].mean(0) - target) ** 2).sum()
+
+    def recorded():
+        q, v = q0, torch.zeros_like(q0).requires_grad_(True)
+        for k in range(steps):
+            q, v = step(q, v, k)
+        return loss_fn(q, v)
+
+    def wall(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t, out
+
+    # plain rollout: the same frames through SolverFEM.step, one captured graph per frame
+    a, b = model.state(), model.state()
+    stream = torch.cuda.Stream(device)
+
+    def plain_frame():
+        x, y = a, b
+        for _ in range(sc.substeps):
+            solver.step(x, y, None, None, sc.dt)
+            x, y = y, x
+
+    with torch.cuda.stream(stream):
+        plain_frame()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            plain_frame()
+
+    def plain():
+        with torch.cuda.stream(stream):
+            for _ in range(sc.frames):
+                graph.replay()
+
+    recorded().backward()  # warm-up of the recorded path
+    plain()
+    res = {"plain_s": [], "forward_s": [], "backward_s": [], "checkpointed_s": []}
+    for _ in range(max(1, repeats)):
+        res["plain_s"].append(wall(plain)[0])
+        t_f, loss = wall(recorded)
+        res["forward_s"].append(t_f)
+        res["backward_s"].append(wall(loss.backward)[0])
+        res["checkpointed_s"].append(wall(lambda: checkpointed_gradient(
+            step, q0, torch.zeros_like(q0), steps, every, loss_fn, params=(scale,)))[0])
+    med = {k: float(sorted(v)[len(v) // 2]) for k, v in res.items()}
+    dof_substeps = 3 * P * steps
+    del graph
+    return {
+        "workload": "tet4_beam_16x4x4 hanging (425 nodes, 1,536 tets), 120 frames x 4 substeps, 30 CG, "
+                    "loss on the tip-face centroid, gradients wrt 1,536 shear scales and v0",
+        "plain_value": dof_substeps / med["plain_s"], "unit": UNIT,
+        "forward_ms": 1e3 * med["forward_s"], "backward_ms": 1e3 * med["backward_s"],
+        "plain_ms": 1e3 * med["plain_s"], "checkpointed_gradient_ms": 1e3 * med["checkpointed_s"],
+        "backward_over_forward": med["backward_s"] / med["forward_s"],
+        "gradient_value": dof_substeps / (med["forward_s"] + med["backward_s"]),
+        "checkpointed_gradient_value": dof_substeps / med["checkpointed_s"],
+        "gradient_over_plain": med["plain_s"] / (med["forward_s"] + med["backward_s"]),
+        "timer": "wall clock around synchronised passes (host-driven autograd)", "repeats": max(1, repeats),
+    }
+
+
 def run_gb300(args) -> None:
     import torch
 
@@ -412,6 +509,9 @@ def run_gb300(args) -> None:
     batched = None
     if not args.no_batched and rank == 0:
         batched = batched_measurement(device, args.steps, args.warmup)
+    adjoint = None
+    if not args.no_adjoint and rank == 0:
+        adjoint = adjoint_measurement(device, 3)
 
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_baseline(args.cpu_cells or args.cells, args.cpu_sample)
@@ -434,6 +534,7 @@ def run_gb300(args) -> None:
             "cpu_baseline": cpu,
             "finite": finite,
             "batched": batched,
+            "adjoint": adjoint,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

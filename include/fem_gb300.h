@@ -142,6 +142,15 @@ int fem_set_tolerance(FemHandle* handle, float tolerance);
  * default 2e9.  A wait that runs out makes the kernel return early and sets the
  * sticky FEM_ERR_TIMEOUT status that fem_get_stats reports. */
 int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
+
+/* Launch tuning of the persistent PCG kernel (chosen by an autotuner).  Not
+ * capturable: a change rebuilds the launch tables. */
+#define FEM_TUNE_SPMV_UNROLL 1       /* block columns in flight per thread: 1, 2 or 4 (default 4) */
+#define FEM_TUNE_L2_RESIDENT_BYTES 2 /* matrix bytes loaded evict_last (kept in L2 across iterations); -1 = 60% of L2; default 0 */
+#define FEM_TUNE_RESIDENT_SLICES 3   /* read-only: resulting number of L2-resident 32-row slices */
+#define FEM_TUNE_GRID 4              /* read-only: cooperative grid size */
+int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
+int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);
 int fem_reset(FemHandle* handle, void* stream);
 float* fem_velocity_increment_ptr(FemHandle* handle);
@@ -165,6 +174,31 @@ int fem_export_bsr(FemHandle* handle, int32_t* offsets, int32_t* columns, float*
 int fem_export_preconditioner(FemHandle* handle, float* inverse_blocks, void* stream);
 /* Raw element/constant blocks in the reference's triplet layout [P | 2S | 16T | 64H] (bsr_values). */
 int fem_export_triplets(FemHandle* handle, int32_t* rows, int32_t* columns, float* values, void* stream);
+
+/* ---- Differentiation with the system matrix held fixed (the reference's
+ * differentiable branch, differentiation.py:149-394).  A substep is
+ * rhs = h sum f(q, v, a) + h ext - sum_j A_ij (v_j - v_i) + spring damping,
+ * dv = (PAP + I - P)^-1 P rhs, v' = v + dv, q' = q + h v'.  Its VJP uses a
+ * second solve with the same symmetric A (fem_solve), the force VJP
+ * (fem_force_vjp) and the predictor VJP (fem_predictor_vjp). */
+
+/* Optional per-tet shear scale (device [T], NULL to clear) multiplying mu in
+ * the force and tangent kernels; the pointer is read at every launch.  Beyond
+ * the reference (its differentiable controls are the additive activations). */
+int fem_set_mu_scale(FemHandle* handle, const float* scale);
+/* Solve (PAP + I - P) x = P rhs from x = 0 to ||r|| <= tolerance ||P rhs||
+ * (at most maxiter iterations) with the reference's RHS normalisation. */
+int fem_solve(FemHandle* handle, const float* rhs, float* x, float tolerance, int32_t maxiter, void* stream);
+/* Accumulate (d sum f / d q)^T force_bar into q_bar and (d sum f / d v)^T
+ * force_bar into v_bar over all force terms at (q, v, activations); write
+ * dL/d activation and dL/d mu_scale per tet when those pointers are given.
+ * The first call allocates adjoint scratch (call it once before capture). */
+int fem_force_vjp(FemHandle* handle, const float* q, const float* v, const float* activations, const float* gravity,
+                  const float* force_bar, float* q_bar, float* v_bar, float* activation_bar, float* mu_scale_bar,
+                  void* stream);
+/* Accumulate the predictor's VJP into v_bar: -(A rhs_bar)_k + (sum_j A_kj)^T rhs_bar_k
+ * plus the spring-damping term (implicit_predictor.py:9-41). */
+int fem_predictor_vjp(FemHandle* handle, const float* rhs_bar, float dt, float* v_bar, void* stream);
 
 /* Block-Jacobi PCG on a caller-supplied BSR matrix that allocates no device
  * memory.  No counterpart in the reference: it exists for callers that cannot

@@ -22,6 +22,11 @@ FEM_ERR_UNSUPPORTED = 6
 FEM_PRECOND_BLOCK_DIAG = 0
 FEM_PRECOND_DIAG = 1
 
+FEM_TUNE_SPMV_UNROLL = 1
+FEM_TUNE_L2_RESIDENT_BYTES = 2
+FEM_TUNE_RESIDENT_SLICES = 3
+FEM_TUNE_GRID = 4
+
 FEM_TERM_SPRING = 1
 FEM_TERM_TET = 2
 FEM_TERM_HEX = 4
@@ -102,6 +107,8 @@ SIGNATURES = [
     ("fem_set_tolerance", _i32, [_p, _f]),
     ("fem_set_maxiter", _i32, [_p, _i32]),
     ("fem_set_wait_limit", _i32, [_p, ctypes.c_int64]),
+    ("fem_set_tuning", _i32, [_p, _i32, ctypes.c_int64]),
+    ("fem_get_tuning", _i32, [_p, _i32, ctypes.POINTER(ctypes.c_int64)]),
     ("fem_reset", _i32, [_p, _p]),
     ("fem_velocity_increment_ptr", _p, [_p]),
     ("fem_get_stats", _i32, [_p, ctypes.POINTER(FemStats), _p, _p]),
@@ -113,6 +120,10 @@ SIGNATURES = [
     ("fem_export_bsr", _i32, [_p, _p, _p, _p, _p]),
     ("fem_export_preconditioner", _i32, [_p, _p, _p]),
     ("fem_export_triplets", _i32, [_p, _p, _p, _p, _p]),
+    ("fem_set_mu_scale", _i32, [_p, _p]),
+    ("fem_solve", _i32, [_p, _p, _p, _f, _i32, _p]),
+    ("fem_force_vjp", _i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
+    ("fem_predictor_vjp", _i32, [_p, _p, _f, _p, _p]),
     ("fem_pcg_solve_noalloc", _i32, [_p, _p, _p, _p, _p, _i32, _f, _i32, _p, _p]),
     ("fem_status_string", ctypes.c_char_p, [_i32]),
     ("fem_version", ctypes.c_char_p, []),

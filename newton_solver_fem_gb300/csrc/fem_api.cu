@@ -15,14 +15,8 @@
 #include "fem_internal.cuh"
 
 namespace fem {
-void upload_hex_reference_table();
 size_t pcg_smem_bytes(int L, int S);
 }  // namespace fem
-
-struct FemHandle {
-    fem::Handle h;
-    int device = 0;
-};
 
 namespace {
 
@@ -109,6 +103,71 @@ int cuda_status(cudaError_t e, Handle* h = nullptr) {
     std::string msg = std::string("CUDA error: ") + cudaGetErrorString(e);
     if (h) h->last_error = msg;
     return set_error(FEM_ERR_CUDA, msg);
+}
+
+
+template <class T>
+T* upload_plain(const std::vector<T>& v, std::vector<void*>& owned, cudaError_t& err) {
+    if (v.empty() || err != cudaSuccess) return nullptr;
+    void* p = nullptr;
+    err = cudaMalloc(&p, v.size() * sizeof(T));
+    if (err != cudaSuccess) return nullptr;
+    owned.push_back(p);
+    err = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return (T*)p;
+}
+
+// (Re)compute the PCG grid for the handle's kernel variant, the per-(CTA,
+// scene) segment tables of the deterministic reductions and the L2-resident
+// slice count.  Allocates (at construction and on a tuning change only).
+int configure_launch(Handle& h) {
+    if (h.P == 0) return FEM_OK;
+    for (void* p : h.launch_allocations) cudaFree(p);
+    h.launch_allocations.clear();
+    cudaError_t err = fem::pcg_configure(h);
+    if (err != cudaSuccess) return cuda_status(err, &h);
+    const std::vector<int>& slice_scene = h.host_slice_scene;
+    const int nscenes = h.nscenes;
+    std::vector<int> cta_seg_base(h.grid, 0), cta_first_scene(h.grid, nscenes), scene_seg0(nscenes + 1, 0);
+    int nseg = 0, L = h.slices_per_cta;
+    std::vector<int> count(nscenes, 0);
+    for (int c = 0; c < h.grid; ++c) {
+        int first = c * L, last = std::min(first + L, h.nslices);
+        cta_seg_base[c] = nseg;
+        if (first >= last) continue;
+        cta_first_scene[c] = slice_scene[first];
+        for (int s = slice_scene[first]; s <= slice_scene[last - 1]; ++s) {
+            count[s]++;
+            ++nseg;
+        }
+    }
+    // segments are ordered by (cta, scene), which is also scene-major
+    for (int s = 0; s < nscenes; ++s) scene_seg0[s + 1] = scene_seg0[s] + count[s];
+    h.nseg = nseg;
+    h.cta_seg_base = upload_plain(cta_seg_base, h.launch_allocations, err);
+    h.cta_first_scene = upload_plain(cta_first_scene, h.launch_allocations, err);
+    h.scene_seg0 = upload_plain(scene_seg0, h.launch_allocations, err);
+    std::vector<double> zeros(2 * 3 * (size_t)std::max(1, nseg), 0.0);
+    h.seg_part = upload_plain(zeros, h.launch_allocations, err);
+    if (err != cudaSuccess) return cuda_status(err, &h);
+    // L2-resident prefix of the matrix stream (40 bytes per stored block)
+    int64_t budget = h.l2_resident_bytes;
+    if (budget < 0) {
+        int dev = 0, l2 = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+        budget = (int64_t)(0.6 * (double)l2);
+    }
+    int64_t acc = 0;
+    int rs = 0;
+    for (int sl = 0; sl < h.nslices; ++sl) {
+        int64_t bytes = (int64_t)(h.host_slice_ptr[sl + 1] - h.host_slice_ptr[sl]) * fem::kSlice * 40;
+        if (acc + bytes > budget) break;
+        acc += bytes;
+        ++rs;
+    }
+    h.resident_slices = rs;
+    return FEM_OK;
 }
 
 }  // namespace
@@ -226,6 +285,7 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     h.tol = d->tolerance;
     h.nfixed = d->fixed_count;
     fem::upload_hex_reference_table();
+    fem::upload_hex_reference_table_adjoint();
 
     // ---- empty-material tets produce no triplets (kernels.py:690-700)
     std::vector<unsigned char> tet_empty(T, 0);
@@ -459,42 +519,15 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     }
 
     // ---- launch configuration and deterministic-reduction segment tables
-    cudaError_t err = P > 0 ? fem::pcg_configure(h) : cudaSuccess;
-    if (err != cudaSuccess) {
-        int code = cuda_status(err);
-        fem_destroy(H);
-        return code;
-    }
-    if (P > 0) {
-        std::vector<int> cta_seg_base(h.grid, 0), cta_first_scene(h.grid, nscenes), scene_seg0(nscenes + 1, 0);
-        int nseg = 0, L = h.slices_per_cta;
-        std::vector<int> seg_scene;
-        for (int c = 0; c < h.grid; ++c) {
-            int first = c * L, last = std::min(first + L, h.nslices);
-            cta_seg_base[c] = nseg;
-            if (first >= last) continue;
-            cta_first_scene[c] = slice_scene[first];
-            for (int s = slice_scene[first]; s <= slice_scene[last - 1]; ++s) {
-                seg_scene.push_back(s);
-                ++nseg;
-            }
-        }
-        // segments are ordered by (cta, scene), which is also scene-major
-        std::vector<int> count(nscenes, 0);
-        for (int s : seg_scene) count[s]++;
-        for (int s = 0; s < nscenes; ++s) scene_seg0[s + 1] = scene_seg0[s] + count[s];
-        h.nseg = nseg;
-        h.cta_seg_base = b.upload(cta_seg_base);
-        h.cta_first_scene = b.upload(cta_first_scene);
-        h.scene_seg0 = b.upload(scene_seg0);
-        h.seg_part = b.alloc<double>(2 * 3 * (size_t)std::max(1, nseg));
-    }
-    if (b.status != FEM_OK) {
-        int code = b.status;
+    h.host_slice_scene = slice_scene;
+    h.host_slice_ptr = slice_ptr;
+    int code = configure_launch(h);
+    if (code != FEM_OK) {
         g_error = h.last_error;
         fem_destroy(H);
         return code;
     }
+    cudaError_t err = cudaSuccess;
 
     // ---- initial assembly at the construction positions (solver.py:330-341)
     cudaStream_t s0 = nullptr;
@@ -516,6 +549,7 @@ int fem_destroy(FemHandle* H) {
     if (H == nullptr) return FEM_OK;
     DeviceGuard g(H->device);
     for (cudaEvent_t e : H->h.timing_events) cudaEventDestroy(e);
+    for (void* p : H->h.launch_allocations) cudaFree(p);
     for (void* p : H->h.allocations) cudaFree(p);
     delete H;
     return FEM_OK;
@@ -635,6 +669,36 @@ int fem_set_tolerance(FemHandle* H, float tolerance) {
         return set_error(FEM_ERR_BAD_ARG, "linear_solver_tolerance must be finite and positive");
     H->h.tol = tolerance;
     return FEM_OK;
+}
+
+int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
+    Handle& h = H->h;
+    DeviceGuard g(H->device);
+    if (key == FEM_TUNE_SPMV_UNROLL) {
+        if (value != 1 && value != 2 && value != 4) return set_error(FEM_ERR_BAD_ARG, "unroll must be 1, 2 or 4");
+        h.spmv_unroll = (int)value;
+    } else if (key == FEM_TUNE_L2_RESIDENT_BYTES) {
+        if (value < -1) return set_error(FEM_ERR_BAD_ARG, "resident bytes must be >= -1");
+        h.l2_resident_bytes = value;
+    } else {
+        return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_status(e, &h);
+    return configure_launch(h);
+}
+
+int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
+    if (H == nullptr || value == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle or output");
+    Handle& h = H->h;
+    switch (key) {
+        case FEM_TUNE_SPMV_UNROLL: *value = h.spmv_unroll; return FEM_OK;
+        case FEM_TUNE_L2_RESIDENT_BYTES: *value = h.l2_resident_bytes; return FEM_OK;
+        case FEM_TUNE_RESIDENT_SLICES: *value = h.resident_slices; return FEM_OK;
+        case FEM_TUNE_GRID: *value = h.grid; return FEM_OK;
+        default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
+    }
 }
 
 int fem_set_wait_limit(FemHandle* H, int64_t nanoseconds) {

@@ -58,12 +58,13 @@ __global__ void node_prepare_kernel(int P, float* __restrict__ q, float* __restr
 // restoring force of each corner into out[4 t + a].
 __global__ void tet_force_kernel(int T, const int4* __restrict__ idx, const float* __restrict__ pose,
                                  const float* __restrict__ mat, const float4* __restrict__ q4,
-                                 const float4* __restrict__ v4, const float* __restrict__ act, float lo, float hi,
-                                 float4* __restrict__ out) {
+                                 const float4* __restrict__ v4, const float* __restrict__ act,
+                                 const float* __restrict__ mu_scale, float lo, float hi, float4* __restrict__ out) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T) return;
     int4 n = idx[t];
     float k_mu = mat[3 * t], k_lambda = mat[3 * t + 1], k_damp = mat[3 * t + 2];
+    if (mu_scale != nullptr) k_mu *= mu_scale[t];  // per-element shear scale (differentiable control)
     float4* o = out + 4 * t;
     if (k_mu == 0.0f && k_lambda == 0.0f && k_damp == 0.0f) {
         float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -345,13 +346,15 @@ constexpr int kTetFactor = 40;
 // the 576-byte block run of each element is written contiguously.
 __global__ void __launch_bounds__(kTetTangentThreads) tet_tangent_kernel(
     int T, const int4* __restrict__ idx, const float* __restrict__ pose, const float* __restrict__ mat,
-    const float4* __restrict__ q4, float lo, float hi, float dt, int64_t trip_off, float* __restrict__ vals) {
+    const float* __restrict__ mu_scale, const float4* __restrict__ q4, float lo, float hi, float dt, int64_t trip_off,
+    float* __restrict__ vals) {
     __shared__ float sm[kTetTangentThreads][kTetFactor + 1];
     int lt = threadIdx.x;
     int t = blockIdx.x * kTetTangentThreads + lt;
     float* fct = sm[lt];
     if (t < T) {
         float k_mu = mat[3 * t], k_lambda = mat[3 * t + 1];
+        if (mu_scale != nullptr) k_mu *= mu_scale[t];
         if (k_mu == 0.0f && k_lambda == 0.0f && mat[3 * t + 2] == 0.0f) {
             fct[39] = 2.0f;  // empty material: rows/cols are -1, nothing to write
         } else {
@@ -545,14 +548,20 @@ inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) /
 }  // namespace
 
 void upload_hex_reference_table() {
-    // dN_a/dxi at Gauss point g, evaluated in float32 exactly as the
-    // reference's _hex_dN_dxi (kernels.py:1356-1419).  Once per device.
+    // Once per device.
     static bool done[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
     if (done[dev]) return;
-    const float gp = 0.5773502691896258f;
     float table[8][8][3];
+    fill_hex_reference_table(table);
+    if (cudaMemcpyToSymbol(c_dNdxi, table, sizeof(table)) == cudaSuccess) done[dev] = true;
+}
+
+// dN_a/dxi at Gauss point g, evaluated in float32 exactly as the reference's
+// _hex_dN_dxi (kernels.py:1356-1419).
+void fill_hex_reference_table(float table[8][8][3]) {
+    const float gp = 0.5773502691896258f;
     auto sgn_xi = [](int k) { return (k == 1 || k == 2 || k == 5 || k == 6) ? 1.0f : -1.0f; };
     auto sgn_eta = [](int k) { return (k == 2 || k == 3 || k == 6 || k == 7) ? 1.0f : -1.0f; };
     auto sgn_zeta = [](int k) { return (k >= 4) ? 1.0f : -1.0f; };
@@ -565,7 +574,6 @@ void upload_hex_reference_table() {
             table[g][a][2] = (1.0f + xa * xi) * (1.0f + ya * eta) * za * 0.125f;
         }
     }
-    if (cudaMemcpyToSymbol(c_dNdxi, table, sizeof(table)) == cudaSuccess) done[dev] = true;
 }
 
 cudaError_t launch_node_prepare(Handle& h, float* q, float* v, bool restore_fixed, bool pack_v, bool pack_x,
@@ -579,8 +587,8 @@ cudaError_t launch_node_prepare(Handle& h, float* q, float* v, bool restore_fixe
 cudaError_t launch_element_forces(Handle& h, const float* activations, cudaStream_t s) {
     if (h.T > 0) {
         tet_force_kernel<<<blocks_for(h.T, 128), 128, 0, s>>>(h.T, h.tet_idx, h.tet_pose, h.tet_mat, h.q4, h.v4,
-                                                              h.enable_act ? activations : nullptr, h.min_stretch,
-                                                              h.max_stretch, h.elem_force);
+                                                              h.enable_act ? activations : nullptr, h.mu_scale,
+                                                              h.min_stretch, h.max_stretch, h.elem_force);
     }
     if (h.H > 0) {
         hex_force_kernel<<<blocks_for(8 * (int64_t)h.H, 256), 256, 0, s>>>(
@@ -642,7 +650,8 @@ cudaError_t launch_element_tangent(Handle& h, float dt, cudaStream_t s) {
     int64_t tet_off = (int64_t)h.P + 2 * (int64_t)h.S;
     if (h.T > 0)
         tet_tangent_kernel<<<blocks_for(h.T, kTetTangentThreads), kTetTangentThreads, 0, s>>>(
-            h.T, h.tet_idx, h.tet_pose, h.tet_mat, h.q4, h.min_stretch, h.max_stretch, dt, tet_off, h.trip_vals);
+            h.T, h.tet_idx, h.tet_pose, h.tet_mat, h.mu_scale, h.q4, h.min_stretch, h.max_stretch, dt, tet_off,
+            h.trip_vals);
     if (h.H > 0)
         hex_tangent_kernel<<<blocks_for(h.H, kHexPerCta), 256, 0, s>>>(
             h.H, h.hex_idx, h.hex_invJ, h.hex_detw, h.hex_mat, h.q4, h.min_stretch, h.max_stretch, dt,

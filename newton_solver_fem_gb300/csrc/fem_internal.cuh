@@ -77,6 +77,8 @@ struct PcgArgs {
     float dt;
     long long limit_ns;  // give up a barrier wait after this many ns
     int write_state;  // 1: integrate state (step); 0: solve only
+    int resident_slices;  // slices [0, resident_slices) are loaded with the L2 evict_last policy
+    const float* solve_rhs;  // non-null: solve A x = solve_rhs from x0 = 0 (no predictor), x -> dv
 };
 
 struct Handle {
@@ -93,6 +95,9 @@ struct Handle {
     int enable_act = 0, precond = 0, maxiter = 50;
     float tol = 1e-2f;
     long long wait_limit_ns = 2000000000LL;
+    int spmv_unroll = 4;          // block columns in flight per thread in the PCG SpMV (1, 2 or 4)
+    int64_t l2_resident_bytes = 0;   // matrix bytes loaded evict_last (-1: 60% of L2); measured slower, so off
+    int resident_slices = 0;
     bool tangent_prepared = false;
     // node data
     float* rest = nullptr;
@@ -111,6 +116,8 @@ struct Handle {
     float* hex_invJ = nullptr;  // [H*72]
     float* hex_detw = nullptr;  // [H*8]
     float* hex_mat = nullptr;   // [H*3]
+    const float* mu_scale = nullptr;  // optional caller-owned per-tet shear scale [T]
+    float4* elem_grad = nullptr;      // adjoint scratch [2 * (4T + 8H)], allocated on first VJP
     int* spring_idx = nullptr;  // [2S]
     float* spring_rest = nullptr;
     float* spring_ke = nullptr;
@@ -167,8 +174,16 @@ struct Handle {
     bool timing = false;
     std::vector<cudaEvent_t> timing_events;  // start/end pairs
     std::vector<void*> allocations;
+    std::vector<void*> launch_allocations;  // segment tables, rebuilt on a tuning change
+    std::vector<int> host_slice_scene;
+    std::vector<int> host_slice_ptr;
     std::string last_error;
 };
+
+// dN_a/dxi at the 8 Gauss points (host copy, filled as the reference computes it)
+void fill_hex_reference_table(float table[8][8][3]);
+void upload_hex_reference_table();          // fem_elements.cu copy
+void upload_hex_reference_table_adjoint();  // fem_adjoint.cu copy
 
 // --- launchers (fem_elements.cu) ---
 cudaError_t launch_node_prepare(Handle& h, float* q, float* v, bool restore_fixed, bool pack_v, bool pack_x,
@@ -184,6 +199,16 @@ cudaError_t launch_export_bsr(Handle& h, float* values, cudaStream_t s);
 cudaError_t launch_export_triplets(Handle& h, float* values, cudaStream_t s);
 // --- launchers (fem_pcg.cu) ---
 cudaError_t pcg_configure(Handle& h);
-cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s);
+// Step mode (solve_rhs == nullptr): predictor, normalised PCG from the dv warm start, integration.
+// Solve mode: A x = solve_rhs from zero (projected at fixed rows), x written to x_out.
+cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s,
+                       const float* solve_rhs = nullptr, float* x_out = nullptr, float tol = -1.0f,
+                       int maxiter = -1);
 
 }  // namespace fem
+
+// The opaque handle of the C ABI.
+struct FemHandle {
+    fem::Handle h;
+    int device = 0;
+};

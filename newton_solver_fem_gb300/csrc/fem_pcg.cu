@@ -133,6 +133,116 @@ __device__ __forceinline__ float3 next_p(float4 z, float4 p, float beta) {
     return f3(fmaf(beta, p.x, z.x), fmaf(beta, p.y, z.y), fmaf(beta, p.z, z.z));
 }
 
+// ---------------------------------------------------------------------------
+// Matrix stream loads.  The matrix is read-only during the kernel, so it goes
+// through the non-coherent path without L1 allocation, with an L2 eviction
+// policy per slice: the first `resident_slices` slices are loaded evict_last
+// so that they stay in L2 from one CG iteration to the next, the rest
+// evict_first so that streaming them does not displace the resident part or
+// the CG vectors.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long policy_evict_last() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ unsigned long long policy_evict_first() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ float4 ld_mat4(const float4* p, unsigned long long pol) {
+    float4 v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float ld_mat1(const float* p, unsigned long long pol) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int ld_col(const int* p, unsigned long long pol) {
+    int v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+struct Entry {
+    float4 A, B;
+    float C;
+    int j;
+};
+
+__device__ __forceinline__ Entry load_entry(const PcgArgs& a, size_t e, unsigned long long pol) {
+    Entry m;
+    m.A = ld_mat4(a.valA + e, pol);
+    m.B = ld_mat4(a.valB + e, pol);
+    m.C = ld_mat1(a.valC + e, pol);
+    m.j = ld_col(a.scol + e, pol);
+    return m;
+}
+
+// y_row = sum_k A_k p_{j_k}, with p = z (first iteration) or z + beta p_old.
+// U block columns are loaded before any is used, so U entries (and then U
+// gathers) are in flight per thread; the sum keeps the k order of U = 1.
+template <int U, bool FIRST>
+__device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int len, int lane, const float4* pold,
+                                              float beta, unsigned long long pol) {
+    float3 acc = f3(0.f, 0.f, 0.f);
+    int k = 0;
+    if (U > 1) {
+        for (; k + U <= len; k += U) {
+            Entry m[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) m[u] = load_entry(a, (size_t)(base + k + u) * kSlice + lane, pol);
+            float3 p[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) p[u] = FIRST ? xyz(a.z[m[u].j]) : next_p(a.z[m[u].j], pold[m[u].j], beta);
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc = acc + bmul(m[u].A, m[u].B, m[u].C, p[u]);
+        }
+    }
+    for (; k < len; ++k) {
+        Entry m = load_entry(a, (size_t)(base + k) * kSlice + lane, pol);
+        float3 p = FIRST ? xyz(a.z[m.j]) : next_p(a.z[m.j], pold[m.j], beta);
+        acc = acc + bmul(m.A, m.B, m.C, p);
+    }
+    return acc;
+}
+
+// Prologue pass: cv = sum_k A_k (v_j - v_i) and ax = sum_k A_k x_j in one read of the row.
+template <int U>
+__device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int len, int lane, float3 vi, float3& cv,
+                                              float3& ax, unsigned long long pol) {
+    int k = 0;
+    if (U > 1) {
+        for (; k + U <= len; k += U) {
+            Entry m[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) m[u] = load_entry(a, (size_t)(base + k + u) * kSlice + lane, pol);
+            float3 vj[U], xj[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                vj[u] = xyz(a.v4[m[u].j]);
+                xj[u] = xyz(a.x[m[u].j]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                cv = cv + bmul(m[u].A, m[u].B, m[u].C, vj[u] - vi);
+                ax = ax + bmul(m[u].A, m[u].B, m[u].C, xj[u]);
+            }
+        }
+    }
+    for (; k < len; ++k) {
+        Entry m = load_entry(a, (size_t)(base + k) * kSlice + lane, pol);
+        float3 vj = xyz(a.v4[m.j]), xj = xyz(a.x[m.j]);
+        cv = cv + bmul(m.A, m.B, m.C, vj - vi);
+        ax = ax + bmul(m.A, m.B, m.C, xj);
+    }
+}
+
 struct Smem {
     float* part;      // [L * 3]
     SceneState* st;   // [S]
@@ -216,7 +326,10 @@ __device__ __forceinline__ float rhs_scale(float maximum) {
     return scale;
 }
 
+template <int U>
 __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
+    const unsigned long long pol_last = policy_evict_last();
+    const unsigned long long pol_first = policy_evict_first();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_ok;
     __shared__ int s_any;
@@ -246,33 +359,30 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
             int row = meta.x + lane;
             unsigned info = a.row_info[row];
             float3 rhs = f3(0.f, 0.f, 0.f), u = f3(0.f, 0.f, 0.f);
-            if (!(info & kFixedBit)) {
-                int len = (int)(info & ~kFixedBit);
-                float3 vi = xyz(a.v4[row]);
-                float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
-                int base = a.slice_ptr[sl];
-                for (int k = 0; k < len; ++k) {
-                    size_t e = (size_t)(base + k) * kSlice + lane;
-                    float4 A = a.valA[e], B = a.valB[e];
-                    float C = a.valC[e];
-                    int j = a.scol[e];
-                    float3 vj = xyz(a.v4[j]);
-                    float3 xj = xyz(a.x[j]);
-                    cv = cv + bmul(A, B, C, vj - vi);
-                    ax = ax + bmul(A, B, C, xj);
+            if (a.solve_rhs != nullptr) {
+                // solve mode: A x = b from x0 = 0, b given (projected at fixed rows)
+                if (!(info & kFixedBit)) rhs = load3(a.solve_rhs, row);
+                u = rhs;
+            } else {
+                if (!(info & kFixedBit)) {
+                    int len = (int)(info & ~kFixedBit);
+                    float3 vi = xyz(a.v4[row]);
+                    float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
+                    row_predictor<U>(a, a.slice_ptr[sl], len, lane, vi, cv, ax,
+                                     sl < a.resident_slices ? pol_last : pol_first);
+                    rhs = load3(a.f_ws, row) - cv;
+                    for (int e = a.spring_ptr[row]; e < a.spring_ptr[row + 1]; ++e) {
+                        int ent = a.spring_ent[e];
+                        int s = ent >> 1;
+                        int ia = a.spring_idx[2 * s], ib = a.spring_idx[2 * s + 1];
+                        if (ia < 0 || ib < 0) continue;
+                        float3 corr = (xyz(a.v4[ia]) - xyz(a.v4[ib])) * (h * a.spring_kd[s]);
+                        rhs = (ent & 1) ? rhs - corr : rhs + corr;
+                    }
+                    u = rhs - ax;
                 }
-                rhs = load3(a.f_ws, row) - cv;
-                for (int e = a.spring_ptr[row]; e < a.spring_ptr[row + 1]; ++e) {
-                    int ent = a.spring_ent[e];
-                    int s = ent >> 1;
-                    int ia = a.spring_idx[2 * s], ib = a.spring_idx[2 * s + 1];
-                    if (ia < 0 || ib < 0) continue;
-                    float3 corr = (xyz(a.v4[ia]) - xyz(a.v4[ib])) * (h * a.spring_kd[s]);
-                    rhs = (ent & 1) ? rhs - corr : rhs + corr;
-                }
-                u = rhs - ax;
+                store3(a.f_ws, row, rhs);
             }
-            store3(a.f_ws, row, rhs);
             a.r[row] = f4(u);
             mx = fmaxf(fabsf(rhs.x), fmaxf(fabsf(rhs.y), fabsf(rhs.z)));
         }
@@ -301,10 +411,14 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
             float sc = st.scale;
             float3 x = f3(0.f, 0.f, 0.f), r = f3(0.f, 0.f, 0.f);
             if (!st.zero) {
-                x = xyz(a.x[row]) * sc;
+                if (a.solve_rhs == nullptr) x = xyz(a.x[row]) * sc;  // solve mode starts from zero
                 r = xyz(a.r[row]) * sc;
             }
-            float3 b = load3(a.f_ws, row) * sc;
+            float3 b;
+            if (a.solve_rhs != nullptr)
+                b = (a.row_info[row] & kFixedBit) ? f3(0.f, 0.f, 0.f) : load3(a.solve_rhs, row) * sc;
+            else
+                b = load3(a.f_ws, row) * sc;
             float3 z = minv_mul(a.minv, row, r);
             a.x[row] = f4(x);
             a.r[row] = f4(r);
@@ -364,20 +478,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
                 if (!(info & kFixedBit)) {
                     int len = (int)(info & ~kFixedBit);
                     int base = a.slice_ptr[sl];
-                    acc = f3(0.f, 0.f, 0.f);
-                    if (firstit) {
-                        for (int k = 0; k < len; ++k) {
-                            size_t e = (size_t)(base + k) * kSlice + lane;
-                            int j = a.scol[e];
-                            acc = acc + bmul(a.valA[e], a.valB[e], a.valC[e], xyz(a.z[j]));
-                        }
-                    } else {
-                        for (int k = 0; k < len; ++k) {
-                            size_t e = (size_t)(base + k) * kSlice + lane;
-                            int j = a.scol[e];
-                            acc = acc + bmul(a.valA[e], a.valB[e], a.valC[e], next_p(a.z[j], pold[j], beta));
-                        }
-                    }
+                    unsigned long long pol = sl < a.resident_slices ? pol_last : pol_first;
+                    acc = firstit ? row_times_p<U, true>(a, base, len, lane, pold, beta, pol)
+                                  : row_times_p<U, false>(a, base, len, lane, pold, beta, pol);
                 }
                 pnew[row] = f4(pc);
                 a.y[row] = f4(acc);
@@ -489,6 +592,19 @@ size_t pcg_smem_bytes(int L, int S) {
     return off;
 }
 
+using PcgKernel = void (*)(PcgArgs);
+
+PcgKernel pcg_kernel_for(int unroll) {
+    switch (unroll) {
+        case 2: return pcg_kernel<2>;
+        case 4: return pcg_kernel<4>;
+        default: return pcg_kernel<1>;
+    }
+}
+
+// Grid size and slices per CTA for the handle's kernel variant: as many CTAs as
+// the variant can keep co-resident (the cooperative limit), but no more than
+// one per 8 slices.
 cudaError_t pcg_configure(Handle& h) {
     int dev = 0;
     cudaError_t err = cudaGetDevice(&dev);
@@ -497,6 +613,7 @@ cudaError_t pcg_configure(Handle& h) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return cudaErrorNotSupported;
+    PcgKernel kern = pcg_kernel_for(h.spmv_unroll);
     int warps_per_cta = kPcgThreads / 32;
     int needed = (h.nslices + warps_per_cta - 1) / warps_per_cta;
     if (needed < 1) needed = 1;
@@ -506,9 +623,9 @@ cudaError_t pcg_configure(Handle& h) {
         int L = (h.nslices + grid - 1) / grid;
         if (L < 1) L = 1;
         size_t smem = pcg_smem_bytes(L, h.nscenes);
-        if (smem > 48 * 1024) cudaFuncSetAttribute(pcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 0;
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_kernel, kPcgThreads, smem);
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPcgThreads, smem);
         if (err != cudaSuccess) return err;
         if (per_sm < 1) return cudaErrorInvalidConfiguration;
         int cap = per_sm * sms;
@@ -521,11 +638,12 @@ cudaError_t pcg_configure(Handle& h) {
     if (h.slices_per_cta < 1) h.slices_per_cta = 1;
     h.pcg_smem = pcg_smem_bytes(h.slices_per_cta, h.nscenes);
     if (h.pcg_smem > 48 * 1024)
-        cudaFuncSetAttribute(pcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h.pcg_smem);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h.pcg_smem);
     return cudaSuccess;
 }
 
-cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s) {
+cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s,
+                       const float* solve_rhs, float* x_out, float tol, int maxiter) {
     PcgArgs a;
     a.valA = h.valA;
     a.valB = h.valB;
@@ -553,7 +671,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.spring_idx = h.spring_idx;
     a.spring_kd = h.spring_kd;
     a.f_ws = f_ws;
-    a.dv = h.dv;
+    a.dv = x_out != nullptr ? x_out : h.dv;
     a.q_out = q_out;
     a.v_out = v_out;
     a.x = h.x;
@@ -566,11 +684,13 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.status = h.status;
     a.scene_stats = h.scene_stats;
     a.cum_iters = h.cum_iters;
-    a.maxiter = h.maxiter;
-    a.tol = h.tol;
+    a.maxiter = maxiter >= 0 ? maxiter : h.maxiter;
+    a.tol = tol > 0.0f ? tol : h.tol;
     a.dt = dt;
     a.limit_ns = h.wait_limit_ns;
     a.write_state = write_state;
+    a.resident_slices = h.resident_slices;
+    a.solve_rhs = solve_rhs;
     cudaError_t err = cudaMemsetAsync(h.barrier, 0, sizeof(unsigned), s);
     if (err != cudaSuccess) return err;
     cudaLaunchConfig_t cfg = {};
@@ -583,7 +703,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, pcg_kernel, a);
+    return cudaLaunchKernelEx(&cfg, pcg_kernel_for(h.spmv_unroll), a);
 }
 
 }  // namespace fem

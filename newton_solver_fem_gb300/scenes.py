@@ -265,12 +265,23 @@ def tet_jittered_48(n: int = 48, seed: int = 3) -> Scene:
 
 
 def tet_beam(seed: int = 4) -> Scene:
-    """16x4x4 cubes of 0.05 m x 6 tets (1,536 tets, 425 nodes), x=0 end fixed, mu scale U[0.8,1.2]."""
-    x, tets, mats, mass = tet_block(16, 4, 4, 0.05, (0, 0, 0), 1.0e5, 0.45, 1000.0)
+    """16x4x4 cubes of 0.05 m x 6 tets (1,536 tets, 425 nodes) hanging from its fixed top end, mu scale U[0.8,1.2].
+
+    The beam's long axis is z: the 25 nodes of the top face (z = 0.8 m) are
+    fixed and the tip face is z = 0, with gravity along the axis.  The
+    differentiable contract assembles A once at the rest pose, so the workload
+    must stay in small strain with 30 CG iterations converging from zero.  A
+    cantilever under gravity cannot do both at h = 1/240 (its tip sag times
+    h^2 E / (rho cell^2) is about 1 m whatever E is); the hanging beam stretches
+    by about rho g L^2 / 2E = 3 cm, oscillates 1-6 cm below rest, and CG
+    reaches a relative residual of 1e-6 in 30 iterations.  The target is 0.05 m
+    below the tip face's rest centroid.
+    """
+    x, tets, mats, mass = tet_block(4, 4, 16, 0.05, (0, 0, 0), 1.0e5, 0.45, 1000.0)
     rng = np.random.default_rng(seed)
     scale = rng.uniform(0.8, 1.2, size=len(tets)).astype(np.float32)
-    fixed = np.nonzero(np.isclose(x[:, 0], 0.0))[0].astype(np.int32)
-    tip = np.nonzero(np.isclose(x[:, 0], x[:, 0].max()))[0].astype(np.int32)
+    fixed = np.nonzero(np.isclose(x[:, 2], x[:, 2].max()))[0].astype(np.int32)
+    tip = np.nonzero(np.isclose(x[:, 2], 0.0))[0].astype(np.int32)
     target = x[tip].mean(axis=0) - np.array([0.0, 0.0, 0.05])
     return Scene("tet4_beam_16x4x4", x, mass, tets=tets, tet_materials=mats, fixed=fixed, substeps=4,
                  frames=120, maxiter=30, seed=seed,
