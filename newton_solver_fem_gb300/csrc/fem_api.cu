@@ -147,7 +147,7 @@ int configure_launch(Handle& h) {
     h.cta_seg_base = upload_plain(cta_seg_base, h.launch_allocations, err);
     h.cta_first_scene = upload_plain(cta_first_scene, h.launch_allocations, err);
     h.scene_seg0 = upload_plain(scene_seg0, h.launch_allocations, err);
-    std::vector<double> zeros(2 * 3 * (size_t)std::max(1, nseg), 0.0);
+    std::vector<float> zeros(2 * 3 * (size_t)std::max(1, nseg), 0.0f);
     h.seg_part = upload_plain(zeros, h.launch_allocations, err);
     if (err != cudaSuccess) return cuda_status(err, &h);
     // L2-resident prefix of the matrix stream (40 bytes per stored block)
@@ -489,10 +489,9 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     h.minv = b.alloc<float>(9 * (size_t)P);
     h.x = b.alloc<float4>(P);
     h.r = b.alloc<float4>(P);
-    h.z = b.alloc<float4>(P);
-    h.p0 = b.alloc<float4>(P);
-    h.p1 = b.alloc<float4>(P);
-    h.y = b.alloc<float4>(P);
+    h.zp0 = b.alloc<float4>(2 * (size_t)P);
+    h.zp1 = b.alloc<float4>(2 * (size_t)P);
+    h.stage = b.alloc<float4>(2 * (size_t)P);
     if (d->velocity_increment != nullptr) {
         h.dv = d->velocity_increment;
         h.dv_owned = false;

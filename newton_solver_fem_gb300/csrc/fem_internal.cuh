@@ -46,7 +46,7 @@ struct PcgArgs {
     const int* __restrict__ scene_slice0;     // [S+1]
     const int* __restrict__ scene_seg0;       // [S+1]
     int nscenes;
-    double* seg_part;  // [2][nseg * 3], alternating between consecutive reductions
+    float* seg_part;  // [2][nseg * 3], alternating between consecutive reductions
     int nseg;
     // node data
     const float4* __restrict__ v4;     // packed velocity (fixed zeroed)
@@ -60,13 +60,15 @@ struct PcgArgs {
     float* dv;         // [P*3] warm start in, velocity increment out
     float* q_out;      // [P*3]
     float* v_out;      // [P*3]
-    // CG vectors
+    // CG vectors.  z and the search direction p of a node share one 32-byte
+    // record (zp[2i] = z_i, zp[2i+1] = p_i) so that a gathered column costs one
+    // sector; two record buffers alternate between iterations.
     float4* x;
     float4* r;
-    float4* z;
-    float4* p0;
-    float4* p1;
-    float4* y;
+    float4* zp0;
+    float4* zp1;
+    float4* stage;   // [2P] (p_i, y_i) handed from phase A to phase B when not staged in shared memory
+    int stage_smem;  // 1: the staging lives in the CTA's shared memory
     // control
     unsigned* barrier;
     int* status;
@@ -153,7 +155,10 @@ struct Handle {
     unsigned* row_info = nullptr;
     float* minv = nullptr;  // [P*9]
     // CG
-    float4 *x = nullptr, *r = nullptr, *z = nullptr, *p0 = nullptr, *p1 = nullptr, *y = nullptr;
+    float4 *x = nullptr, *r = nullptr;
+    float4 *zp0 = nullptr, *zp1 = nullptr;  // [2P] each: (z_i, p_i) records
+    float4* stage = nullptr;                // [2P] (p_i, y_i) phase A -> phase B staging
+    int stage_smem = 0;
     float* dv = nullptr;
     bool dv_owned = true;
     // reductions / control
@@ -165,7 +170,7 @@ struct Handle {
     int* scene_slice0 = nullptr;
     int* scene_seg0 = nullptr;
     int nseg = 0;
-    double* seg_part = nullptr;
+    float* seg_part = nullptr;
     unsigned* barrier = nullptr;
     int* status = nullptr;
     SceneStats* scene_stats = nullptr;

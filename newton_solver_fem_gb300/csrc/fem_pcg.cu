@@ -18,6 +18,12 @@
 // Matrix layout: SELL-32 (slice of 32 consecutive rows of one scene, thread
 // per row), the 9 block values split into two float4 planes and one float
 // plane so that a warp streams 512 + 512 + 128 contiguous bytes per block column.
+// z and p of a node share one 32-byte record, so the gather of a column
+// (z_j and p_j for p = z + beta p) touches a single sector.  Iteration it reads
+// record buffer it & 1; phase A hands each row's p and y to phase B through a
+// staging area (shared memory when the CTA's slices fit, else a global
+// buffer), and phase B writes the whole next record (z, p) at once, so every
+// record write covers full sectors.
 #include <cooperative_groups.h>
 
 #include "fem_internal.cuh"
@@ -57,36 +63,28 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Bounded grid barrier over a monotone counter (zeroed before the launch).
-// Gives up after limit_ns nanoseconds, or as soon as another CTA has given up,
-// and reports false; the caller then leaves the kernel.
-__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned nblocks, unsigned& epoch, int* status,
-                                             long long limit_ns, int* s_ok) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        epoch += 1;
-        unsigned target = epoch * nblocks;
-        __threadfence();
-        atomicAdd(counter, 1u);
-        int ok = 1;
-        unsigned long long t0 = global_ns();
-        unsigned spins = 0;
-        while (ld_acquire(counter) < target) {
-            if ((++spins & 63u) == 1u) {  // first spin, then every 64th
-                if ((ld_relaxed_int(status) & kStatusTimeout) != 0 ||
-                    (long long)(global_ns() - t0) >= limit_ns) {
-                    ok = 0;
-                    atomicOr(status, kStatusTimeout);
-                    break;
-                }
+// Grid barrier over a monotone counter (zeroed before the launch), entered by
+// one thread per CTA after a CTA or warp barrier has ordered the CTA's writes
+// before it.  The arrival is a release reduction, so those writes are visible
+// at GPU scope before it; the wait is an acquire load, so the other CTAs'
+// writes are visible after it.  The wait is bounded: it gives up after
+// limit_ns nanoseconds, or as soon as another CTA has given up, and returns 0.
+__device__ __forceinline__ int arrive_and_wait(unsigned* counter, unsigned nblocks, unsigned& epoch, int* status,
+                                               long long limit_ns) {
+    epoch += 1;
+    const unsigned target = epoch * nblocks;
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
+    const unsigned long long t0 = global_ns();
+    unsigned spins = 0;
+    while ((int)(ld_acquire(counter) - target) < 0) {  // wrap-safe: the counter only grows
+        if ((++spins & 63u) == 1u) {  // first spin, then every 64th
+            if ((ld_relaxed_int(status) & kStatusTimeout) != 0 || (long long)(global_ns() - t0) >= limit_ns) {
+                atomicOr(status, kStatusTimeout);
+                return 0;
             }
-            __nanosleep(20);
         }
-        __threadfence();
-        *s_ok = ok;
     }
-    __syncthreads();
-    return *s_ok != 0;
+    return 1;
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -99,17 +97,6 @@ __device__ __forceinline__ float warp_max(float v) {
     for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
     return v;
 }
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
-__device__ __forceinline__ double warp_max_d(double v) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
-    return v;
-}
-
 __device__ __forceinline__ float3 bmul(float4 a, float4 b, float c, float3 p) {
     return f3(a.x * p.x + a.y * p.y + a.z * p.z, a.w * p.x + b.x * p.y + b.y * p.z, b.z * p.x + b.w * p.y + c * p.z);
 }
@@ -184,11 +171,19 @@ __device__ __forceinline__ Entry load_entry(const PcgArgs& a, size_t e, unsigned
     return m;
 }
 
+// p_j = z_j (first iteration) or z_j + beta p_j from record buffer rec.
+template <bool FIRST>
+__device__ __forceinline__ float3 gather_p(const float4* rec, int j, float beta) {
+    const float4* q = rec + 2 * (size_t)j;
+    if (FIRST) return xyz(q[0]);
+    return next_p(q[0], q[1], beta);
+}
+
 // y_row = sum_k A_k p_{j_k}, with p = z (first iteration) or z + beta p_old.
 // U block columns are loaded before any is used, so U entries (and then U
 // gathers) are in flight per thread; the sum keeps the k order of U = 1.
 template <int U, bool FIRST>
-__device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int len, int lane, const float4* pold,
+__device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int len, int lane, const float4* rec,
                                               float beta, unsigned long long pol) {
     float3 acc = f3(0.f, 0.f, 0.f);
     int k = 0;
@@ -199,14 +194,14 @@ __device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int le
             for (int u = 0; u < U; ++u) m[u] = load_entry(a, (size_t)(base + k + u) * kSlice + lane, pol);
             float3 p[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) p[u] = FIRST ? xyz(a.z[m[u].j]) : next_p(a.z[m[u].j], pold[m[u].j], beta);
+            for (int u = 0; u < U; ++u) p[u] = gather_p<FIRST>(rec, m[u].j, beta);
 #pragma unroll
             for (int u = 0; u < U; ++u) acc = acc + bmul(m[u].A, m[u].B, m[u].C, p[u]);
         }
     }
     for (; k < len; ++k) {
         Entry m = load_entry(a, (size_t)(base + k) * kSlice + lane, pol);
-        float3 p = FIRST ? xyz(a.z[m.j]) : next_p(a.z[m.j], pold[m.j], beta);
+        float3 p = gather_p<FIRST>(rec, m.j, beta);
         acc = acc + bmul(m.A, m.B, m.C, p);
     }
     return acc;
@@ -244,79 +239,112 @@ __device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int le
 }
 
 struct Smem {
-    float* part;      // [L * 3]
+    float* part;      // [L * 3] slice partials
     SceneState* st;   // [S]
-    double* tot;      // [S * 3]
-    double* red;      // [32 * 3] block-reduce scratch
+    float* tot;       // [S * 3] per-scene totals of the last reduction
+    float4* stage;    // [L * 32 * 2] (p, y) per row, when staged in shared memory
 };
 
-// Per-CTA segment partials: sum (or max) of the slice partials of each scene
-// this CTA covers, in slice order, written to buf.  Consecutive reductions
-// alternate between two buffers: a CTA that races ahead can only write a
-// buffer again after the next grid barrier, which every CTA reaches only once
-// it has finished reading that buffer's previous contents.
-__device__ void write_segments(const PcgArgs& a, const Smem& sm, double* buf, int nv, bool is_max, int first,
-                               int last) {
-    __syncthreads();
-    if (first >= last) return;
-    int s0 = a.cta_first_scene[blockIdx.x];
-    int nsc = a.slice_scene[last - 1] - s0 + 1;
-    for (int t = threadIdx.x; t < nsc; t += blockDim.x) {
-        int s = s0 + t;
-        int lo = max(a.scene_slice0[s], first), hi = min(a.scene_slice0[s + 1], last);
-        for (int k = 0; k < nv; ++k) {
-            double acc = 0.0;
-            for (int sl = lo; sl < hi; ++sl) {
-                double v = (double)sm.part[(sl - first) * 3 + k];
-                acc = is_max ? fmax(acc, v) : acc + v;
-            }
-            buf[(size_t)(a.cta_seg_base[blockIdx.x] + t) * 3 + k] = acc;
-        }
-    }
+// Scenes up to this count are reduced lane-parallel over their segments by one
+// warp; more scenes are reduced one scene per thread by the whole CTA.
+constexpr int kWarpReducedScenes = 4;
+
+// Largest slices per CTA whose (p, y) staging goes to shared memory (1 KB per slice).
+constexpr int kStageSmemMaxSlices = 32;
+
+// Byte offsets of the dynamic shared memory sections; every section starts on
+// a 16-byte boundary (the staging area holds float4).  One definition serves
+// the kernel and the host-side size.
+struct SmemLayout {
+    size_t part, st, tot, stage, total;
+};
+__host__ __device__ __forceinline__ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
+__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S) {
+    SmemLayout m;
+    m.part = 0;
+    m.st = m.part + align16((size_t)L * 3 * sizeof(float));
+    m.tot = m.st + align16((size_t)S * sizeof(SceneState));
+    m.stage = m.tot + align16((size_t)S * 3 * sizeof(float));
+    m.total = m.stage + (L <= kStageSmemMaxSlices ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
+    return m;
 }
 
-// After a grid barrier: every CTA forms the per-scene totals from the segment
-// partials in the same fixed order.
-__device__ void scene_totals(const PcgArgs& a, const Smem& sm, const double* buf, int nv, bool is_max) {
-    int S = a.nscenes;
-    if (S <= 4) {
-        int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int s = 0; s < S; ++s) {
-            int lo = a.scene_seg0[s], hi = a.scene_seg0[s + 1];
-            double acc[3] = {0.0, 0.0, 0.0};
-            for (int g = lo + threadIdx.x; g < hi; g += blockDim.x)
+// Where row `row` (lane `lane` of slice `sl`) stages its p and y between the phases.
+__device__ __forceinline__ float4* stage_slot(const PcgArgs& a, const Smem& sm, int sl, int first, int lane, int row) {
+    return a.stage_smem ? sm.stage + 2 * ((sl - first) * kSlice + lane) : a.stage + 2 * (size_t)row;
+}
+
+// One grid-wide reduction step, entered by every thread of the CTA once the
+// slice partials of the current phase are in sm.part:
+//   1. warp 0 writes this CTA's per-scene segment partials (sum or max of its
+//      slices of the scene, in slice order) to buf;
+//   2. one thread arrives at the grid barrier and waits for every CTA;
+//   3. the per-scene totals over all segments, in a fixed order, go to sm.tot.
+// Every CTA forms bit-identical totals.  Consecutive reductions alternate
+// between two buffers: a CTA that races ahead can only write a buffer again
+// after the next barrier, which every CTA reaches only once it has finished
+// reading that buffer's previous contents.  Partials and totals are float,
+// like the reference solver's float32 dot products; the order is fixed, so
+// results are deterministic.  Returns false after a timed-out wait.
+__device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf, int nv, bool is_max, int first,
+                                   int last, unsigned& epoch, int* s_ok) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int S = a.nscenes;
+    __syncthreads();  // slice partials complete
+    if (warp == 0) {
+        if (first < last) {
+            const int s0 = a.cta_first_scene[blockIdx.x];
+            const int nsc = a.slice_scene[last - 1] - s0 + 1;
+            for (int t = lane; t < nsc; t += 32) {
+                const int sc = s0 + t;
+                const int lo = max(a.scene_slice0[sc], first), hi = min(a.scene_slice0[sc + 1], last);
                 for (int k = 0; k < nv; ++k) {
-                    double v = buf[(size_t)g * 3 + k];
-                    acc[k] = is_max ? fmax(acc[k], v) : acc[k] + v;
-                }
-            for (int k = 0; k < nv; ++k) {
-                double v = is_max ? warp_max_d(acc[k]) : warp_sum_d(acc[k]);
-                if (lane == 0) sm.red[warp * 3 + k] = v;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int k = 0; k < nv; ++k) {
-                    double t = 0.0;
-                    for (int w = 0; w < nw; ++w) t = is_max ? fmax(t, sm.red[w * 3 + k]) : t + sm.red[w * 3 + k];
-                    sm.tot[s * 3 + k] = t;
+                    float acc = 0.f;
+                    for (int sl = lo; sl < hi; ++sl) {
+                        float v = sm.part[(sl - first) * 3 + k];
+                        acc = is_max ? fmaxf(acc, v) : acc + v;
+                    }
+                    buf[(size_t)(a.cta_seg_base[blockIdx.x] + t) * 3 + k] = acc;
                 }
             }
-            __syncthreads();
         }
-    } else {
-        for (int s = threadIdx.x; s < S; s += blockDim.x) {
-            int lo = a.scene_seg0[s], hi = a.scene_seg0[s + 1];
-            for (int k = 0; k < nv; ++k) {
-                double t = 0.0;
-                for (int g = lo; g < hi; ++g) {
-                    double v = buf[(size_t)g * 3 + k];
-                    t = is_max ? fmax(t, v) : t + v;
+        __syncwarp();
+        int ok = 1;
+        if (lane == 0) ok = arrive_and_wait(a.barrier, gridDim.x, epoch, a.status, a.limit_ns);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (ok && S <= kWarpReducedScenes) {
+            for (int sc = 0; sc < S; ++sc) {
+                const int lo = a.scene_seg0[sc], hi = a.scene_seg0[sc + 1];
+                for (int k = 0; k < nv; ++k) {
+                    float acc = 0.f;
+                    for (int g = lo + lane; g < hi; g += 32) {
+                        float v = __ldcg(buf + (size_t)g * 3 + k);
+                        acc = is_max ? fmaxf(acc, v) : acc + v;
+                    }
+                    acc = is_max ? warp_max(acc) : warp_sum(acc);
+                    if (lane == 0) sm.tot[sc * 3 + k] = acc;
                 }
-                sm.tot[s * 3 + k] = t;
+            }
+        }
+        if (lane == 0) *s_ok = ok;
+    }
+    __syncthreads();
+    if (!*s_ok) return false;
+    if (S > kWarpReducedScenes) {
+        for (int sc = threadIdx.x; sc < S; sc += blockDim.x) {
+            const int lo = a.scene_seg0[sc], hi = a.scene_seg0[sc + 1];
+            for (int k = 0; k < nv; ++k) {
+                float acc = 0.f;
+                for (int g = lo; g < hi; ++g) {
+                    float v = __ldcg(buf + (size_t)g * 3 + k);
+                    acc = is_max ? fmaxf(acc, v) : acc + v;
+                }
+                sm.tot[sc * 3 + k] = acc;
             }
         }
         __syncthreads();
     }
+    return true;
 }
 
 __device__ __forceinline__ float rhs_scale(float maximum) {
@@ -336,18 +364,15 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
     const int S = a.nscenes;
     const int L = a.slices_per_cta;
     Smem sm;
-    sm.part = reinterpret_cast<float*>(smem_raw);
-    size_t off = ((size_t)L * 3 * sizeof(float) + 15) & ~(size_t)15;
-    sm.st = reinterpret_cast<SceneState*>(smem_raw + off);
-    off += ((size_t)S * sizeof(SceneState) + 15) & ~(size_t)15;
-    sm.tot = reinterpret_cast<double*>(smem_raw + off);
-    off += (size_t)S * 3 * sizeof(double);
-    sm.red = reinterpret_cast<double*>(smem_raw + off);
+    const SmemLayout lay = smem_layout(L, S);
+    sm.part = reinterpret_cast<float*>(smem_raw + lay.part);
+    sm.st = reinterpret_cast<SceneState*>(smem_raw + lay.st);
+    sm.tot = reinterpret_cast<float*>(smem_raw + lay.tot);
+    sm.stage = reinterpret_cast<float4*>(smem_raw + lay.stage);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int first = blockIdx.x * L;
     const int last = min(first + L, a.nslices);
-    const unsigned nblocks = gridDim.x;
     unsigned epoch = 0;
     const float h = a.dt;
 
@@ -389,11 +414,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
         mx = warp_max(mx);
         if (lane == 0) sm.part[(sl - first) * 3] = mx;
     }
-    double* const buf0 = a.seg_part;
-    double* const buf1 = a.seg_part + (size_t)a.nseg * 3;
-    write_segments(a, sm, buf0, 1, true, first, last);
-    if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
-    scene_totals(a, sm, buf0, 1, true);
+    float* const buf0 = a.seg_part;
+    float* const buf1 = a.seg_part + (size_t)a.nseg * 3;
+    if (!reduce_across_grid(a, sm, buf0, 1, true, first, last, epoch, &s_ok)) return;
     for (int s = threadIdx.x; s < S; s += blockDim.x) {
         float mxs = (float)sm.tot[s * 3];
         sm.st[s].scale = rhs_scale(mxs);
@@ -422,7 +445,8 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
             float3 z = minv_mul(a.minv, row, r);
             a.x[row] = f4(x);
             a.r[row] = f4(r);
-            a.z[row] = f4(z);
+            a.zp0[2 * (size_t)row] = f4(z);
+            a.zp0[2 * (size_t)row + 1] = f4(f3(0.f, 0.f, 0.f));  // full record; p unused in the first iteration
             rr = dot3(r, r);
             rz = dot3(r, z);
             bb = dot3(b, b);
@@ -435,9 +459,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
             p[0] = rr; p[1] = rz; p[2] = bb;
         }
     }
-    write_segments(a, sm, buf1, 3, false, first, last);
-    if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
-    scene_totals(a, sm, buf1, 3, false);
+    if (!reduce_across_grid(a, sm, buf1, 3, false, first, last, epoch, &s_ok)) return;
     if (threadIdx.x == 0) s_any = 0;
     __syncthreads();
     for (int s = threadIdx.x; s < S; s += blockDim.x) {
@@ -460,8 +482,8 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
 
     // ---------------- CG iterations
     for (int it = 0; s_any; ++it) {
-        const float4* pold = (it & 1) ? a.p1 : a.p0;
-        float4* pnew = (it & 1) ? a.p0 : a.p1;
+        const float4* rec = (it & 1) ? a.zp1 : a.zp0;  // z and p of this iteration
+        float4* rec_next = (it & 1) ? a.zp0 : a.zp1;   // (z, p) for the next, written by phase B
         // phase A: p = z + beta p, y = (PAP + I - P) p, partial p.y
         for (int sl = first + warp; sl < last; sl += W) {
             int2 meta = a.slice_meta[sl];
@@ -472,26 +494,25 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
                 unsigned info = a.row_info[row];
                 const bool firstit = st.iters == 0;
                 const float beta = st.beta;
-                float4 zi = a.z[row];
-                float3 pc = firstit ? xyz(zi) : next_p(zi, pold[row], beta);
+                float4 zi = rec[2 * (size_t)row];
+                float3 pc = firstit ? xyz(zi) : next_p(zi, rec[2 * (size_t)row + 1], beta);
                 float3 acc = pc;  // fixed rows: identity (their p is zero)
                 if (!(info & kFixedBit)) {
                     int len = (int)(info & ~kFixedBit);
                     int base = a.slice_ptr[sl];
                     unsigned long long pol = sl < a.resident_slices ? pol_last : pol_first;
-                    acc = firstit ? row_times_p<U, true>(a, base, len, lane, pold, beta, pol)
-                                  : row_times_p<U, false>(a, base, len, lane, pold, beta, pol);
+                    acc = firstit ? row_times_p<U, true>(a, base, len, lane, rec, beta, pol)
+                                  : row_times_p<U, false>(a, base, len, lane, rec, beta, pol);
                 }
-                pnew[row] = f4(pc);
-                a.y[row] = f4(acc);
+                float4* stg = stage_slot(a, sm, sl, first, lane, row);
+                stg[0] = f4(pc);
+                stg[1] = f4(acc);
                 pap = dot3(pc, acc);
             }
             pap = warp_sum(pap);
             if (lane == 0) sm.part[(sl - first) * 3] = pap;
         }
-        write_segments(a, sm, buf0, 1, false, first, last);
-        if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
-        scene_totals(a, sm, buf0, 1, false);
+        if (!reduce_across_grid(a, sm, buf0, 1, false, first, last, epoch, &s_ok)) return;
         for (int s = threadIdx.x; s < S; s += blockDim.x) {
             SceneState& st = sm.st[s];
             if (st.active) st.alpha = (float)(st.rz / sm.tot[s * 3]);
@@ -505,14 +526,16 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
             if (st.active && lane < meta.y) {
                 int row = meta.x + lane;
                 float alpha = st.alpha;
-                float3 p = xyz(pnew[row]), yv = xyz(a.y[row]);
+                const float4* stg = stage_slot(a, sm, sl, first, lane, row);
+                float3 p = xyz(stg[0]), yv = xyz(stg[1]);
                 float3 x = xyz(a.x[row]), r = xyz(a.r[row]);
                 x = x + p * alpha;
                 r = r - yv * alpha;
                 float3 z = minv_mul(a.minv, row, r);
                 a.x[row] = f4(x);
                 a.r[row] = f4(r);
-                a.z[row] = f4(z);
+                rec_next[2 * (size_t)row] = f4(z);
+                rec_next[2 * (size_t)row + 1] = f4(p);
                 rr = dot3(r, r);
                 rz = dot3(r, z);
             }
@@ -523,9 +546,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
                 p[0] = rr; p[1] = rz;
             }
         }
-        write_segments(a, sm, buf1, 2, false, first, last);
-        if (!grid_barrier(a.barrier, nblocks, epoch, a.status, a.limit_ns, &s_ok)) return;
-        scene_totals(a, sm, buf1, 2, false);
+        if (!reduce_across_grid(a, sm, buf1, 2, false, first, last, epoch, &s_ok)) return;
         if (threadIdx.x == 0) s_any = 0;
         __syncthreads();
         for (int s = threadIdx.x; s < S; s += blockDim.x) {
@@ -585,11 +606,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
 }  // namespace
 
 size_t pcg_smem_bytes(int L, int S) {
-    size_t off = ((size_t)L * 3 * sizeof(float) + 15) & ~(size_t)15;
-    off += ((size_t)S * sizeof(SceneState) + 15) & ~(size_t)15;
-    off += (size_t)S * 3 * sizeof(double);
-    off += 32 * 3 * sizeof(double);
-    return off;
+    return smem_layout(L, S).total;
 }
 
 using PcgKernel = void (*)(PcgArgs);
@@ -636,7 +653,10 @@ cudaError_t pcg_configure(Handle& h) {
     h.grid = grid;
     h.slices_per_cta = (h.nslices + grid - 1) / grid;
     if (h.slices_per_cta < 1) h.slices_per_cta = 1;
-    h.pcg_smem = pcg_smem_bytes(h.slices_per_cta, h.nscenes);
+    const SmemLayout lay = smem_layout(h.slices_per_cta, h.nscenes);
+    if ((lay.st | lay.tot | lay.stage) & 15) return cudaErrorMisalignedAddress;  // float4/double sections
+    h.pcg_smem = lay.total;
+    h.stage_smem = h.slices_per_cta <= kStageSmemMaxSlices;
     if (h.pcg_smem > 48 * 1024)
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h.pcg_smem);
     return cudaSuccess;
@@ -676,10 +696,10 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.v_out = v_out;
     a.x = h.x;
     a.r = h.r;
-    a.z = h.z;
-    a.p0 = h.p0;
-    a.p1 = h.p1;
-    a.y = h.y;
+    a.zp0 = h.zp0;
+    a.zp1 = h.zp1;
+    a.stage = h.stage;
+    a.stage_smem = h.stage_smem;
     a.barrier = h.barrier;
     a.status = h.status;
     a.scene_stats = h.scene_stats;
