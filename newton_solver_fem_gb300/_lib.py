@@ -26,6 +26,8 @@ FEM_TUNE_SPMV_UNROLL = 1
 FEM_TUNE_L2_RESIDENT_BYTES = 2
 FEM_TUNE_RESIDENT_SLICES = 3
 FEM_TUNE_GRID = 4
+FEM_TUNE_CTA_THREADS = 5
+FEM_TUNE_GRID_CAP = 6
 
 FEM_TERM_SPRING = 1
 FEM_TERM_TET = 2

@@ -11,7 +11,7 @@
 namespace fem {
 
 constexpr int kSlice = 32;          // rows per SELL slice (one warp, thread per row)
-constexpr int kPcgThreads = 256;    // persistent PCG block size (8 warps)
+constexpr int kPcgMaxThreads = 1024;  // largest persistent PCG block (the launch bound)
 constexpr unsigned kFixedBit = 0x80000000u;  // row_info: fixed-node flag; low bits = row length
 
 // Device-side status bits (FemStats.status).
@@ -99,6 +99,8 @@ struct Handle {
     long long wait_limit_ns = 2000000000LL;
     int spmv_unroll = 4;          // block columns in flight per thread in the PCG SpMV (1, 2 or 4)
     int64_t l2_resident_bytes = 0;   // matrix bytes loaded evict_last (-1: 60% of L2); measured slower, so off
+    int pcg_threads = 1024;          // threads per PCG CTA (256, 512 or 1024): one CTA per SM by default
+    int grid_cap = 0;                // upper bound on the PCG grid (0: co-residency limit only)
     int resident_slices = 0;
     bool tangent_prepared = false;
     // node data

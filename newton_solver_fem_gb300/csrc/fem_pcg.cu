@@ -249,8 +249,12 @@ struct Smem {
 // warp; more scenes are reduced one scene per thread by the whole CTA.
 constexpr int kWarpReducedScenes = 4;
 
-// Largest slices per CTA whose (p, y) staging goes to shared memory (1 KB per slice).
-constexpr int kStageSmemMaxSlices = 32;
+// The (p, y) staging of a CTA goes to shared memory when it needs at most
+// this many bytes per warp of the CTA (1 KB per slice).
+constexpr int kStageBytesPerWarp = 6 * 1024;
+__host__ __device__ __forceinline__ bool stage_in_smem(int L, int threads) {
+    return (size_t)L * kSlice * 2 * sizeof(float4) <= (size_t)kStageBytesPerWarp * (threads / 32);
+}
 
 // Byte offsets of the dynamic shared memory sections; every section starts on
 // a 16-byte boundary (the staging area holds float4).  One definition serves
@@ -259,13 +263,13 @@ struct SmemLayout {
     size_t part, st, tot, stage, total;
 };
 __host__ __device__ __forceinline__ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
-__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S) {
+__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage) {
     SmemLayout m;
     m.part = 0;
     m.st = m.part + align16((size_t)L * 3 * sizeof(float));
     m.tot = m.st + align16((size_t)S * sizeof(SceneState));
     m.stage = m.tot + align16((size_t)S * 3 * sizeof(float));
-    m.total = m.stage + (L <= kStageSmemMaxSlices ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
+    m.total = m.stage + (stage ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
     return m;
 }
 
@@ -355,7 +359,7 @@ __device__ __forceinline__ float rhs_scale(float maximum) {
 }
 
 template <int U>
-__global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
+__global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const unsigned long long pol_last = policy_evict_last();
     const unsigned long long pol_first = policy_evict_first();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -364,7 +368,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
     const int S = a.nscenes;
     const int L = a.slices_per_cta;
     Smem sm;
-    const SmemLayout lay = smem_layout(L, S);
+    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0);
     sm.part = reinterpret_cast<float*>(smem_raw + lay.part);
     sm.st = reinterpret_cast<SceneState*>(smem_raw + lay.st);
     sm.tot = reinterpret_cast<float*>(smem_raw + lay.tot);
@@ -605,10 +609,6 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs a) {
 
 }  // namespace
 
-size_t pcg_smem_bytes(int L, int S) {
-    return smem_layout(L, S).total;
-}
-
 using PcgKernel = void (*)(PcgArgs);
 
 PcgKernel pcg_kernel_for(int unroll) {
@@ -619,9 +619,12 @@ PcgKernel pcg_kernel_for(int unroll) {
     }
 }
 
-// Grid size and slices per CTA for the handle's kernel variant: as many CTAs as
-// the variant can keep co-resident (the cooperative limit), but no more than
-// one per 8 slices.
+// Grid size, slices per CTA and staging place for the handle's kernel variant
+// and CTA size: as many CTAs as stay co-resident (the cooperative limit, and
+// the optional cap), but no more than one per warp-count of slices.  The grid
+// only shrinks from pass to pass (a smaller grid means more slices per CTA and
+// possibly more shared memory), and the loop ends with a configuration whose
+// occupancy covers the grid.
 cudaError_t pcg_configure(Handle& h) {
     int dev = 0;
     cudaError_t err = cudaGetDevice(&dev);
@@ -631,35 +634,40 @@ cudaError_t pcg_configure(Handle& h) {
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return cudaErrorNotSupported;
     PcgKernel kern = pcg_kernel_for(h.spmv_unroll);
-    int warps_per_cta = kPcgThreads / 32;
-    int needed = (h.nslices + warps_per_cta - 1) / warps_per_cta;
-    if (needed < 1) needed = 1;
-    // grid depends on shared memory, which depends on slices per CTA: iterate
-    int grid = needed;
-    for (int pass = 0; pass < 4; ++pass) {
-        int L = (h.nslices + grid - 1) / grid;
-        if (L < 1) L = 1;
-        size_t smem = pcg_smem_bytes(L, h.nscenes);
-        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int threads = h.pcg_threads;
+    const int warps_per_cta = threads / 32;
+    int grid = (h.nslices + warps_per_cta - 1) / warps_per_cta;
+    if (grid < 1) grid = 1;
+    if (h.grid_cap > 0 && grid > h.grid_cap) grid = h.grid_cap;
+    for (int pass = 0;; ++pass) {
+        const int L = (h.nslices + grid - 1) / grid > 0 ? (h.nslices + grid - 1) / grid : 1;
+        bool stage = stage_in_smem(L, threads) && pass < 16;  // give up shared staging if it never settles
         int per_sm = 0;
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPcgThreads, smem);
-        if (err != cudaSuccess) return err;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            const SmemLayout lay = smem_layout(L, h.nscenes, stage);
+            if ((lay.st | lay.tot | lay.stage) & 15) return cudaErrorMisalignedAddress;  // float4 sections
+            if (lay.total > 48 * 1024) {
+                err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
+                if (err != cudaSuccess) return err;
+            }
+            err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, lay.total);
+            if (err != cudaSuccess) return err;
+            if (per_sm >= 1 || !stage) {
+                h.pcg_smem = lay.total;
+                break;
+            }
+            stage = false;  // staging does not fit at all: use the global buffer
+        }
         if (per_sm < 1) return cudaErrorInvalidConfiguration;
-        int cap = per_sm * sms;
-        int g = needed < cap ? needed : cap;
-        if (g == grid && pass > 0) break;
-        grid = g;
+        const int cap = per_sm * sms;
+        if (grid <= cap) {
+            h.grid = grid;
+            h.slices_per_cta = L;
+            h.stage_smem = stage ? 1 : 0;
+            return cudaSuccess;
+        }
+        grid = cap;
     }
-    h.grid = grid;
-    h.slices_per_cta = (h.nslices + grid - 1) / grid;
-    if (h.slices_per_cta < 1) h.slices_per_cta = 1;
-    const SmemLayout lay = smem_layout(h.slices_per_cta, h.nscenes);
-    if ((lay.st | lay.tot | lay.stage) & 15) return cudaErrorMisalignedAddress;  // float4/double sections
-    h.pcg_smem = lay.total;
-    h.stage_smem = h.slices_per_cta <= kStageSmemMaxSlices;
-    if (h.pcg_smem > 48 * 1024)
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h.pcg_smem);
-    return cudaSuccess;
 }
 
 cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s,
@@ -715,7 +723,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     if (err != cudaSuccess) return err;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(h.grid);
-    cfg.blockDim = dim3(kPcgThreads);
+    cfg.blockDim = dim3(h.pcg_threads);
     cfg.dynamicSmemBytes = h.pcg_smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
