@@ -1,7 +1,10 @@
 """Autotuner for the persistent PCG kernel's launch variant.
 
 Tunables (``fem_set_tuning``): the SpMV unroll (block columns in flight per
-thread: 1, 2, 4) and the matrix bytes loaded with the L2 evict_last policy.
+thread: 1, 2, 4), the threads per persistent CTA (256, 512, 1024: the grid is
+as many CTAs as stay co-resident) and the matrix bytes loaded with the L2
+evict_last policy.  L2 residency lost on every matrix larger than L2, so the
+default candidates leave it at 0.
 For a solver and a frame function the tuner restores the same initial state
 for every candidate, runs one warm-up frame, then times the PCG launches of
 ``frames`` eager frames with per-launch CUDA events.  It scores each candidate
@@ -26,7 +29,8 @@ import torch
 
 from . import _lib
 
-DEFAULT_CANDIDATES = [(u, r) for u in (1, 2, 4) for r in (0, 40 << 20, 77 << 20, 100 << 20)]
+# (unroll, CTA threads, L2-resident bytes)
+DEFAULT_CANDIDATES = [(u, t, 0) for t in (1024, 512, 256) for u in (4, 2)] + [(1, 1024, 0)]
 CACHE = Path(os.environ.get("FEM_GB300_TUNE_CACHE", Path.home() / ".cache" / "fem_gb300_tune.json"))
 
 
@@ -36,16 +40,18 @@ def _key(solver) -> str:
     return f"{name}|P={solver.model.particle_count}|blocks={info['stored_blocks']}|S={solver.model.scene_count}"
 
 
-def apply(solver, unroll: int, resident_bytes: int) -> None:
+def apply(solver, unroll: int, threads: int, resident_bytes: int) -> None:
     lib = _lib.load()
     _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_SPMV_UNROLL, int(unroll)))
+    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_CTA_THREADS, int(threads)))
     _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_L2_RESIDENT_BYTES, int(resident_bytes)))
 
 
 def current(solver) -> dict:
     lib = _lib.load()
     out = {}
-    for name, key in (("unroll", _lib.FEM_TUNE_SPMV_UNROLL), ("resident_bytes", _lib.FEM_TUNE_L2_RESIDENT_BYTES),
+    for name, key in (("unroll", _lib.FEM_TUNE_SPMV_UNROLL), ("threads", _lib.FEM_TUNE_CTA_THREADS),
+                      ("resident_bytes", _lib.FEM_TUNE_L2_RESIDENT_BYTES),
                       ("resident_slices", _lib.FEM_TUNE_RESIDENT_SLICES), ("grid", _lib.FEM_TUNE_GRID)):
         v = ctypes.c_int64()
         _lib.check(lib.fem_get_tuning(solver._handle, key, ctypes.byref(v)))
@@ -75,7 +81,7 @@ def measure(solver, frame, restore, frames: int = 3) -> dict:
 
 def autotune(solver, frame, restore, candidates=None, frames: int = 3, use_cache: bool = True,
              verbose: bool = False) -> dict:
-    """Pick and apply the fastest (unroll, resident bytes) for this solver; returns the record."""
+    """Pick and apply the fastest (unroll, CTA threads, resident bytes) for this solver; returns the record."""
     key = _key(solver)
     cache = {}
     if use_cache and CACHE.exists():
@@ -85,18 +91,17 @@ def autotune(solver, frame, restore, candidates=None, frames: int = 3, use_cache
             cache = {}
     if use_cache and key in cache:
         best = cache[key]
-        apply(solver, best["unroll"], best["resident_bytes"])
+        apply(solver, best["unroll"], best.get("threads", 1024), best["resident_bytes"])
         return best
     records = []
-    for unroll, resident in candidates or DEFAULT_CANDIDATES:
-        apply(solver, unroll, resident)
-        rec = {"unroll": unroll, "resident_bytes": resident, **current(solver), **measure(solver, frame, restore,
-                                                                                         frames)}
+    for unroll, threads, resident in candidates or DEFAULT_CANDIDATES:
+        apply(solver, unroll, threads, resident)
+        rec = {**current(solver), **measure(solver, frame, restore, frames)}
         records.append(rec)
         if verbose:
             print(json.dumps(rec), flush=True)
     best = min(records, key=lambda r: r["us_per_iteration"])
-    apply(solver, best["unroll"], best["resident_bytes"])
+    apply(solver, best["unroll"], best["threads"], best["resident_bytes"])
     if use_cache:
         cache[key] = best
         try:
