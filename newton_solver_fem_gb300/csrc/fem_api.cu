@@ -466,13 +466,36 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     h.elem_force = b.alloc<float4>(4 * (size_t)T + 8 * (size_t)Hn);
     h.q4 = b.alloc<float4>(P);
     h.v4 = b.alloc<float4>(P);
-    h.trip_vals = b.alloc<float>(9 * (size_t)ntrip);
+    h.trip.a = b.alloc<float4>((size_t)ntrip);
+    h.trip.b = b.alloc<float4>((size_t)ntrip);
+    h.trip.c = b.alloc<float>((size_t)ntrip);
     h.trip_rows = b.upload(trip_rows);
     h.trip_cols = b.upload(trip_cols);
+    // contributor lists keyed by SELL entry (empty for padding), so the
+    // assembly reads entry -> range -> triplet ids with no slot indirection
+    {
+        std::vector<int> sell_cptr(nsell + 1, 0);
+        parallel_for(nsell, [&](int64_t lo, int64_t hi) {
+            for (int64_t e = lo; e < hi; ++e) {
+                int slot = sell_slot[e];
+                sell_cptr[e + 1] = slot < 0 ? 0 : slot_cptr[slot + 1] - slot_cptr[slot];
+            }
+        });
+        for (int64_t e = 0; e < nsell; ++e) sell_cptr[e + 1] += sell_cptr[e];
+        std::vector<int> sell_contrib(sell_cptr[nsell]);
+        parallel_for(nsell, [&](int64_t lo, int64_t hi) {
+            for (int64_t e = lo; e < hi; ++e) {
+                int slot = sell_slot[e];
+                if (slot >= 0)
+                    std::copy(contrib.begin() + slot_cptr[slot], contrib.begin() + slot_cptr[slot + 1],
+                              sell_contrib.begin() + sell_cptr[e]);
+            }
+        });
+        h.sell_cptr = b.upload(sell_cptr);
+        h.sell_contrib = b.upload(sell_contrib);
+    }
     h.sell_slot = b.upload(sell_slot);
     h.sell_row = b.upload(sell_row);
-    h.slot_cptr = b.upload(slot_cptr);
-    h.slot_contrib = b.upload(contrib);
     h.bsr_offsets = b.upload(bsr_offsets);
     h.bsr_columns = b.upload(bsr_columns);
     h.slot_sell = b.upload(slot_sell);

@@ -14,27 +14,47 @@
 namespace fem {
 namespace {
 
-__global__ void gather_kernel(int64_t nsell, const int* __restrict__ sell_slot, const int* __restrict__ sell_row,
-                              const int* __restrict__ scol, const int* __restrict__ cptr,
-                              const int* __restrict__ contrib, const float* __restrict__ trip,
-                              float4* __restrict__ valA, float4* __restrict__ valB, float* __restrict__ valC,
-                              float* __restrict__ minv, int precond) {
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// One thread per SELL entry: sum its contributing triplet blocks in ascending
+// triplet order.  Contributor ids and values are loaded kGatherBatch at a time
+// before any is added, so that many independent loads are in flight per thread.
+constexpr int kGatherBatch = 4;
+
+__global__ void gather_kernel(int64_t nsell, const int* __restrict__ cptr, const int* __restrict__ contrib,
+                              const int* __restrict__ sell_row, const int* __restrict__ scol,
+                              const TripletPlanes trip, float4* __restrict__ valA, float4* __restrict__ valB,
+                              float* __restrict__ valC, float* __restrict__ minv, int precond) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nsell) return;
-    int slot = sell_slot[e];
-    if (slot < 0) return;  // padding: zero since setup
+    const int c0 = cptr[e], c1 = cptr[e + 1];
+    if (c0 == c1) return;  // padding: zero since setup
     float b[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) b[k] = 0.0f;
-    for (int c = cptr[slot]; c < cptr[slot + 1]; ++c) {
-        const float* t = trip + 9 * (int64_t)contrib[c];
+    for (int c = c0; c < c1; c += kGatherBatch) {
+        int id[kGatherBatch];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) b[k] += t[k];
+        for (int u = 0; u < kGatherBatch; ++u) id[u] = c + u < c1 ? __ldg(contrib + c + u) : -1;
+        float v[kGatherBatch][9];
+#pragma unroll
+        for (int u = 0; u < kGatherBatch; ++u) {
+            const int64_t t = id[u] < 0 ? 0 : id[u];
+            const float4 pa = __ldg(trip.a + t), pb = __ldg(trip.b + t);
+            const float pc = __ldg(trip.c + t);
+            v[u][0] = pa.x; v[u][1] = pa.y; v[u][2] = pa.z; v[u][3] = pa.w;
+            v[u][4] = pb.x; v[u][5] = pb.y; v[u][6] = pb.z; v[u][7] = pb.w;
+            v[u][8] = pc;
+        }
+#pragma unroll
+        for (int u = 0; u < kGatherBatch; ++u)
+            if (id[u] >= 0) {
+#pragma unroll
+                for (int k = 0; k < 9; ++k) b[k] += v[u][k];
+            }
     }
     valA[e] = make_float4(b[0], b[1], b[2], b[3]);
     valB[e] = make_float4(b[4], b[5], b[6], b[7]);
     valC[e] = b[8];
-    int row = sell_row[e];
+    const int row = sell_row[e];
     if (scol[e] == row) {
         float inv[9];
         if (precond == FEM_PRECOND_DIAG) inverse_point_diagonal(b, inv);
@@ -43,6 +63,17 @@ __global__ void gather_kernel(int64_t nsell, const int* __restrict__ sell_slot, 
 #pragma unroll
         for (int k = 0; k < 9; ++k) o[k] = inv[k];
     }
+}
+
+// Triplet planes back to the reference's row-major 9 floats per block.
+__global__ void export_triplets_kernel(int64_t ntrip, const TripletPlanes trip, float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntrip) return;
+    const float4 a = trip.a[i], b = trip.b[i];
+    float* o = out + 9 * i;
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+    o[8] = trip.c[i];
 }
 
 __global__ void export_bsr_kernel(int64_t nnzb, const int* __restrict__ slot_sell, const float4* __restrict__ valA,
@@ -64,8 +95,8 @@ cudaError_t launch_gather(Handle& h, cudaStream_t s) {
     if (h.nsell == 0) return cudaSuccess;
     int threads = 256;
     int64_t blocks = (h.nsell + threads - 1) / threads;
-    gather_kernel<<<(unsigned)blocks, threads, 0, s>>>(h.nsell, h.sell_slot, h.sell_row, h.scol, h.slot_cptr,
-                                                       h.slot_contrib, h.trip_vals, h.valA, h.valB, h.valC, h.minv,
+    gather_kernel<<<(unsigned)blocks, threads, 0, s>>>(h.nsell, h.sell_cptr, h.sell_contrib, h.sell_row, h.scol,
+                                                       h.trip, h.valA, h.valB, h.valC, h.minv,
                                                        h.precond);
     return cudaGetLastError();
 }
@@ -80,7 +111,10 @@ cudaError_t launch_export_bsr(Handle& h, float* values, cudaStream_t s) {
 
 cudaError_t launch_export_triplets(Handle& h, float* values, cudaStream_t s) {
     if (h.ntrip == 0) return cudaSuccess;
-    return cudaMemcpyAsync(values, h.trip_vals, sizeof(float) * 9 * (size_t)h.ntrip, cudaMemcpyDeviceToDevice, s);
+    int threads = 256;
+    int64_t blocks = (h.ntrip + threads - 1) / threads;
+    export_triplets_kernel<<<(unsigned)blocks, threads, 0, s>>>(h.ntrip, h.trip, values);
+    return cudaGetLastError();
 }
 
 }  // namespace fem

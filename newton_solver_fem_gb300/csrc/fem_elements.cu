@@ -123,75 +123,92 @@ __global__ void tet_force_kernel(int T, const int4* __restrict__ idx, const floa
 }
 
 // Reference kernels.py:1481-1601.  Lane g of an 8-lane group evaluates Gauss
-// point g of one hex; the 8 per-point corner forces are then summed over the
-// group with a fixed butterfly, lane a keeping corner a.
-__global__ void hex_force_kernel(int H, const int* __restrict__ idx, const float* __restrict__ invJ,
-                                 const float* __restrict__ detw, const float* __restrict__ mat,
-                                 const float4* __restrict__ q4, const float4* __restrict__ v4, float lo, float hi,
-                                 float4* __restrict__ out) {
-    int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    int h = gid >> 3, g = gid & 7;
-    bool live = h < H;
-    int he = live ? h : H - 1;
-    int node = idx[8 * he + g];
-    float3 xg = xyz(q4[node]), vg = xyz(v4[node]);
-    float k_mu = mat[3 * he], k_lambda = mat[3 * he + 1], k_damp = mat[3 * he + 2];
-    float alpha = 1.0f + k_mu / k_lambda - k_mu / (4.0f * k_lambda);
+// point g of one hex.  F = (sum_a x_a (x) dN_a/dxi) inv_J0 and likewise dF/dt,
+// so no per-corner gradient is kept; the corner forces of the point are
+// (P inv_J0^T w) dN_a/dxi.  The 8 points' forces are summed per corner by a
+// fixed three-level reduce-scatter over the group (halves, quarters, eighths):
+// 21 shuffles, lane a ending with corner a.
+__global__ void __launch_bounds__(256, 3) hex_force_kernel(int H, const int* __restrict__ idx,
+                                                        const float* __restrict__ invJ,
+                                                        const float* __restrict__ detw,
+                                                        const float* __restrict__ mat,
+                                                        const float4* __restrict__ q4,
+                                                        const float4* __restrict__ v4, float lo, float hi,
+                                                        float4* __restrict__ out) {
+    __shared__ float s_tab[8][8][3];  // Gauss-point table (lane-varying reads serialise in constant memory)
+    if (threadIdx.x < 192) (&s_tab[0][0][0])[threadIdx.x] = (&c_dNdxi[0][0][0])[threadIdx.x];
+    __syncthreads();
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = gid >> 3, g = gid & 7;
+    const bool live = h < H;
+    const int64_t he = live ? h : H - 1;  // lanes past the end work on a valid hex and store nothing
+    const int node = idx[8 * he + g];
+    const float3 xg = xyz(q4[node]), vg = xyz(v4[node]);
+    const float k_mu = mat[3 * he], k_lambda = mat[3 * he + 1], k_damp = mat[3 * he + 2];
+    const float alpha = 1.0f + k_mu / k_lambda - k_mu / (4.0f * k_lambda);
     M3 iJ;
 #pragma unroll
     for (int k = 0; k < 9; ++k) iJ.m[k / 3][k % 3] = invJ[(8 * he + g) * 9 + k];
-    float w = detw[8 * he + g];
-    int base = threadIdx.x & ~7 & 31;
-    float3 xa[8], va[8], dN[8];
-    M3 F, dFdt;
+    const float w = detw[8 * he + g];
+    const int base = threadIdx.x & 24;  // first lane of this 8-lane group within the warp
+    M3 GX, GV;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) F.m[i][j] = dFdt.m[i][j] = 0.0f;
+        for (int j = 0; j < 3; ++j) GX.m[i][j] = GV.m[i][j] = 0.0f;
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
-        xa[a] = f3(__shfl_sync(0xffffffffu, xg.x, base + a), __shfl_sync(0xffffffffu, xg.y, base + a),
-                   __shfl_sync(0xffffffffu, xg.z, base + a));
-        va[a] = f3(__shfl_sync(0xffffffffu, vg.x, base + a), __shfl_sync(0xffffffffu, vg.y, base + a),
-                   __shfl_sync(0xffffffffu, vg.z, base + a));
-        float3 d = f3(c_dNdxi[g][a][0], c_dNdxi[g][a][1], c_dNdxi[g][a][2]);
-        dN[a] = mulT(iJ, d);  // inv_J0^T dN/dxi
+        const float xs[3] = {__shfl_sync(0xffffffffu, xg.x, base + a), __shfl_sync(0xffffffffu, xg.y, base + a),
+                             __shfl_sync(0xffffffffu, xg.z, base + a)};
+        const float vs[3] = {__shfl_sync(0xffffffffu, vg.x, base + a), __shfl_sync(0xffffffffu, vg.y, base + a),
+                             __shfl_sync(0xffffffffu, vg.z, base + a)};
+        const float d[3] = {s_tab[g][a][0], s_tab[g][a][1], s_tab[g][a][2]};
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            float xi = i == 0 ? xa[a].x : (i == 1 ? xa[a].y : xa[a].z);
-            float vi = i == 0 ? va[a].x : (i == 1 ? va[a].y : va[a].z);
-            F.m[i][0] += xi * dN[a].x;
-            F.m[i][1] += xi * dN[a].y;
-            F.m[i][2] += xi * dN[a].z;
-            dFdt.m[i][0] += vi * dN[a].x;
-            dFdt.m[i][1] += vi * dN[a].y;
-            dFdt.m[i][2] += vi * dN[a].z;
-        }
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                GX.m[i][k] += xs[i] * d[k];
+                GV.m[i][k] += vs[i] * d[k];
+            }
     }
+    M3 F = matmul(GX, iJ);
+    const M3 dFdt = matmul(GV, iJ);
     F = clamp_stretch(F, lo, hi);
-    float3 fc0 = col(F, 0), fc1 = col(F, 1), fc2 = col(F, 2);
-    float Ic = dot3(fc0, fc0) + dot3(fc1, fc1) + dot3(fc2, fc2);
-    float sdev = k_mu * (1.0f - 1.0f / (Ic + 1.0f));
-    float J = fmaxf(det3(F), 0.01f);
-    M3 cof = from_cols(cross3(fc1, fc2), cross3(fc2, fc0), cross3(fc0, fc1));
-    float vol = k_lambda * (J - alpha);
+    const float3 fc0 = col(F, 0), fc1 = col(F, 1), fc2 = col(F, 2);
+    const float Ic = dot3(fc0, fc0) + dot3(fc1, fc1) + dot3(fc2, fc2);
+    const float sdev = k_mu * (1.0f - 1.0f / (Ic + 1.0f));
+    const float J = fmaxf(det3(F), 0.01f);
+    const M3 cof = from_cols(cross3(fc1, fc2), cross3(fc2, fc0), cross3(fc0, fc1));
+    const float vol = k_lambda * (J - alpha);
     M3 P;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) P.m[i][j] = (F.m[i][j] * sdev + dFdt.m[i][j] * k_damp) + cof.m[i][j] * vol;
-    float3 mine = f3(0.f, 0.f, 0.f);
+        for (int j = 0; j < 3; ++j) P.m[i][j] = ((F.m[i][j] * sdev + dFdt.m[i][j] * k_damp) + cof.m[i][j] * vol) * w;
+    const M3 PJ = matmulT(P, iJ);  // P inv_J0^T, so that the corner force is PJ dN_a/dxi
+    float3 f[8];
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        float3 fa = mul(P, dN[a]) * w;
+    for (int a = 0; a < 8; ++a) f[a] = mul(PJ, f3(s_tab[g][a][0], s_tab[g][a][1], s_tab[g][a][2]));
+    // reduce-scatter: keep the half / quarter / eighth of the corners whose index
+    // bits match this lane's, send the rest to the partner, add what it sends
+    float3 r4[4];
+    const bool hi4 = (g & 4) != 0, hi2 = (g & 2) != 0, hi1 = (g & 1) != 0;
 #pragma unroll
-        for (int off = 1; off < 8; off <<= 1) {
-            fa.x += __shfl_xor_sync(0xffffffffu, fa.x, off);
-            fa.y += __shfl_xor_sync(0xffffffffu, fa.y, off);
-            fa.z += __shfl_xor_sync(0xffffffffu, fa.z, off);
-        }
-        if (a == g) mine = fa;
+    for (int k = 0; k < 4; ++k) {
+        const float3 keep = hi4 ? f[4 + k] : f[k], send = hi4 ? f[k] : f[4 + k];
+        r4[k] = keep + f3(__shfl_xor_sync(0xffffffffu, send.x, 4), __shfl_xor_sync(0xffffffffu, send.y, 4),
+                          __shfl_xor_sync(0xffffffffu, send.z, 4));
     }
+    float3 r2[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float3 keep = hi2 ? r4[2 + k] : r4[k], send = hi2 ? r4[k] : r4[2 + k];
+        r2[k] = keep + f3(__shfl_xor_sync(0xffffffffu, send.x, 2), __shfl_xor_sync(0xffffffffu, send.y, 2),
+                          __shfl_xor_sync(0xffffffffu, send.z, 2));
+    }
+    const float3 keep = hi1 ? r2[1] : r2[0], send = hi1 ? r2[0] : r2[1];
+    const float3 mine = keep + f3(__shfl_xor_sync(0xffffffffu, send.x, 1), __shfl_xor_sync(0xffffffffu, send.y, 1),
+                                  __shfl_xor_sync(0xffffffffu, send.z, 1));
     if (live) out[8 * h + g] = f4(-mine);
 }
 
@@ -309,7 +326,7 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
 // Reference kernels.py:294-323 (diagonal with springs), 141-153 (mass only), 326-366 (off-diagonal).
 __global__ void constant_diag_kernel(int P, const float* __restrict__ mass, const int* __restrict__ sptr,
                                      const int* __restrict__ sent, const float* __restrict__ ke,
-                                     const float* __restrict__ kd, float dt, float* __restrict__ vals) {
+                                     const float* __restrict__ kd, float dt, TripletPlanes vals) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
     float dt2 = dt * dt;
@@ -318,23 +335,17 @@ __global__ void constant_diag_kernel(int P, const float* __restrict__ mass, cons
         int s = sent[e] >> 1;
         d = d + dt * kd[s] + dt2 * ke[s];
     }
-    float* o = vals + 9 * (size_t)i;
-    o[0] = d; o[1] = 0.f; o[2] = 0.f;
-    o[3] = 0.f; o[4] = d; o[5] = 0.f;
-    o[6] = 0.f; o[7] = 0.f; o[8] = d;
+    const float o[9] = {d, 0.f, 0.f, 0.f, d, 0.f, 0.f, 0.f, d};
+    store_block(vals, i, o);
 }
 
 __global__ void constant_offdiag_kernel(int P, int S, const float* __restrict__ ke, const float* __restrict__ kd,
-                                        float dt, float* __restrict__ vals) {
+                                        float dt, TripletPlanes vals) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
     float neg_off = -(dt * kd[s] + dt * dt * ke[s]);
-    for (int k = 0; k < 2; ++k) {
-        float* o = vals + 9 * ((size_t)P + 2 * (size_t)s + k);
-        o[0] = neg_off; o[1] = 0.f; o[2] = 0.f;
-        o[3] = 0.f; o[4] = neg_off; o[5] = 0.f;
-        o[6] = 0.f; o[7] = 0.f; o[8] = neg_off;
-    }
+    const float o[9] = {neg_off, 0.f, 0.f, 0.f, neg_off, 0.f, 0.f, 0.f, neg_off};
+    for (int k = 0; k < 2; ++k) store_block(vals, (int64_t)P + 2 * (int64_t)s + k, o);
 }
 
 constexpr int kTetTangentThreads = 128;
@@ -347,7 +358,7 @@ constexpr int kTetFactor = 40;
 __global__ void __launch_bounds__(kTetTangentThreads) tet_tangent_kernel(
     int T, const int4* __restrict__ idx, const float* __restrict__ pose, const float* __restrict__ mat,
     const float* __restrict__ mu_scale, const float4* __restrict__ q4, float lo, float hi, float dt, int64_t trip_off,
-    float* __restrict__ vals) {
+    TripletPlanes vals) {
     __shared__ float sm[kTetTangentThreads][kTetFactor + 1];
     int lt = threadIdx.x;
     int t = blockIdx.x * kTetTangentThreads + lt;
@@ -408,10 +419,12 @@ __global__ void __launch_bounds__(kTetTangentThreads) tet_tangent_kernel(
         const float* f = sm[le];
         float mode = f[39];
         if (mode == 2.0f) continue;
-        float* o = vals + 9 * (trip_off + 16 * (int64_t)te + ab);
+        const int64_t ti = trip_off + 16 * (int64_t)te + ab;
+        float o[9];
         if (mode == 1.0f) {
 #pragma unroll
             for (int k = 0; k < 9; ++k) o[k] = 0.0f;
+            store_block(vals, ti, o);
             continue;
         }
         int a = ab >> 2, bb = ab & 3;
@@ -433,114 +446,107 @@ __global__ void __launch_bounds__(kTetTangentThreads) tet_tangent_kernel(
                 float kvol = ja[i] * jb[j] * lam;
                 o[3 * i + j] = (kdev + kvol) * scale;
             }
+        store_block(vals, ti, o);
     }
 }
 
 constexpr int kHexPerCta = 4;
 
-// Reference kernels.py:1609-1747 with F, the clamp and cof(F) computed once
-// per Gauss point instead of once per (a, b) block.
+// Reference kernels.py:1609-1747.  K_ab = h^2 sum_g w_g [k_mu s (gN_a . gN_b) I
+// + coef (F gN_a)(F gN_b)^T + lambda (cof F gN_a)(cof F gN_b)^T], with F, the
+// clamp and cof F computed once per Gauss point instead of once per (a, b)
+// block.  A CTA takes kHexPerCta hexes, one thread per (hex, point g, node a):
+//   phase 1  thread (g, a) forms x_a (x) gN_a; the 8 lanes of point g sum F with
+//            a fixed xor butterfly (bit-identical in all 8 lanes), apply the
+//            clamp and cof F, and each lane stores gN_a, F gN_a and cof F gN_a
+//            of its node as packed float4 records in shared memory;
+//   phase 2  thread (a, b) accumulates its 3x3 block over the 8 points.
+// Every thread is busy in both phases; one CTA barrier separates them.
 __global__ void __launch_bounds__(256) hex_tangent_kernel(int H, const int* __restrict__ idx,
                                                           const float* __restrict__ invJ,
                                                           const float* __restrict__ detw,
                                                           const float* __restrict__ mat,
                                                           const float4* __restrict__ q4, float lo, float hi, float dt,
-                                                          int64_t trip_off, float* __restrict__ vals) {
-    __shared__ float s_dN[kHexPerCta][8][8][3];
-    __shared__ float s_Fd[kHexPerCta][8][8][3];
-    __shared__ float s_cd[kHexPerCta][8][8][3];
-    __shared__ float s_F[kHexPerCta][8][18];
-    __shared__ float s_c[kHexPerCta][8][4];
-    __shared__ float s_x[kHexPerCta][8][3];
-    int tid = threadIdx.x;
-    int hl = tid >> 6, g = (tid >> 3) & 7, a = tid & 7;
-    int h = blockIdx.x * kHexPerCta + hl;
-    bool live = h < H;
-    if (live) {
-        const float* iJ = invJ + (8 * (int64_t)h + g) * 9;
-        float3 d = f3(c_dNdxi[g][a][0], c_dNdxi[g][a][1], c_dNdxi[g][a][2]);
-        float3 dn = f3(iJ[0] * d.x + iJ[3] * d.y + iJ[6] * d.z, iJ[1] * d.x + iJ[4] * d.y + iJ[7] * d.z,
-                       iJ[2] * d.x + iJ[5] * d.y + iJ[8] * d.z);
-        s_dN[hl][g][a][0] = dn.x;
-        s_dN[hl][g][a][1] = dn.y;
-        s_dN[hl][g][a][2] = dn.z;
-        if (g == 0) {
-            float3 xa = xyz(q4[idx[8 * (int64_t)h + a]]);
-            s_x[hl][a][0] = xa.x;
-            s_x[hl][a][1] = xa.y;
-            s_x[hl][a][2] = xa.z;
-        }
-    }
+                                                          int64_t trip_off, TripletPlanes vals) {
+    // The Gauss-point table is read with a different (point, node) in every
+    // lane; from constant memory that serialises, so it is staged in shared memory.
+    __shared__ float s_tab[8][8][3];
+    // per (hex, point, node): q0 = (gN.xyz, Fd.x), q1 = (Fd.yz, cd.xy), q2 = cd.z
+    __shared__ float4 s_q0[kHexPerCta][8][8];
+    __shared__ float4 s_q1[kHexPerCta][8][8];
+    __shared__ float s_q2[kHexPerCta][8][8];
+    __shared__ float4 s_c[kHexPerCta][8];  // per point: k_mu s w, coef w, lambda w
+    const int tid = threadIdx.x;
+    const int hl = tid >> 6, g = (tid >> 3) & 7, a = tid & 7;
+    const int h = blockIdx.x * kHexPerCta + hl;
+    const bool live = h < H;
+    const int64_t he = live ? h : H - 1;  // lanes past the end work on a valid hex and store nothing
+    if (tid < 192) (&s_tab[0][0][0])[tid] = (&c_dNdxi[0][0][0])[tid];
     __syncthreads();
-    if (tid < kHexPerCta * 8) {
-        int hh = tid >> 3, gg = tid & 7;
-        int he = blockIdx.x * kHexPerCta + hh;
-        if (he < H) {
-            M3 F;
+    {
+        const float* iJ = invJ + (8 * he + g) * 9;
+        const float3 d = f3(s_tab[g][a][0], s_tab[g][a][1], s_tab[g][a][2]);
+        const float3 dn = f3(iJ[0] * d.x + iJ[3] * d.y + iJ[6] * d.z, iJ[1] * d.x + iJ[4] * d.y + iJ[7] * d.z,
+                             iJ[2] * d.x + iJ[5] * d.y + iJ[8] * d.z);
+        const float3 xa = xyz(q4[idx[8 * he + a]]);
+        M3 F;
+        const float xs[3] = {xa.x, xa.y, xa.z};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            F.m[i][0] = xs[i] * dn.x;
+            F.m[i][1] = xs[i] * dn.y;
+            F.m[i][2] = xs[i] * dn.z;
+        }
+#pragma unroll
+        for (int off = 1; off < 8; off <<= 1)
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
-                for (int j = 0; j < 3; ++j) F.m[i][j] = 0.0f;
-#pragma unroll
-            for (int aa = 0; aa < 8; ++aa)
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) F.m[i][j] += s_x[hh][aa][i] * s_dN[hh][gg][aa][j];
-            F = clamp_stretch(F, lo, hi);
-            float3 fc0 = col(F, 0), fc1 = col(F, 1), fc2 = col(F, 2);
-            float Ic = dot3(fc0, fc0) + dot3(fc1, fc1) + dot3(fc2, fc2);
-            float Ic1 = fmaxf(Ic + 1.0f, 1.0e-6f);
-            float s = 1.0f - 1.0f / Ic1;
-            float k_mu = mat[3 * (int64_t)he], k_lambda = mat[3 * (int64_t)he + 1];
-            float coef = k_mu * 2.0f / (Ic1 * Ic1);
-            M3 cof = from_cols(cross3(fc1, fc2), cross3(fc2, fc0), cross3(fc0, fc1));
-#pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                s_F[hh][gg][k] = F.m[k / 3][k % 3];
-                s_F[hh][gg][9 + k] = cof.m[k / 3][k % 3];
-            }
-            s_c[hh][gg][0] = k_mu * s;
-            s_c[hh][gg][1] = coef;
-            s_c[hh][gg][2] = k_lambda;
-            s_c[hh][gg][3] = detw[8 * (int64_t)he + gg];
-        }
-    }
-    __syncthreads();
-    if (live) {
-        const float* Fm = s_F[hl][g];
-        float3 dn = f3(s_dN[hl][g][a][0], s_dN[hl][g][a][1], s_dN[hl][g][a][2]);
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            s_Fd[hl][g][a][i] = Fm[3 * i] * dn.x + Fm[3 * i + 1] * dn.y + Fm[3 * i + 2] * dn.z;
-            s_cd[hl][g][a][i] = Fm[9 + 3 * i] * dn.x + Fm[9 + 3 * i + 1] * dn.y + Fm[9 + 3 * i + 2] * dn.z;
+                for (int j = 0; j < 3; ++j) F.m[i][j] += __shfl_xor_sync(0xffffffffu, F.m[i][j], off);
+        F = clamp_stretch(F, lo, hi);
+        const float3 fc0 = col(F, 0), fc1 = col(F, 1), fc2 = col(F, 2);
+        const float Ic = dot3(fc0, fc0) + dot3(fc1, fc1) + dot3(fc2, fc2);
+        const float Ic1 = fmaxf(Ic + 1.0f, 1.0e-6f);
+        const float sdev = 1.0f - 1.0f / Ic1;
+        const float k_mu = mat[3 * he], k_lambda = mat[3 * he + 1];
+        const float coef = k_mu * 2.0f / (Ic1 * Ic1);
+        const M3 cof = from_cols(cross3(fc1, fc2), cross3(fc2, fc0), cross3(fc0, fc1));
+        const float3 fd = mul(F, dn), cd = mul(cof, dn);
+        s_q0[hl][g][a] = make_float4(dn.x, dn.y, dn.z, fd.x);
+        s_q1[hl][g][a] = make_float4(fd.y, fd.z, cd.x, cd.y);
+        s_q2[hl][g][a] = cd.z;
+        if (a == 0) {
+            const float w = detw[8 * he + g];
+            s_c[hl][g] = make_float4(k_mu * sdev * w, coef * w, k_lambda * w, 0.0f);
         }
     }
     __syncthreads();
     if (!live) return;
-    int ra = (tid >> 3) & 7, cb = tid & 7;
+    const int ra = (tid >> 3) & 7, cb = tid & 7;
     float K[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) K[k] = 0.0f;
 #pragma unroll
     for (int gg = 0; gg < 8; ++gg) {
-        float kms = s_c[hl][gg][0], coef = s_c[hl][gg][1], lam = s_c[hl][gg][2], w = s_c[hl][gg][3];
-        float dot_ab = s_dN[hl][gg][ra][0] * s_dN[hl][gg][cb][0] + s_dN[hl][gg][ra][1] * s_dN[hl][gg][cb][1] +
-                       s_dN[hl][gg][ra][2] * s_dN[hl][gg][cb][2];
-        float diag = kms * dot_ab;
+        const float4 c = s_c[hl][gg];
+        const float4 a0 = s_q0[hl][gg][ra], a1 = s_q1[hl][gg][ra];
+        const float4 b0 = s_q0[hl][gg][cb], b1 = s_q1[hl][gg][cb];
+        const float a2 = s_q2[hl][gg][ra], b2 = s_q2[hl][gg][cb];
+        const float fa[3] = {a0.w, a1.x, a1.y}, ca[3] = {a1.z, a1.w, a2};
+        const float fb[3] = {b0.w * c.y, b1.x * c.y, b1.y * c.y}, cbv[3] = {b1.z * c.z, b1.w * c.z, b2 * c.z};
+        const float diag = c.x * (a0.x * b0.x + a0.y * b0.y + a0.z * b0.z);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                float kdev = (i == j ? diag : 0.0f) + s_Fd[hl][gg][ra][i] * s_Fd[hl][gg][cb][j] * coef;
-                float kvol = s_cd[hl][gg][ra][i] * s_cd[hl][gg][cb][j] * lam;
-                K[3 * i + j] = K[3 * i + j] + (kdev + kvol) * w;
-            }
+            for (int j = 0; j < 3; ++j) K[3 * i + j] += fa[i] * fb[j] + ca[i] * cbv[j];
+        K[0] += diag;
+        K[4] += diag;
+        K[8] += diag;
     }
-    float scale = dt * dt;
-    float* o = vals + 9 * (trip_off + 64 * (int64_t)h + 8 * ra + cb);
+    const float scale = dt * dt;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) o[k] = K[k] * scale;
+    for (int k = 0; k < 9; ++k) K[k] *= scale;
+    store_block(vals, trip_off + 64 * (int64_t)h + 8 * ra + cb, K);
 }
 
 inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
@@ -639,10 +645,10 @@ cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity
 cudaError_t launch_constant_blocks(Handle& h, float dt, cudaStream_t s) {
     if (h.P > 0)
         constant_diag_kernel<<<blocks_for(h.P, 256), 256, 0, s>>>(h.P, h.mass, h.node_spring_ptr, h.node_spring_ent,
-                                                                  h.spring_ke, h.spring_kd, dt, h.trip_vals);
+                                                                  h.spring_ke, h.spring_kd, dt, h.trip);
     if (h.S > 0)
         constant_offdiag_kernel<<<blocks_for(h.S, 256), 256, 0, s>>>(h.P, h.S, h.spring_ke, h.spring_kd, dt,
-                                                                     h.trip_vals);
+                                                                     h.trip);
     return cudaGetLastError();
 }
 
@@ -651,11 +657,11 @@ cudaError_t launch_element_tangent(Handle& h, float dt, cudaStream_t s) {
     if (h.T > 0)
         tet_tangent_kernel<<<blocks_for(h.T, kTetTangentThreads), kTetTangentThreads, 0, s>>>(
             h.T, h.tet_idx, h.tet_pose, h.tet_mat, h.mu_scale, h.q4, h.min_stretch, h.max_stretch, dt, tet_off,
-            h.trip_vals);
+            h.trip);
     if (h.H > 0)
         hex_tangent_kernel<<<blocks_for(h.H, kHexPerCta), 256, 0, s>>>(
             h.H, h.hex_idx, h.hex_invJ, h.hex_detw, h.hex_mat, h.q4, h.min_stretch, h.max_stretch, dt,
-            tet_off + 16 * (int64_t)h.T, h.trip_vals);
+            tet_off + 16 * (int64_t)h.T, h.trip);
     return cudaGetLastError();
 }
 

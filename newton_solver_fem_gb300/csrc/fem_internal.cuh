@@ -18,6 +18,24 @@ constexpr unsigned kFixedBit = 0x80000000u;  // row_info: fixed-node flag; low b
 constexpr int kStatusTimeout = 1 << 2;
 constexpr int kStatusNonFinite = 1 << 1;
 
+// Triplet blocks (the reference layout [P | 2S | 16T | 64H]) stored in three
+// planes, the same split as the SELL matrix: block i is (a[i], b[i], c[i]) =
+// ((a00 a01 a02 a10), (a11 a12 a20 a21), a22), so that a block is written and
+// read with two aligned 16-byte accesses and one 4-byte access.
+struct TripletPlanes {
+    float4* a = nullptr;
+    float4* b = nullptr;
+    float* c = nullptr;
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void store_block(const TripletPlanes& t, int64_t i, const float* v) {
+    t.a[i] = make_float4(v[0], v[1], v[2], v[3]);
+    t.b[i] = make_float4(v[4], v[5], v[6], v[7]);
+    t.c[i] = v[8];
+}
+#endif
+
 // Per-scene persistent solver statistics written by the PCG epilogue.
 struct SceneStats {
     int iterations;
@@ -136,10 +154,10 @@ struct Handle {
     float4* q4 = nullptr;
     float4* v4 = nullptr;
     // assembly
-    float* trip_vals = nullptr;   // [ntrip*9]
+    TripletPlanes trip;           // [ntrip] blocks
     int* sell_slot = nullptr;     // [nsell] canonical slot or -1
-    int* slot_cptr = nullptr;     // [nnzb+1]
-    int* slot_contrib = nullptr;  // triplet ids
+    int* sell_cptr = nullptr;     // [nsell+1] contributor range of each SELL entry
+    int* sell_contrib = nullptr;  // triplet ids, ascending within each entry
     int* bsr_offsets = nullptr;   // [P+1]
     int* bsr_columns = nullptr;   // [nnzb]
     int* slot_sell = nullptr;     // [nnzb] canonical slot -> SELL entry
