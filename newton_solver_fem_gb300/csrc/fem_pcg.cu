@@ -281,34 +281,43 @@ __device__ __forceinline__ float4* stage_slot(const PcgArgs& a, const Smem& sm, 
 // One grid-wide reduction step, entered by every thread of the CTA once the
 // slice partials of the current phase are in sm.part:
 //   1. warp 0 writes this CTA's per-scene segment partials (sum or max of its
-//      slices of the scene, in slice order) to buf;
+//      slices of the scene: lane-strided, then a fixed xor butterfly) to buf;
 //   2. one thread arrives at the grid barrier and waits for every CTA;
-//   3. the per-scene totals over all segments, in a fixed order, go to sm.tot.
+//   3. the per-scene totals over all segments (each lane sums its strided
+//      segments in ascending order, then the butterfly) go to sm.tot, and
+//      upd(s) runs once per scene: on lane s of warp 0 for a few scenes, else
+//      on the thread that formed scene s's totals.
 // Every CTA forms bit-identical totals.  Consecutive reductions alternate
 // between two buffers: a CTA that races ahead can only write a buffer again
 // after the next barrier, which every CTA reaches only once it has finished
 // reading that buffer's previous contents.  Partials and totals are float,
 // like the reference solver's float32 dot products; the order is fixed, so
-// results are deterministic.  Returns false after a timed-out wait.
+// results are deterministic.  When s_any is given it is cleared on entry (for
+// the updates to set).  Returns false after a timed-out wait.
+constexpr int kSegLoadBatch = 8;  // segment partials a lane loads before adding them
+
+template <class Update>
 __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf, int nv, bool is_max, int first,
-                                   int last, unsigned& epoch, int* s_ok) {
+                                   int last, unsigned& epoch, int* s_ok, int* s_any, Update upd) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int S = a.nscenes;
-    __syncthreads();  // slice partials complete
+    if (threadIdx.x == 0 && s_any != nullptr) *s_any = 0;
+    __syncthreads();  // slice partials complete, activity flag cleared
     if (warp == 0) {
         if (first < last) {
             const int s0 = a.cta_first_scene[blockIdx.x];
             const int nsc = a.slice_scene[last - 1] - s0 + 1;
-            for (int t = lane; t < nsc; t += 32) {
+            for (int t = 0; t < nsc; ++t) {
                 const int sc = s0 + t;
                 const int lo = max(a.scene_slice0[sc], first), hi = min(a.scene_slice0[sc + 1], last);
                 for (int k = 0; k < nv; ++k) {
                     float acc = 0.f;
-                    for (int sl = lo; sl < hi; ++sl) {
-                        float v = sm.part[(sl - first) * 3 + k];
+                    for (int sl = lo + lane; sl < hi; sl += 32) {
+                        const float v = sm.part[(sl - first) * 3 + k];
                         acc = is_max ? fmaxf(acc, v) : acc + v;
                     }
-                    buf[(size_t)(a.cta_seg_base[blockIdx.x] + t) * 3 + k] = acc;
+                    acc = is_max ? warp_max(acc) : warp_sum(acc);
+                    if (lane == 0) buf[(size_t)(a.cta_seg_base[blockIdx.x] + t) * 3 + k] = acc;
                 }
             }
         }
@@ -319,36 +328,47 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
         if (ok && S <= kWarpReducedScenes) {
             for (int sc = 0; sc < S; ++sc) {
                 const int lo = a.scene_seg0[sc], hi = a.scene_seg0[sc + 1];
-                for (int k = 0; k < nv; ++k) {
-                    float acc = 0.f;
-                    for (int g = lo + lane; g < hi; g += 32) {
-                        float v = __ldcg(buf + (size_t)g * 3 + k);
-                        acc = is_max ? fmaxf(acc, v) : acc + v;
+                float acc[3] = {0.f, 0.f, 0.f};
+                for (int g0 = lo + lane; g0 < hi; g0 += 32 * kSegLoadBatch) {
+                    float v[kSegLoadBatch][3];
+#pragma unroll
+                    for (int u = 0; u < kSegLoadBatch; ++u) {
+                        const int g = g0 + 32 * u;
+                        for (int k = 0; k < nv; ++k) v[u][k] = g < hi ? __ldcg(buf + (size_t)g * 3 + k) : 0.f;
                     }
-                    acc = is_max ? warp_max(acc) : warp_sum(acc);
-                    if (lane == 0) sm.tot[sc * 3 + k] = acc;
+#pragma unroll
+                    for (int u = 0; u < kSegLoadBatch; ++u)
+                        if (g0 + 32 * u < hi)
+                            for (int k = 0; k < nv; ++k) acc[k] = is_max ? fmaxf(acc[k], v[u][k]) : acc[k] + v[u][k];
+                }
+                for (int k = 0; k < nv; ++k) {
+                    const float t = is_max ? warp_max(acc[k]) : warp_sum(acc[k]);
+                    if (lane == 0) sm.tot[sc * 3 + k] = t;
                 }
             }
+            __syncwarp();
+            if (lane < S) upd(lane);
         }
         if (lane == 0) *s_ok = ok;
     }
-    __syncthreads();
-    if (!*s_ok) return false;
     if (S > kWarpReducedScenes) {
+        __syncthreads();
+        if (!*s_ok) return false;
         for (int sc = threadIdx.x; sc < S; sc += blockDim.x) {
             const int lo = a.scene_seg0[sc], hi = a.scene_seg0[sc + 1];
             for (int k = 0; k < nv; ++k) {
                 float acc = 0.f;
                 for (int g = lo; g < hi; ++g) {
-                    float v = __ldcg(buf + (size_t)g * 3 + k);
+                    const float v = __ldcg(buf + (size_t)g * 3 + k);
                     acc = is_max ? fmaxf(acc, v) : acc + v;
                 }
                 sm.tot[sc * 3 + k] = acc;
             }
+            upd(sc);
         }
-        __syncthreads();
     }
-    return true;
+    __syncthreads();
+    return *s_ok != 0;
 }
 
 __device__ __forceinline__ float rhs_scale(float maximum) {
@@ -420,13 +440,12 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     }
     float* const buf0 = a.seg_part;
     float* const buf1 = a.seg_part + (size_t)a.nseg * 3;
-    if (!reduce_across_grid(a, sm, buf0, 1, true, first, last, epoch, &s_ok)) return;
-    for (int s = threadIdx.x; s < S; s += blockDim.x) {
-        float mxs = (float)sm.tot[s * 3];
+    auto set_scale = [&](int s) {
+        const float mxs = sm.tot[s * 3];
         sm.st[s].scale = rhs_scale(mxs);
         sm.st[s].zero = mxs == 0.0f;
-    }
-    __syncthreads();
+    };
+    if (!reduce_across_grid(a, sm, buf0, 1, true, first, last, epoch, &s_ok, nullptr, set_scale)) return;
 
     // ---------------- phase 1: normalise, initial residual and preconditioned residual
     for (int sl = first + warp; sl < last; sl += W) {
@@ -463,10 +482,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             p[0] = rr; p[1] = rz; p[2] = bb;
         }
     }
-    if (!reduce_across_grid(a, sm, buf1, 3, false, first, last, epoch, &s_ok)) return;
-    if (threadIdx.x == 0) s_any = 0;
-    __syncthreads();
-    for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    auto start_cg = [&](int s) {
         SceneState& st = sm.st[s];
         st.rr = sm.tot[s * 3];
         st.rz = sm.tot[s * 3 + 1];
@@ -481,8 +497,8 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             atomicOr(a.status, kStatusNonFinite);
         }
         if (st.active) atomicOr(&s_any, 1);
-    }
-    __syncthreads();
+    };
+    if (!reduce_across_grid(a, sm, buf1, 3, false, first, last, epoch, &s_ok, &s_any, start_cg)) return;
 
     // ---------------- CG iterations
     for (int it = 0; s_any; ++it) {
@@ -516,12 +532,11 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             pap = warp_sum(pap);
             if (lane == 0) sm.part[(sl - first) * 3] = pap;
         }
-        if (!reduce_across_grid(a, sm, buf0, 1, false, first, last, epoch, &s_ok)) return;
-        for (int s = threadIdx.x; s < S; s += blockDim.x) {
+        auto set_alpha = [&](int s) {
             SceneState& st = sm.st[s];
             if (st.active) st.alpha = (float)(st.rz / sm.tot[s * 3]);
-        }
-        __syncthreads();
+        };
+        if (!reduce_across_grid(a, sm, buf0, 1, false, first, last, epoch, &s_ok, nullptr, set_alpha)) return;
         // phase B: x += alpha p, r -= alpha y, z = M r, partial r.r and r.z
         for (int sl = first + warp; sl < last; sl += W) {
             int2 meta = a.slice_meta[sl];
@@ -550,13 +565,10 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 p[0] = rr; p[1] = rz;
             }
         }
-        if (!reduce_across_grid(a, sm, buf1, 2, false, first, last, epoch, &s_ok)) return;
-        if (threadIdx.x == 0) s_any = 0;
-        __syncthreads();
-        for (int s = threadIdx.x; s < S; s += blockDim.x) {
+        auto next_iteration = [&](int s) {
             SceneState& st = sm.st[s];
-            if (!st.active) continue;
-            double rr = sm.tot[s * 3], rz_new = sm.tot[s * 3 + 1];
+            if (!st.active) return;
+            const double rr = sm.tot[s * 3], rz_new = sm.tot[s * 3 + 1];
             st.iters += 1;
             st.beta = (float)(rz_new / st.rz);
             st.rz = rz_new;
@@ -567,8 +579,8 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 atomicOr(a.status, kStatusNonFinite);
             }
             if (st.active) atomicOr(&s_any, 1);
-        }
-        __syncthreads();
+        };
+        if (!reduce_across_grid(a, sm, buf1, 2, false, first, last, epoch, &s_ok, &s_any, next_iteration)) return;
     }
 
     // ---------------- epilogue: restore scale, integrate, fixed restore
