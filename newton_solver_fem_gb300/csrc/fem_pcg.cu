@@ -243,6 +243,10 @@ struct Smem {
     SceneState* st;   // [S]
     float* tot;       // [S * 3] per-scene totals of the last reduction
     float4* stage;    // [L * 32 * 2] (p, y) per row, when staged in shared memory
+    int* segb;        // [nsc + 1] slice bounds of this CTA's per-scene segments
+    int* sseg;        // [S + 1] first segment of every scene (copy of scene_seg0)
+    int nsc;          // scenes (segments) this CTA covers
+    int segbase;      // this CTA's first segment
 };
 
 // Scenes up to this count are reduced lane-parallel over their segments by one
@@ -260,7 +264,7 @@ __host__ __device__ __forceinline__ bool stage_in_smem(int L, int threads) {
 // a 16-byte boundary (the staging area holds float4).  One definition serves
 // the kernel and the host-side size.
 struct SmemLayout {
-    size_t part, st, tot, stage, total;
+    size_t part, st, tot, segb, sseg, stage, total;
 };
 __host__ __device__ __forceinline__ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
 __host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage) {
@@ -268,7 +272,9 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool st
     m.part = 0;
     m.st = m.part + align16((size_t)L * 3 * sizeof(float));
     m.tot = m.st + align16((size_t)S * sizeof(SceneState));
-    m.stage = m.tot + align16((size_t)S * 3 * sizeof(float));
+    m.segb = m.tot + align16((size_t)S * 3 * sizeof(float));
+    m.sseg = m.segb + align16((size_t)(L + 1) * sizeof(int));
+    m.stage = m.sseg + align16((size_t)(S + 1) * sizeof(int));
     m.total = m.stage + (stage ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
     return m;
 }
@@ -304,21 +310,16 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
     if (threadIdx.x == 0 && s_any != nullptr) *s_any = 0;
     __syncthreads();  // slice partials complete, activity flag cleared
     if (warp == 0) {
-        if (first < last) {
-            const int s0 = a.cta_first_scene[blockIdx.x];
-            const int nsc = a.slice_scene[last - 1] - s0 + 1;
-            for (int t = 0; t < nsc; ++t) {
-                const int sc = s0 + t;
-                const int lo = max(a.scene_slice0[sc], first), hi = min(a.scene_slice0[sc + 1], last);
-                for (int k = 0; k < nv; ++k) {
-                    float acc = 0.f;
-                    for (int sl = lo + lane; sl < hi; sl += 32) {
-                        const float v = sm.part[(sl - first) * 3 + k];
-                        acc = is_max ? fmaxf(acc, v) : acc + v;
-                    }
-                    acc = is_max ? warp_max(acc) : warp_sum(acc);
-                    if (lane == 0) buf[(size_t)(a.cta_seg_base[blockIdx.x] + t) * 3 + k] = acc;
+        for (int t = 0; t < sm.nsc; ++t) {
+            const int lo = sm.segb[t], hi = sm.segb[t + 1];
+            for (int k = 0; k < nv; ++k) {
+                float acc = 0.f;
+                for (int sl = lo + lane; sl < hi; sl += 32) {
+                    const float v = sm.part[(sl - first) * 3 + k];
+                    acc = is_max ? fmaxf(acc, v) : acc + v;
                 }
+                acc = is_max ? warp_max(acc) : warp_sum(acc);
+                if (lane == 0) buf[(size_t)(sm.segbase + t) * 3 + k] = acc;
             }
         }
         __syncwarp();
@@ -327,7 +328,7 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (ok && S <= kWarpReducedScenes) {
             for (int sc = 0; sc < S; ++sc) {
-                const int lo = a.scene_seg0[sc], hi = a.scene_seg0[sc + 1];
+                const int lo = sm.sseg[sc], hi = sm.sseg[sc + 1];
                 float acc[3] = {0.f, 0.f, 0.f};
                 for (int g0 = lo + lane; g0 < hi; g0 += 32 * kSegLoadBatch) {
                     float v[kSegLoadBatch][3];
@@ -355,7 +356,7 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
         __syncthreads();
         if (!*s_ok) return false;
         for (int sc = threadIdx.x; sc < S; sc += blockDim.x) {
-            const int lo = a.scene_seg0[sc], hi = a.scene_seg0[sc + 1];
+            const int lo = sm.sseg[sc], hi = sm.sseg[sc + 1];
             for (int k = 0; k < nv; ++k) {
                 float acc = 0.f;
                 for (int g = lo; g < hi; ++g) {
@@ -393,10 +394,22 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     sm.st = reinterpret_cast<SceneState*>(smem_raw + lay.st);
     sm.tot = reinterpret_cast<float*>(smem_raw + lay.tot);
     sm.stage = reinterpret_cast<float4*>(smem_raw + lay.stage);
+    sm.segb = reinterpret_cast<int*>(smem_raw + lay.segb);
+    sm.sseg = reinterpret_cast<int*>(smem_raw + lay.sseg);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int first = blockIdx.x * L;
     const int last = min(first + L, a.nslices);
+    // Launch-constant reduction tables, staged once (the first grid reduction's
+    // CTA barrier orders these writes before their use).
+    {
+        const int s0 = a.cta_first_scene[blockIdx.x];
+        sm.nsc = first < last ? a.slice_scene[last - 1] - s0 + 1 : 0;
+        sm.segbase = a.cta_seg_base[blockIdx.x];
+        for (int t = threadIdx.x; t <= sm.nsc; t += blockDim.x)
+            sm.segb[t] = t == 0 ? first : (t == sm.nsc ? last : a.scene_slice0[s0 + t]);
+        for (int t = threadIdx.x; t <= S; t += blockDim.x) sm.sseg[t] = a.scene_seg0[t];
+    }
     unsigned epoch = 0;
     const float h = a.dt;
 
@@ -657,7 +670,7 @@ cudaError_t pcg_configure(Handle& h) {
         int per_sm = 0;
         for (int attempt = 0; attempt < 2; ++attempt) {
             const SmemLayout lay = smem_layout(L, h.nscenes, stage);
-            if ((lay.st | lay.tot | lay.stage) & 15) return cudaErrorMisalignedAddress;  // float4 sections
+            if ((lay.st | lay.tot | lay.segb | lay.sseg | lay.stage) & 15) return cudaErrorMisalignedAddress;
             if (lay.total > 48 * 1024) {
                 err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
                 if (err != cudaSuccess) return err;
