@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched vs plain measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-beam gradient measurement")
+    p.add_argument("--trace-iterations", action="store_true",
+                   help="print the CG iterations of every PCG launch of the eager warm-up frame to stderr "
+                        "(maps an ncu launch index to its iteration count)")
     return p.parse_args()
 
 
@@ -438,7 +441,17 @@ def run_gb300(args) -> None:
             a, b = b, a
 
     with torch.cuda.stream(stream):
-        frame(s0, s1)  # eager warm-up (first refresh, lazy setup)
+        if args.trace_iterations:
+            a, b = s0, s1
+            solver.refresh_tangent(a.particle_q)
+            for k in range(substeps):
+                solver.step(a, b, None, None, sc.dt)
+                a, b = b, a
+                torch.cuda.synchronize()
+                print(json.dumps({"pcg_launch": k, "iterations": solver.stats()["max_iterations"]}), file=sys.stderr,
+                      flush=True)
+        else:
+            frame(s0, s1)  # eager warm-up (first refresh, lazy setup)
     torch.cuda.synchronize()
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
