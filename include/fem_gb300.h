@@ -149,7 +149,8 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
 #define FEM_TUNE_L2_RESIDENT_BYTES 2 /* matrix bytes loaded evict_last (kept in L2 across iterations); -1 = 60% of L2; default 0 */
 #define FEM_TUNE_RESIDENT_SLICES 3   /* read-only: resulting number of L2-resident 32-row slices */
 #define FEM_TUNE_GRID 4              /* read-only: cooperative grid size */
-#define FEM_TUNE_CTA_THREADS 5       /* threads per PCG CTA: 256, 512 or 1024 (default 1024) */
+#define FEM_TUNE_CTA_THREADS 5       /* threads per PCG CTA: 256, 512, 1024, or 0 = automatic (default): 1024 when there are
+                                        at least 32 slices per SM, else 256; the getter returns the size in use */
 #define FEM_TUNE_GRID_CAP 6          /* upper bound on the PCG grid (0 = as many CTAs as fit, the default) */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);

@@ -703,8 +703,8 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
         if (value < -1) return set_error(FEM_ERR_BAD_ARG, "resident bytes must be >= -1");
         h.l2_resident_bytes = value;
     } else if (key == FEM_TUNE_CTA_THREADS) {
-        if (value != 256 && value != 512 && value != 1024)
-            return set_error(FEM_ERR_BAD_ARG, "CTA threads must be 256, 512 or 1024");
+        if (value != 0 && value != 256 && value != 512 && value != 1024)
+            return set_error(FEM_ERR_BAD_ARG, "CTA threads must be 0 (automatic), 256, 512 or 1024");
         h.pcg_threads = (int)value;
     } else if (key == FEM_TUNE_GRID_CAP) {
         if (value < 0 || value > (1 << 20)) return set_error(FEM_ERR_BAD_ARG, "grid cap must be in [0, 2^20]");
@@ -725,7 +725,7 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_L2_RESIDENT_BYTES: *value = h.l2_resident_bytes; return FEM_OK;
         case FEM_TUNE_RESIDENT_SLICES: *value = h.resident_slices; return FEM_OK;
         case FEM_TUNE_GRID: *value = h.grid; return FEM_OK;
-        case FEM_TUNE_CTA_THREADS: *value = h.pcg_threads; return FEM_OK;
+        case FEM_TUNE_CTA_THREADS: *value = h.pcg_threads_used; return FEM_OK;
         case FEM_TUNE_GRID_CAP: *value = h.grid_cap; return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }

@@ -117,7 +117,8 @@ struct Handle {
     long long wait_limit_ns = 2000000000LL;
     int spmv_unroll = 4;          // block columns in flight per thread in the PCG SpMV (1, 2 or 4)
     int64_t l2_resident_bytes = 0;   // matrix bytes loaded evict_last (-1: 60% of L2); measured slower, so off
-    int pcg_threads = 1024;          // threads per PCG CTA (256, 512 or 1024): one CTA per SM by default
+    int pcg_threads = 0;             // threads per PCG CTA (256, 512, 1024; 0 = chosen from the problem size)
+    int pcg_threads_used = 0;        // the CTA size of the current configuration
     int grid_cap = 0;                // upper bound on the PCG grid (0: co-residency limit only)
     int resident_slices = 0;
     bool tangent_prepared = false;

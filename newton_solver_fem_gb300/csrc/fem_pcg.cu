@@ -659,7 +659,11 @@ cudaError_t pcg_configure(Handle& h) {
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return cudaErrorNotSupported;
     PcgKernel kern = pcg_kernel_for(h.spmv_unroll);
-    const int threads = h.pcg_threads;
+    // Automatic CTA size: one 1024-thread CTA per SM once every SM has a slice
+    // per warp (fewer CTAs make the grid reductions cheaper); small systems keep
+    // 256-thread CTAs, whose CTA barriers are cheaper than a wide CTA's.
+    const int threads = h.pcg_threads > 0 ? h.pcg_threads : (h.nslices >= 32 * sms ? 1024 : 256);
+    h.pcg_threads_used = threads;
     const int warps_per_cta = threads / 32;
     int grid = (h.nslices + warps_per_cta - 1) / warps_per_cta;
     if (grid < 1) grid = 1;
@@ -748,7 +752,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     if (err != cudaSuccess) return err;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(h.grid);
-    cfg.blockDim = dim3(h.pcg_threads);
+    cfg.blockDim = dim3(h.pcg_threads_used);
     cfg.dynamicSmemBytes = h.pcg_smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
