@@ -203,6 +203,44 @@ int fem_force_vjp(FemHandle* handle, const float* q, const float* v, const float
  * plus the spring-damping term (implicit_predictor.py:9-41). */
 int fem_predictor_vjp(FemHandle* handle, const float* rhs_bar, float dt, float* v_bar, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Prepared affine step.  Replaces the reference's PreparedFEMStep
+ * (prepared_step.py:64-302; SolverFEM.prepare_step, solver.py:483-500).  The
+ * caller owns the workspace: seven device arrays, [N,3] float32 except
+ * diagonal ([N,3,3]); the functions read and write only those and the
+ * handle's matrix, preconditioner and scratch.
+ * ------------------------------------------------------------------------- */
+typedef struct FemPreparedWs {
+    float* q;          /* prepared positions (fixed nodes restored) */
+    float* v;          /* prepared velocities (fixed nodes zero) */
+    float* impulse;    /* h * sum of the force terms (+ h * the load passed to fem_prepare) */
+    float* predictor;  /* sum_j A_ij (v_j - v_i) */
+    float* base_rhs;   /* fem_prepared_rhs with no extra load */
+    float* increment;  /* the workspace's velocity increment (warm start of fem_prepared_solve) */
+    float* diagonal;   /* diagonal blocks of PAP + I - P (identity at fixed nodes) */
+} FemPreparedWs;
+
+/* prepared_step.py:126-183: copies q_in, v_in (unchanged), evaluates the force terms once. */
+int fem_prepare(FemHandle* h, const FemPreparedWs* ws, const float* q_in, const float* v_in,
+                const float* external_forces_or_null, const float* activations_or_null, const float* gravity,
+                float dt, void* stream);
+/* prepared_step.py:185-213: out = impulse + dt*ext - predictor + spring damping, zero at fixed nodes.
+ * out must not alias ext. */
+int fem_prepared_rhs(FemHandle* h, const FemPreparedWs* ws, const float* external_forces_or_null, float dt, float* out,
+                     void* stream);
+/* prepared_step.py:215-224: y = (PAP + I - P) x; x and y distinct. */
+int fem_apply_operator(FemHandle* h, const float* x, float* y, void* stream);
+/* prepared_step.py:226-235: z = M r (block-Jacobi, or point-Jacobi with preconditioner=1); r and z distinct. */
+int fem_apply_preconditioner(FemHandle* h, const float* r, float* z, void* stream);
+/* prepared_step.py:252-275: normalised PCG for (PAP + I - P) dv = rhs from ws->increment; the result
+ * replaces ws->increment.  Statistics through fem_get_stats. */
+int fem_prepared_solve(FemHandle* h, const FemPreparedWs* ws, const float* rhs, float tolerance, int32_t maxiter,
+                       float dt, void* stream);
+/* prepared_step.py:277-302: v_out = ws->v + dv, q_out = ws->q + dt * v_out, fixed nodes restored;
+ * the outputs must not be the workspace arrays. */
+int fem_prepared_reconstruct(FemHandle* h, const FemPreparedWs* ws, const float* dv, float dt, float* q_out,
+                             float* v_out, void* stream);
+
 /* Block-Jacobi PCG on a caller-supplied BSR matrix that allocates no device
  * memory.  No counterpart in the reference: it exists for callers that cannot
  * call cudaMalloc at solve time (a host application that owns all device

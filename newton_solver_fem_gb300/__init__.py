@@ -7,6 +7,7 @@ The numerical work runs in ``libfemgb300.so`` (``include/fem_gb300.h``).
 """
 
 from .builder import FEMBuilder, LinearFEMData, Model, State, Control, hex_gauss_data, model_from_arrays
+from .prepared_step import PreparedFEMStep
 from .solver import BsrMatrix, SolverFEM, SolverLinearFEM
 
 __all__ = [
@@ -15,6 +16,7 @@ __all__ = [
     "FEMBuilder",
     "LinearFEMData",
     "Model",
+    "PreparedFEMStep",
     "SolverFEM",
     "SolverLinearFEM",
     "State",

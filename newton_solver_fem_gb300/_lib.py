@@ -98,6 +98,10 @@ class FemStats(ctypes.Structure):
     ]
 
 
+class FemPreparedWs(ctypes.Structure):
+    _fields_ = [(name, _p) for name in ("q", "v", "impulse", "predictor", "base_rhs", "increment", "diagonal")]
+
+
 # (name, restype, argtypes) for every symbol declared in include/fem_gb300.h
 SIGNATURES = [
     ("fem_create", _i32, [ctypes.POINTER(FemDesc), ctypes.POINTER(_p)]),
@@ -126,6 +130,12 @@ SIGNATURES = [
     ("fem_solve", _i32, [_p, _p, _p, _f, _i32, _p]),
     ("fem_force_vjp", _i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     ("fem_predictor_vjp", _i32, [_p, _p, _f, _p, _p]),
+    ("fem_prepare", _i32, [_p, ctypes.POINTER(FemPreparedWs), _p, _p, _p, _p, _p, _f, _p]),
+    ("fem_prepared_rhs", _i32, [_p, ctypes.POINTER(FemPreparedWs), _p, _f, _p, _p]),
+    ("fem_apply_operator", _i32, [_p, _p, _p, _p]),
+    ("fem_apply_preconditioner", _i32, [_p, _p, _p, _p]),
+    ("fem_prepared_solve", _i32, [_p, ctypes.POINTER(FemPreparedWs), _p, _f, _i32, _f, _p]),
+    ("fem_prepared_reconstruct", _i32, [_p, ctypes.POINTER(FemPreparedWs), _p, _f, _p, _p, _p]),
     ("fem_pcg_solve_noalloc", _i32, [_p, _p, _p, _p, _p, _i32, _f, _i32, _p, _p]),
     ("fem_status_string", ctypes.c_char_p, [_i32]),
     ("fem_version", ctypes.c_char_p, []),

@@ -98,7 +98,8 @@ struct PcgArgs {
     long long limit_ns;  // give up a barrier wait after this many ns
     int write_state;  // 1: integrate state (step); 0: solve only
     int resident_slices;  // slices [0, resident_slices) are loaded with the L2 evict_last policy
-    const float* solve_rhs;  // non-null: solve A x = solve_rhs from x0 = 0 (no predictor), x -> dv
+    const float* solve_rhs;  // non-null: solve A x = solve_rhs (no predictor), x -> dv
+    int solve_warm;          // solve mode: start from the packed x (else from zero)
 };
 
 struct Handle {
@@ -227,9 +228,10 @@ cudaError_t launch_export_triplets(Handle& h, float* values, cudaStream_t s);
 cudaError_t pcg_configure(Handle& h);
 // Step mode (solve_rhs == nullptr): predictor, normalised PCG from the dv warm start, integration.
 // Solve mode: A x = solve_rhs from zero (projected at fixed rows), x written to x_out.
+// Solve mode with solve_warm: start from the packed h.x instead of zero (normalised like step mode).
 cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s,
                        const float* solve_rhs = nullptr, float* x_out = nullptr, float tol = -1.0f,
-                       int maxiter = -1);
+                       int maxiter = -1, bool solve_warm = false);
 
 }  // namespace fem
 

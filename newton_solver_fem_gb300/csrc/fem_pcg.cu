@@ -422,9 +422,15 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             unsigned info = a.row_info[row];
             float3 rhs = f3(0.f, 0.f, 0.f), u = f3(0.f, 0.f, 0.f);
             if (a.solve_rhs != nullptr) {
-                // solve mode: A x = b from x0 = 0, b given (projected at fixed rows)
+                // solve mode: A x = b, b given (projected at fixed rows), from x0 = 0 or the packed x
                 if (!(info & kFixedBit)) rhs = load3(a.solve_rhs, row);
                 u = rhs;
+                if (a.solve_warm && !(info & kFixedBit)) {
+                    float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
+                    row_predictor<U>(a, a.slice_ptr[sl], (int)(info & ~kFixedBit), lane, xyz(a.v4[row]), cv, ax,
+                                     sl < a.resident_slices ? pol_last : pol_first);
+                    u = rhs - ax;
+                }
             } else {
                 if (!(info & kFixedBit)) {
                     int len = (int)(info & ~kFixedBit);
@@ -470,7 +476,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             float sc = st.scale;
             float3 x = f3(0.f, 0.f, 0.f), r = f3(0.f, 0.f, 0.f);
             if (!st.zero) {
-                if (a.solve_rhs == nullptr) x = xyz(a.x[row]) * sc;  // solve mode starts from zero
+                if (a.solve_rhs == nullptr || a.solve_warm) x = xyz(a.x[row]) * sc;  // else solve mode starts from zero
                 r = xyz(a.r[row]) * sc;
             }
             float3 b;
@@ -700,7 +706,7 @@ cudaError_t pcg_configure(Handle& h) {
 }
 
 cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s,
-                       const float* solve_rhs, float* x_out, float tol, int maxiter) {
+                       const float* solve_rhs, float* x_out, float tol, int maxiter, bool solve_warm) {
     PcgArgs a;
     a.valA = h.valA;
     a.valB = h.valB;
@@ -748,6 +754,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.write_state = write_state;
     a.resident_slices = h.resident_slices;
     a.solve_rhs = solve_rhs;
+    a.solve_warm = solve_warm ? 1 : 0;
     cudaError_t err = cudaMemsetAsync(h.barrier, 0, sizeof(unsigned), s);
     if (err != cudaSuccess) return err;
     cudaLaunchConfig_t cfg = {};

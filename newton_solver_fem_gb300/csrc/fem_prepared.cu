@@ -1,0 +1,291 @@
+// Prepared affine step: the reference's PreparedFEMStep (prepared_step.py:64-302)
+// over the handle's assembled matrix.
+//
+//   fem_prepare              copy q, v (fixed nodes restored in the copy), evaluate the
+//                            force terms once: impulse = h sum f (+ h ext), predictor
+//                            sum_j A_ij (v_j - v_i), diagonal blocks of PAP + I - P and
+//                            base_rhs = rhs(no extra load)              (lines 126-183)
+//   fem_prepared_rhs         impulse + h ext - predictor + spring damping, projected
+//                                                                        (lines 185-213)
+//   fem_apply_operator       (PAP + I - P) x                             (lines 215-224)
+//   fem_apply_preconditioner block-Jacobi M r                            (lines 226-235)
+//   fem_prepared_solve       normalised PCG from the workspace's increment (lines 252-275)
+//   fem_prepared_reconstruct v' = v + dv, q' = q + h v', fixed restored   (lines 277-302)
+//
+// The workspace arrays belong to the caller (FemPreparedWs), so every entry
+// point is stateless with respect to it and the pointers stay stable for
+// CUDA graphs.
+#include "fem_internal.cuh"
+#include "fem_math.cuh"
+
+namespace fem {
+namespace {
+
+__device__ __forceinline__ float3 ld3(const float* p, int i) { return f3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+__device__ __forceinline__ void st3(float* p, int i, float3 v) {
+    p[3 * i] = v.x;
+    p[3 * i + 1] = v.y;
+    p[3 * i + 2] = v.z;
+}
+__device__ __forceinline__ float3 block_mul(float4 a, float4 b, float c, float3 p) {
+    return f3(a.x * p.x + a.y * p.y + a.z * p.z, a.w * p.x + b.x * p.y + b.y * p.z, b.z * p.x + b.w * p.y + c * p.z);
+}
+
+// Workspace state: fixed nodes take their rest position and zero velocity
+// (fixed_particles.py:11-21), applied to the copy only.
+__global__ void prepare_state_kernel(int P, const float* __restrict__ q_in, const float* __restrict__ v_in,
+                                     const unsigned char* __restrict__ fixed, const float* __restrict__ rest,
+                                     float* __restrict__ pq, float* __restrict__ pv, float4* __restrict__ q4,
+                                     float4* __restrict__ v4) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const bool fx = fixed[i] != 0;
+    const float3 q = fx ? ld3(rest, i) : ld3(q_in, i);
+    const float3 v = fx ? f3(0.f, 0.f, 0.f) : ld3(v_in, i);
+    st3(pq, i, q);
+    st3(pv, i, v);
+    q4[i] = f4(q);
+    v4[i] = f4(v);
+}
+
+// One warp per SELL slice, lane per row: predictor sum_k A_ik (v_k - v_i) and
+// the diagonal block of PAP + I - P (A_ii, identity at fixed rows).
+__global__ void predictor_diag_kernel(int nslices, const int* __restrict__ slice_ptr, const int2* __restrict__ meta,
+                                      const unsigned* __restrict__ row_info, const float4* __restrict__ valA,
+                                      const float4* __restrict__ valB, const float* __restrict__ valC,
+                                      const int* __restrict__ scol, const float4* __restrict__ v4,
+                                      float* __restrict__ pred, float* __restrict__ diag) {
+    const int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (sl >= nslices) return;
+    const int2 m = meta[sl];
+    if (lane >= m.y) return;
+    const int row = m.x + lane;
+    const unsigned info = row_info[row];
+    const int len = (int)(info & ~kFixedBit);
+    const float3 vi = xyz(v4[row]);
+    float3 acc = f3(0.f, 0.f, 0.f);
+    float d[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int k = 0; k < len; ++k) {
+        const size_t e = (size_t)(slice_ptr[sl] + k) * kSlice + lane;
+        const float4 a = valA[e], b = valB[e];
+        const float c = valC[e];
+        const int j = scol[e];
+        acc = acc + block_mul(a, b, c, xyz(v4[j]) - vi);
+        if (j == row) {
+            d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w;
+            d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w; d[8] = c;
+        }
+    }
+    if (info & kFixedBit) {
+        for (int k = 0; k < 9; ++k) d[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+    }
+    st3(pred, row, acc);
+    for (int k = 0; k < 9; ++k) diag[9 * (size_t)row + k] = d[k];
+}
+
+// out = impulse + h ext - predictor, then the spring damping restore
+// (implicit_predictor.py:28-41), then zero at fixed rows (fixed_particles.py:159-160).
+__global__ void prepared_rhs_kernel(int P, const float* __restrict__ impulse, const float* __restrict__ ext, float dt,
+                                    const float* __restrict__ pred, const int* __restrict__ sptr,
+                                    const int* __restrict__ sent, const int* __restrict__ sidx,
+                                    const float* __restrict__ skd, const float* __restrict__ pv,
+                                    const unsigned char* __restrict__ fixed, float* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    if (fixed[i]) {
+        st3(out, i, f3(0.f, 0.f, 0.f));
+        return;
+    }
+    float3 r = ld3(impulse, i);
+    if (ext != nullptr) r = r + ld3(ext, i) * dt;
+    r = r - ld3(pred, i);
+    for (int e = sptr[i]; e < sptr[i + 1]; ++e) {
+        const int ent = sent[e], s = ent >> 1;
+        const int ia = sidx[2 * s], ib = sidx[2 * s + 1];
+        if (ia < 0 || ib < 0) continue;
+        const float3 corr = (ld3(pv, ia) - ld3(pv, ib)) * (dt * skd[s]);
+        r = (ent & 1) ? r - corr : r + corr;
+    }
+    st3(out, i, r);
+}
+
+// y = (PAP + I - P) x: fixed rows return x_i; free rows skip fixed columns.
+__global__ void apply_operator_kernel(int nslices, const int* __restrict__ slice_ptr, const int2* __restrict__ meta,
+                                      const unsigned* __restrict__ row_info, const float4* __restrict__ valA,
+                                      const float4* __restrict__ valB, const float* __restrict__ valC,
+                                      const int* __restrict__ scol, const float* __restrict__ x,
+                                      float* __restrict__ y) {
+    const int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (sl >= nslices) return;
+    const int2 m = meta[sl];
+    if (lane >= m.y) return;
+    const int row = m.x + lane;
+    const unsigned info = row_info[row];
+    if (info & kFixedBit) {
+        st3(y, row, ld3(x, row));
+        return;
+    }
+    const int len = (int)(info & ~kFixedBit);
+    float3 acc = f3(0.f, 0.f, 0.f);
+    for (int k = 0; k < len; ++k) {
+        const size_t e = (size_t)(slice_ptr[sl] + k) * kSlice + lane;
+        const int j = scol[e];
+        if (row_info[j] & kFixedBit) continue;
+        acc = acc + block_mul(valA[e], valB[e], valC[e], ld3(x, j));
+    }
+    st3(y, row, acc);
+}
+
+__global__ void apply_preconditioner_kernel(int P, const float* __restrict__ minv, const float* __restrict__ r,
+                                            float* __restrict__ z) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const float* b = minv + 9 * (size_t)i;
+    const float3 v = ld3(r, i);
+    st3(z, i, f3(b[0] * v.x + b[1] * v.y + b[2] * v.z, b[3] * v.x + b[4] * v.y + b[5] * v.z,
+                 b[6] * v.x + b[7] * v.y + b[8] * v.z));
+}
+
+__global__ void pack_warm_start_kernel(int P, const float* __restrict__ dv, const unsigned char* __restrict__ fixed,
+                                       float4* __restrict__ x4) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    x4[i] = fixed[i] ? make_float4(0.f, 0.f, 0.f, 0.f) : f4(ld3(dv, i));
+}
+
+// kernels.py:115-128 (update_state), then the fixed restore.
+__global__ void reconstruct_kernel(int P, const float* __restrict__ dv, const float* __restrict__ pq,
+                                   const float* __restrict__ pv, const unsigned char* __restrict__ fixed,
+                                   const float* __restrict__ rest, float dt, float* __restrict__ q_out,
+                                   float* __restrict__ v_out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    float3 v = ld3(pv, i) + ld3(dv, i);
+    float3 q = ld3(pq, i) + v * dt;
+    if (fixed[i]) {
+        q = ld3(rest, i);
+        v = f3(0.f, 0.f, 0.f);
+    }
+    st3(q_out, i, q);
+    st3(v_out, i, v);
+}
+
+inline int blocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+bool ws_ok(const FemPreparedWs* w) {
+    return w && w->q && w->v && w->impulse && w->predictor && w->base_rhs && w->increment && w->diagonal;
+}
+
+struct Guard {
+    int prev = -1;
+    explicit Guard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~Guard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int status_of(cudaError_t e) { return e == cudaSuccess ? FEM_OK : FEM_ERR_CUDA; }
+
+cudaError_t launch_rhs(Handle& h, const FemPreparedWs* w, const float* ext, float dt, float* out, cudaStream_t s) {
+    prepared_rhs_kernel<<<blocks(h.P, 256), 256, 0, s>>>(h.P, w->impulse, ext, dt, w->predictor, h.node_spring_ptr,
+                                                         h.node_spring_ent, h.spring_idx, h.spring_kd, w->v,
+                                                         h.fixed_mask, out);
+    return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace fem
+
+using fem::Handle;
+
+extern "C" {
+
+int fem_prepare(FemHandle* H, const FemPreparedWs* w, const float* q_in, const float* v_in,
+                const float* external_forces, const float* activations, const float* gravity, float dt,
+                void* stream) {
+    if (H == nullptr || !fem::ws_ok(w) || q_in == nullptr || v_in == nullptr) return FEM_ERR_BAD_ARG;
+    Handle& h = H->h;
+    if (!(dt > 0.0f)) return FEM_ERR_BAD_ARG;
+    if (h.enable_act && h.T > 0 && activations == nullptr) return FEM_ERR_BAD_ARG;
+    if (h.P == 0) return FEM_OK;
+    fem::Guard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    fem::prepare_state_kernel<<<fem::blocks(h.P, 256), 256, 0, s>>>(h.P, q_in, v_in, h.fixed_mask, h.rest, w->q,
+                                                                      w->v, h.q4, h.v4);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = fem::launch_element_forces(h, activations, s);
+    if (err == cudaSuccess)
+        err = fem::launch_node_forces(h, external_forces, gravity, dt, 0x3f, true, w->impulse, s);
+    if (err == cudaSuccess && h.nslices > 0) {
+        fem::predictor_diag_kernel<<<fem::blocks((int64_t)h.nslices * 32, 256), 256, 0, s>>>(
+            h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.scol, h.v4, w->predictor,
+            w->diagonal);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = fem::launch_rhs(h, w, nullptr, dt, w->base_rhs, s);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(w->increment, h.dv, sizeof(float) * 3 * (size_t)h.P, cudaMemcpyDeviceToDevice, s);
+    return fem::status_of(err);
+}
+
+int fem_prepared_rhs(FemHandle* H, const FemPreparedWs* w, const float* external_forces, float dt, float* out,
+                     void* stream) {
+    if (H == nullptr || !fem::ws_ok(w) || out == nullptr || out == external_forces) return FEM_ERR_BAD_ARG;
+    Handle& h = H->h;
+    if (h.P == 0) return FEM_OK;
+    fem::Guard g(H->device);
+    return fem::status_of(fem::launch_rhs(h, w, external_forces, dt, out, (cudaStream_t)stream));
+}
+
+int fem_apply_operator(FemHandle* H, const float* x, float* y, void* stream) {
+    if (H == nullptr || x == nullptr || y == nullptr || x == y) return FEM_ERR_BAD_ARG;
+    Handle& h = H->h;
+    if (h.P == 0 || h.nslices == 0) return FEM_OK;
+    fem::Guard g(H->device);
+    fem::apply_operator_kernel<<<fem::blocks((int64_t)h.nslices * 32, 256), 256, 0, (cudaStream_t)stream>>>(
+        h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.scol, x, y);
+    return fem::status_of(cudaGetLastError());
+}
+
+int fem_apply_preconditioner(FemHandle* H, const float* r, float* z, void* stream) {
+    if (H == nullptr || r == nullptr || z == nullptr || r == z) return FEM_ERR_BAD_ARG;
+    Handle& h = H->h;
+    if (h.P == 0) return FEM_OK;
+    fem::Guard g(H->device);
+    fem::apply_preconditioner_kernel<<<fem::blocks(h.P, 256), 256, 0, (cudaStream_t)stream>>>(h.P, h.minv, r, z);
+    return fem::status_of(cudaGetLastError());
+}
+
+int fem_prepared_solve(FemHandle* H, const FemPreparedWs* w, const float* rhs, float tolerance, int32_t maxiter,
+                       float dt, void* stream) {
+    if (H == nullptr || !fem::ws_ok(w) || rhs == nullptr) return FEM_ERR_BAD_ARG;
+    if (!(tolerance > 0.0f) || maxiter < 0) return FEM_ERR_BAD_ARG;
+    Handle& h = H->h;
+    if (h.P == 0) return FEM_OK;
+    fem::Guard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    fem::pack_warm_start_kernel<<<fem::blocks(h.P, 256), 256, 0, s>>>(h.P, w->increment, h.fixed_mask, h.x);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess)
+        err = fem::launch_pcg(h, dt, 0, nullptr, nullptr, nullptr, s, rhs, w->increment, tolerance, maxiter,
+                              /*solve_warm=*/true);
+    return fem::status_of(err);
+}
+
+int fem_prepared_reconstruct(FemHandle* H, const FemPreparedWs* w, const float* dv, float dt, float* q_out,
+                             float* v_out, void* stream) {
+    if (H == nullptr || !fem::ws_ok(w) || dv == nullptr || q_out == nullptr || v_out == nullptr) return FEM_ERR_BAD_ARG;
+    if (q_out == w->q || v_out == w->v) return FEM_ERR_BAD_ARG;
+    Handle& h = H->h;
+    if (h.P == 0) return FEM_OK;
+    fem::Guard g(H->device);
+    fem::reconstruct_kernel<<<fem::blocks(h.P, 256), 256, 0, (cudaStream_t)stream>>>(
+        h.P, dv, w->q, w->v, h.fixed_mask, h.rest, dt, q_out, v_out);
+    return fem::status_of(cudaGetLastError());
+}
+
+}  // extern "C"

@@ -141,6 +141,8 @@ class SolverFEM:
         model.particle_kd = float(self_contact_kd)
         self._lib = _lib.load()
         self._handle = ctypes.c_void_p()
+        self._revision = 0  # matrix revision (refresh_tangent, rebuild_element_blocks, model changes)
+        self._prepared_step = None
         P = model.particle_count
         # persistent velocity increment, owned here so it is visible as a tensor
         self.dv = torch.zeros((P, 3), dtype=torch.float32, device=self.device)
@@ -274,10 +276,7 @@ class SolverFEM:
                         ("state_out.particle_q", state_out.particle_q),
                         ("state_out.particle_qd", state_out.particle_qd), ("state_in.particle_f", state_in.particle_f)):
             _f32(t, (P, 3), name, dev)
-        act = None
-        if self.enable_tet_activations and self.model.tet_count:
-            act = control.tet_activations if control is not None else self.model.tet_activations
-            _f32(act, (self.model.tet_count,), "tet_activations", dev)
+        act = self._activations(control)
         code = self._lib.fem_step(
             self._handle, state_in.particle_q.data_ptr(), state_in.particle_qd.data_ptr(),
             state_out.particle_q.data_ptr(), state_out.particle_qd.data_ptr(), state_in.particle_f.data_ptr(),
@@ -287,6 +286,30 @@ class SolverFEM:
             stats = self.stats()
             self.last_cg_iters = stats["max_iterations"]
         return state_out
+
+    def _activations(self, control):
+        """The per-tet activations the force kernels read (None unless enabled)."""
+        if not (self.enable_tet_activations and self.model.tet_count):
+            return None
+        act = control.tet_activations if control is not None else self.model.tet_activations
+        _f32(act, (self.model.tet_count,), "tet_activations", self.device)
+        return act
+
+    def prepare_step(self, state_in, control, contacts, dt, *, external_forces=None):
+        """Prepare reusable affine mechanics without integrating (reference ``solver.py:483-500``).
+
+        Returns the solver's persistent :class:`PreparedFEMStep` with the
+        constrained operator, the preconditioner, the base impulse and trial
+        reconstruction.  The caller owns tangent refresh and must prepare again
+        for every new accepted state, control or matrix revision.
+        """
+        from .prepared_step import PreparedFEMStep
+
+        if torch.cuda.is_current_stream_capturing():
+            raise RuntimeError("Prepare FEM mechanics before CUDA graph capture")
+        if getattr(self, "_prepared_step", None) is None:
+            self._prepared_step = PreparedFEMStep(self)
+        return self._prepared_step.prepare(state_in, control, contacts, dt, external_forces)
 
     def stats(self) -> dict:
         """Synchronise and return the last solve's statistics (raises on a device timeout / NaN)."""
@@ -322,12 +345,14 @@ class SolverFEM:
         _lib.check(self._lib.fem_refresh_tangent(self._handle, particle_q.data_ptr(), dt, self._stream()),
                    "refresh_tangent")
         self.dt = dt
+        self._revision += 1  # a new matrix revision invalidates prepared steps (solver.py:466-471)
 
     def rebuild_element_blocks(self, particle_q: torch.Tensor, dt: float, *, update_preconditioner=True) -> None:
         """Reassemble the Tet4/Hex8 blocks at particle_q and dt (the preconditioner refreshes in place)."""
         _f32(particle_q, (self.model.particle_count, 3), "particle_q", self.device)
         _lib.check(self._lib.fem_rebuild_element_blocks(self._handle, particle_q.data_ptr(), float(dt),
                                                         self._stream()), "rebuild_element_blocks")
+        self._revision += 1
 
     def refresh_preconditioner(self) -> None:
         _lib.check(self._lib.fem_refresh_preconditioner(self._handle, self._stream()), "refresh_preconditioner")
@@ -338,6 +363,7 @@ class SolverFEM:
 
     def notify_model_changed(self, flags) -> None:
         """Gravity is read live from ``model.gravity``; topology edits need a new solver."""
+        self._revision += 1
 
     # ------------------------------------------------------------------ matrix views
     def matrix_info(self) -> dict:

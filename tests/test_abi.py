@@ -42,11 +42,13 @@ def test_every_declared_symbol_is_exported_and_bound(library):
 
 
 def test_ctypes_struct_layout_matches_c(tmp_path):
-    """sizeof/offsetof of FemDesc and FemStats as gcc lays them out equal the ctypes mirrors."""
+    """sizeof/offsetof of FemDesc, FemStats and FemPreparedWs as gcc lays them out equal the ctypes mirrors."""
     fields = [name for name, _ in _lib.FemDesc._fields_]
+    ws_fields = [name for name, _ in _lib.FemPreparedWs._fields_]
     src = tmp_path / "layout.c"
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {",
-             'printf("%zu %zu\\n", sizeof(FemDesc), sizeof(FemStats));']
+             'printf("%zu %zu %zu\\n", sizeof(FemDesc), sizeof(FemStats), sizeof(FemPreparedWs));']
+    lines += [f'printf("%zu\\n", offsetof(FemPreparedWs, {f}));' for f in ws_fields]
     lines += [f'printf("%zu\\n", offsetof(FemDesc, {f}));' for f in fields]
     lines += ["return 0; }"]
     src.write_text("\n".join(lines))
@@ -55,7 +57,10 @@ def test_ctypes_struct_layout_matches_c(tmp_path):
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     assert int(out[0]) == ctypes.sizeof(_lib.FemDesc)
     assert int(out[1]) == ctypes.sizeof(_lib.FemStats)
-    for f, off in zip(fields, out[2:]):
+    assert int(out[2]) == ctypes.sizeof(_lib.FemPreparedWs)
+    for f, off in zip(ws_fields, out[3:3 + len(ws_fields)]):
+        assert getattr(_lib.FemPreparedWs, f).offset == int(off), f
+    for f, off in zip(fields, out[3 + len(ws_fields):]):
         assert getattr(_lib.FemDesc, f).offset == int(off), f
 
 
