@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched vs plain measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-beam gradient measurement")
+    p.add_argument("--no-tet", action="store_true", help="skip the jittered Tet4 48^3 measurement")
     p.add_argument("--trace-iterations", action="store_true",
                    help="print the CG iterations of every PCG launch of the eager warm-up frame to stderr "
                         "(maps an ncu launch index to its iteration count)")
@@ -315,6 +316,57 @@ def batched_measurement(device: str, steps: int, warmup: int) -> dict:
     return out
 
 
+def tet_measurement(device: str, steps: int, warmup: int) -> dict:
+    """Jittered Tet4 48^3 block (663,552 tets, 795,024 edge springs, ground): frames as captured graphs."""
+    import torch
+
+    from newton_solver_fem_gb300 import SolverFEM, model_from_arrays, scenes
+
+    sc = scenes.tet_jittered_48()
+    model = model_from_arrays(sc.x, sc.mass, tets=sc.tets, tet_materials=sc.tet_materials, springs=sc.springs,
+                              spring_ke=sc.spring_ke, spring_kd=sc.spring_kd, velocity=sc.velocity,
+                              radius=sc.radius, gravity=sc.gravity, device=device)
+    ke, kd, kf, mu = sc.ground
+    solver = SolverFEM(model, dt=sc.dt, solver_type="cg", preconditioner_type="block_diag",
+                       linear_solver_maxiter=sc.maxiter, linear_solver_tolerance=sc.tolerance, self_contact_ke=0.0,
+                       ground_plane=sc.ground_plane, ground_ke=ke, ground_kd=kd, ground_kf=kf, ground_mu=mu)
+    P = model.particle_count
+    a, b = model.state(), model.state()
+    stream = torch.cuda.Stream(device)
+
+    def frame():
+        x, y = a, b
+        solver.refresh_tangent(x.particle_q)
+        for _ in range(sc.substeps):
+            solver.step(x, y, None, None, sc.dt)
+            x, y = y, x
+
+    with torch.cuda.stream(stream):
+        frame()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            frame()
+    for _ in range(max(3, warmup)):
+        graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(steps):
+            graph.replay()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    st = solver.stats()
+    del graph
+    return {"workload": "tet4_jittered_48^3 (117,649 nodes, 663,552 tets, 795,024 springs, ground), "
+                        "10 substeps/frame, 50 CG at tol 1e-2",
+            "ms_per_frame": ms, "value": 3 * P * sc.substeps / (ms / 1e3), "unit": UNIT,
+            "cg_iterations_last_substep": st["max_iterations"], "finite": bool(torch.isfinite(a.particle_q).all())}
+
+
 def adjoint_measurement(device: str, repeats: int) -> dict:
     """Differentiable beam (16x4x4 cubes, 1,536 tets, 120 frames x 4 substeps, 30 CG): gradient vs plain rollout.
 
@@ -411,6 +463,63 @@ def adjoint_measurement(device: str, repeats: int) -> dict:
     }
 
 
+def batched_adjoint_measurement(device: str, frames: int = 60) -> dict:
+    """256 uneven scenes: a 60-frame rollout and its batched adjoint pass (checkpoints every frame).
+
+    The matrix is assembled once at rest and held fixed (the differentiable
+    contract); solves use the scenes' tolerance (1e-2, at most 50 CG).  The
+    loss is the mean height of all nodes at the end; gradients are taken with
+    respect to the initial velocities.  The plain rollout steps the same 600
+    substeps through ``SolverFEM.step``.
+    """
+    import torch
+
+    from newton_solver_fem_gb300 import scenes
+    from newton_solver_fem_gb300.adjoint import DifferentiableSolver, checkpointed_gradient
+
+    sc = scenes.batched_scenes()
+    model, solver = scene_solver(sc, device, sc.scene_offsets)
+    P = model.particle_count
+    steps = frames * sc.substeps
+    solver.refresh_tangent(model.particle_q.clone())
+    diff = DifferentiableSolver(solver, tolerance=sc.tolerance, maxiter=sc.maxiter)
+    q0, v0 = model.particle_q.clone(), model.particle_qd.clone()
+
+    def step(q, v, k):
+        return diff.step(q, v, sc.dt)
+
+    def loss_fn(q, v):
+        return q[:, 2].mean()
+
+    def plain():
+        a, b = model.state(), model.state()
+        a.particle_q.copy_(q0)
+        a.particle_qd.copy_(v0)
+        for _ in range(steps):
+            solver.step(a, b, None, None, sc.dt)
+            a, b = b, a
+        return a
+
+    def wall(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t, out
+
+    wall(plain)  # warm-up
+    t_plain, _ = wall(plain)
+    t_grad, out = wall(lambda: checkpointed_gradient(step, q0, v0, steps, sc.substeps, loss_fn))
+    loss, _, dv0, _ = out
+    return {"workload": "256 scenes (1.56M nodes), 60 frames x 10 substeps, tol 1e-2 / 50 CG, frozen A, "
+                        "checkpoints every frame, loss = mean node height, gradient wrt v0",
+            "plain_rollout_ms": 1e3 * t_plain, "gradient_ms": 1e3 * t_grad,
+            "gradient_over_plain": t_grad / t_plain, "plain_value": 3 * P * steps / t_plain,
+            "gradient_value": 3 * P * steps / t_grad, "unit": UNIT,
+            "finite": bool(torch.isfinite(dv0).all()) and bool(torch.isfinite(loss)),
+            "timer": "wall clock around synchronised passes"}
+
+
 def run_gb300(args) -> None:
     import torch
 
@@ -473,10 +582,9 @@ def run_gb300(args) -> None:
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = start.elapsed_time(end) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t)
+    from newton_solver_fem_gb300.replicas import max_over_ranks
+
+    ms = max_over_ranks(ms, device)  # replicas: the slowest rank sets the job time
     value = world * 3 * P * substeps / (ms / 1e3)
 
     # ---- roofline of the dominant kernel: eager frames with per-launch CUDA events
@@ -525,6 +633,11 @@ def run_gb300(args) -> None:
     adjoint = None
     if not args.no_adjoint and rank == 0:
         adjoint = adjoint_measurement(device, 3)
+    tet = None
+    if not args.no_tet and rank == 0:
+        tet = tet_measurement(device, args.steps, args.warmup)
+    if batched is not None and not args.no_adjoint:
+        batched["adjoint"] = batched_adjoint_measurement(device)
 
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_baseline(args.cpu_cells or args.cells, args.cpu_sample)
@@ -548,6 +661,7 @@ def run_gb300(args) -> None:
             "finite": finite,
             "batched": batched,
             "adjoint": adjoint,
+            "tet": tet,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

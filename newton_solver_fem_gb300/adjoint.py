@@ -63,7 +63,13 @@ class DifferentiableSolver:
         _lib.check(self.lib.fem_set_mu_scale(self.solver._handle, ptr))
 
     def step(self, q, v, dt, *, external_forces=None, activations=None, mu_scale=None):
-        """One differentiable substep: returns (q', v') tracked by autograd."""
+        """One differentiable substep: returns (q', v') tracked by autograd.
+
+        The matrix is assembled for ``solver.dt`` and held fixed, so ``dt`` must
+        equal it (differentiation.py:274-276).
+        """
+        if float(dt) != self.solver.dt:
+            raise ValueError("Differentiable dt must match the fixed matrix assembly timestep")
         return _Substep.apply(self, q, v, float(dt), external_forces, activations, mu_scale)
 
     # -- primitives (no autograd) -------------------------------------------

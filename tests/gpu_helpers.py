@@ -82,3 +82,23 @@ def rel_l2(a, b):
 
 def small_batch(count=6, seed=11):
     return scenes.batched_scenes(count=count, seed=seed, dims=(2, 5))
+
+
+def mixed_model(seed=5):
+    """A Hex8 block and a Tet4 block (Rayleigh damping) joined by springs, two supports on each."""
+    xh, hexes, mh, massh = scenes.hex_block(2, 2, 2, 0.05, (0.0, 0.0, 0.0), 2.0e5, 0.4, 1000.0, k_damp=2.0)
+    xt, tets, mt, masst = scenes.tet_block(2, 2, 2, 0.05, (0.15, 0.0, 0.0), 1.0e5, 0.45, 1000.0, k_damp=1.0)
+    off = len(xh)
+    x = np.concatenate([xh, xt])
+    mass = np.concatenate([massh, masst])
+    right_face = np.nonzero(np.isclose(xh[:, 0], 0.1))[0]
+    left_face = off + np.nonzero(np.isclose(xt[:, 0], 0.15))[0]
+    springs = np.stack([right_face, left_face], axis=1).astype(np.int32)
+    rng = np.random.default_rng(seed)
+    vel = rounded(rng.normal(0, 0.05, x.shape))
+    model = model_from_arrays(rounded(x), rounded(mass), tets=tets + off, tet_materials=mt, hexes=hexes,
+                              hex_materials=mh, springs=springs, spring_ke=np.full(len(springs), 500.0, np.float32),
+                              spring_kd=np.full(len(springs), 0.5, np.float32), velocity=vel,
+                              gravity=(0.0, 0.0, -9.81), device=DEVICE)
+    fixed = np.array([0, 1, off + len(xt) - 1, off + len(xt) - 2], np.int32)
+    return model, fixed, rng

@@ -10,9 +10,9 @@ matter and the increments agree to solver precision.
 import numpy as np
 import pytest
 import torch
-from gpu_helpers import DEVICE, rounded, tensor, to_np
+from gpu_helpers import DEVICE, mixed_model, tensor, to_np
 
-from newton_solver_fem_gb300 import PreparedFEMStep, SolverFEM, model_from_arrays, scenes
+from newton_solver_fem_gb300 import PreparedFEMStep, SolverFEM
 
 pytestmark = pytest.mark.gpu
 
@@ -22,26 +22,6 @@ DT = 1.0 / 600.0
 @pytest.fixture(autouse=True)
 def _cuda(cuda_device):
     yield
-
-
-def mixed_model(seed=5):
-    """A Hex8 block and a Tet4 block (Rayleigh damping) joined by springs, two supports on each."""
-    xh, hexes, mh, massh = scenes.hex_block(2, 2, 2, 0.05, (0.0, 0.0, 0.0), 2.0e5, 0.4, 1000.0, k_damp=2.0)
-    xt, tets, mt, masst = scenes.tet_block(2, 2, 2, 0.05, (0.15, 0.0, 0.0), 1.0e5, 0.45, 1000.0, k_damp=1.0)
-    off = len(xh)
-    x = np.concatenate([xh, xt])
-    mass = np.concatenate([massh, masst])
-    right_face = np.nonzero(np.isclose(xh[:, 0], 0.1))[0]
-    left_face = off + np.nonzero(np.isclose(xt[:, 0], 0.15))[0]
-    springs = np.stack([right_face, left_face], axis=1).astype(np.int32)
-    rng = np.random.default_rng(seed)
-    vel = rounded(rng.normal(0, 0.05, x.shape))
-    model = model_from_arrays(rounded(x), rounded(mass), tets=tets + off, tet_materials=mt, hexes=hexes,
-                              hex_materials=mh, springs=springs, spring_ke=np.full(len(springs), 500.0, np.float32),
-                              spring_kd=np.full(len(springs), 0.5, np.float32), velocity=vel,
-                              gravity=(0.0, 0.0, -9.81), device=DEVICE)
-    fixed = np.array([0, 1, off + len(xt) - 1, off + len(xt) - 2], np.int32)
-    return model, fixed, rng
 
 
 def solver_for(model, fixed, **kw):

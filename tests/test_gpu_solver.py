@@ -466,3 +466,32 @@ def test_large_hex_block_true_residual_property():
     if st["unconverged_scenes"] == 0:
         assert res < 1e-2 * 1.01
     assert np.isfinite(to_np(s1.particle_q)).all()
+
+
+def test_full_size_jittered_tet_block_with_springs_and_ground():
+    """Full-size jittered Tet4 48^3 block (663,552 tets, 795,024 edge springs, ground): 3 frames of
+    10 substeps stay finite, every solve meets tol or its iteration cap, and the last substep's true
+    relative residual is re-checked in float64."""
+    sp = pytest.importorskip("scipy.sparse")
+    sc = scenes.tet_jittered_48()
+    model, solver, _ = scene_pair(sc, with_oracle=False)
+    a, b = model.state(), model.state()
+    for frame in range(3):
+        solver.refresh_tangent(a.particle_q)
+        for k in range(sc.substeps):
+            solver.step(a, b, None, None, sc.dt)
+            st = solver.stats()
+            assert st["max_iterations"] <= sc.maxiter
+            a, b = b, a
+    A = solver.A_bsr
+    P = model.particle_count
+    assert A.columns.numel() == 1_707_697  # nnzb of the survey's size table
+    M = sp.bsr_matrix((A.values.cpu().numpy().astype(np.float64), A.columns.cpu().numpy(),
+                       A.offsets.cpu().numpy()), shape=(3 * P, 3 * P))
+    rhs = to_np(b.particle_f).ravel()
+    res = np.linalg.norm(M @ to_np(solver.velocity_increment).ravel() - rhs) / np.linalg.norm(rhs)
+    if st["unconverged_scenes"] == 0:
+        assert res < sc.tolerance * 1.01
+    q = to_np(a.particle_q)
+    assert np.isfinite(q).all()
+    assert q[:, 2].min() > -0.01  # the ground holds the block (penetration below 1 cm)
