@@ -464,13 +464,16 @@ def adjoint_measurement(device: str, repeats: int) -> dict:
 
 
 def batched_adjoint_measurement(device: str, frames: int = 60) -> dict:
-    """256 uneven scenes: a 60-frame rollout and its batched adjoint pass (checkpoints every frame).
+    """256 uneven scenes: a 60-frame rollout and its batched adjoint pass.
 
-    The matrix is assembled once at rest and held fixed (the differentiable
-    contract); solves use the scenes' tolerance (1e-2, at most 50 CG).  The
-    loss is the mean height of all nodes at the end; gradients are taken with
-    respect to the initial velocities.  The plain rollout steps the same 600
-    substeps through ``SolverFEM.step``.
+    Every frame refreshes the tangent at its start, as the frame loop does, and
+    is one checkpoint segment: within a segment the matrix is fixed (the
+    differentiable contract, no dA/dq), and recomputing a segment refreshes
+    the tangent at the segment's checkpoint, so its backward pass uses the
+    same matrix as its forward pass.  Solves use the scenes' tolerance (1e-2,
+    at most 50 CG).  The loss is the mean height of all nodes at the end;
+    gradients are taken with respect to the initial velocities.  The plain
+    rollout runs the same frames through ``SolverFEM.step``.
     """
     import torch
 
@@ -481,11 +484,12 @@ def batched_adjoint_measurement(device: str, frames: int = 60) -> dict:
     model, solver = scene_solver(sc, device, sc.scene_offsets)
     P = model.particle_count
     steps = frames * sc.substeps
-    solver.refresh_tangent(model.particle_q.clone())
     diff = DifferentiableSolver(solver, tolerance=sc.tolerance, maxiter=sc.maxiter)
     q0, v0 = model.particle_q.clone(), model.particle_qd.clone()
 
     def step(q, v, k):
+        if k % sc.substeps == 0:
+            solver.refresh_tangent(q.detach().contiguous())
         return diff.step(q, v, sc.dt)
 
     def loss_fn(q, v):
@@ -495,9 +499,11 @@ def batched_adjoint_measurement(device: str, frames: int = 60) -> dict:
         a, b = model.state(), model.state()
         a.particle_q.copy_(q0)
         a.particle_qd.copy_(v0)
-        for _ in range(steps):
-            solver.step(a, b, None, None, sc.dt)
-            a, b = b, a
+        for _ in range(frames):
+            solver.refresh_tangent(a.particle_q)
+            for _ in range(sc.substeps):
+                solver.step(a, b, None, None, sc.dt)
+                a, b = b, a
         return a
 
     def wall(fn):
@@ -508,15 +514,16 @@ def batched_adjoint_measurement(device: str, frames: int = 60) -> dict:
         return time.perf_counter() - t, out
 
     wall(plain)  # warm-up
-    t_plain, _ = wall(plain)
+    t_plain, end = wall(plain)
     t_grad, out = wall(lambda: checkpointed_gradient(step, q0, v0, steps, sc.substeps, loss_fn))
     loss, _, dv0, _ = out
-    return {"workload": "256 scenes (1.56M nodes), 60 frames x 10 substeps, tol 1e-2 / 50 CG, frozen A, "
-                        "checkpoints every frame, loss = mean node height, gradient wrt v0",
+    return {"workload": "256 scenes (1.56M nodes), 60 frames x 10 substeps, tangent refreshed per frame, "
+                        "tol 1e-2 / 50 CG, checkpoints every frame, loss = mean node height, gradient wrt v0",
             "plain_rollout_ms": 1e3 * t_plain, "gradient_ms": 1e3 * t_grad,
             "gradient_over_plain": t_grad / t_plain, "plain_value": 3 * P * steps / t_plain,
             "gradient_value": 3 * P * steps / t_grad, "unit": UNIT,
-            "finite": bool(torch.isfinite(dv0).all()) and bool(torch.isfinite(loss)),
+            "finite": bool(torch.isfinite(end.particle_q).all()) and bool(torch.isfinite(dv0).all())
+                      and bool(torch.isfinite(loss)),
             "timer": "wall clock around synchronised passes"}
 
 

@@ -23,7 +23,11 @@ per-element shear scale ``s`` (``mu_scale``) is a differentiable control next
 to the reference's additive activations.  ``checkpointed_gradient`` keeps
 state checkpoints every K substeps and recomputes each segment in reverse,
 the frame-checkpoint schedule of the reference's bear training
-(``examples/diffsim/_bear_training.py:239-310``).
+(``examples/diffsim/_bear_training.py:239-310``).  A segment may begin with a
+tangent refresh (the step callback sees the substep index): each segment's
+backward pass follows its recomputation directly, so it uses the matrix its
+forward pass used; a backward pass after the matrix changed raises, as in the
+reference (``differentiation.py:375-376``).
 """
 
 from __future__ import annotations
@@ -114,6 +118,7 @@ class _Substep(torch.autograd.Function):
         q_in, v_in, q_out, v_out = diff.forward_step(q, v, dt, ext, act, scale)
         ctx.diff = diff
         ctx.dt = dt
+        ctx.revision = diff.solver._revision  # the matrix this substep was recorded with
         ctx.has = (ext is not None, act is not None, scale is not None)
         ctx.save_for_backward(q_in, v_in, act if act is not None else q_in.new_empty(0),
                               scale if scale is not None else q_in.new_empty(0))
@@ -122,6 +127,8 @@ class _Substep(torch.autograd.Function):
     @staticmethod
     def backward(ctx, q_out_bar, v_out_bar):
         diff: DifferentiableSolver = ctx.diff
+        if diff.solver._revision != ctx.revision:  # differentiation.py:375-376
+            raise RuntimeError("FEM model/matrix changed after recording; rerun the forward tape before backward")
         q_in, v_in, act, scale = ctx.saved_tensors
         has_ext, has_act, has_scale = ctx.has
         dt = ctx.dt

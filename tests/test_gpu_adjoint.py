@@ -300,3 +300,56 @@ def test_beam_backward_costs_at_most_three_forwards():
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     assert (t2 - t1) <= 3.0 * (t1 - t0), (t1 - t0, t2 - t1)
+
+
+def test_backward_after_a_matrix_refresh_raises():
+    """A tape recorded before refresh_tangent cannot be differentiated (differentiation.py:375-376)."""
+    x, tets, mats, mass, scale, fixed = small_beam()
+    model, solver, _ = make_pair(x, mass, tets=tets, tet_materials=mats, fixed=fixed, dt=1.0 / 240.0,
+                                 with_oracle=False)
+    diff = DifferentiableSolver(solver)
+    v = torch.zeros_like(model.particle_q).requires_grad_(True)
+    q1, v1 = diff.step(model.particle_q.clone(), v, solver.dt)
+    solver.refresh_tangent(q1.detach().contiguous())
+    with pytest.raises(RuntimeError, match="changed after recording"):
+        q1.sum().backward()
+
+
+def test_per_segment_refresh_matches_frozen_matrix_segments():
+    """Checkpointed gradient with a tangent refresh at every segment start equals the product of the
+    per-segment frozen-matrix gradients computed one segment at a time."""
+    x, tets, mats, mass, scale, fixed = small_beam()
+    dt = 1.0 / 240.0
+    model, solver, _ = make_pair(x, mass, tets=tets, tet_materials=mats, fixed=fixed, dt=dt,
+                                 linear_solver_maxiter=200, with_oracle=False)
+    diff = DifferentiableSolver(solver, tolerance=1e-7, maxiter=200)
+    q0 = model.particle_q.clone()
+    v0 = torch.zeros_like(q0)
+
+    def step(q, v, k):
+        if k % 3 == 0:
+            solver.refresh_tangent(q.detach().contiguous())
+        return diff.step(q, v, dt)
+
+    def loss_fn(q, v):
+        return (q[:, 2] ** 2).sum() + 0.1 * (v ** 2).sum()
+
+    _, dq_c, dv_c, _ = checkpointed_gradient(step, q0, v0, 9, 3, loss_fn)
+    # the same chain by hand: forward to each segment start, then segment-wise VJPs from the end
+    with torch.no_grad():
+        starts, q, v = [], q0.clone(), v0.clone()
+        for k in range(9):
+            if k % 3 == 0:
+                starts.append((q.clone(), v.clone()))
+            q, v = step(q, v, k)
+    qf, vf = q.clone().requires_grad_(True), v.clone().requires_grad_(True)
+    qb, vb = torch.autograd.grad(loss_fn(qf, vf), (qf, vf))
+    for seg in reversed(range(3)):
+        qs = starts[seg][0].clone().requires_grad_(True)
+        vs = starts[seg][1].clone().requires_grad_(True)
+        q, v = qs, vs
+        for k in range(3 * seg, 3 * seg + 3):
+            q, v = step(q, v, k)
+        qb, vb = torch.autograd.grad((q, v), (qs, vs), grad_outputs=(qb, vb))
+    np.testing.assert_allclose(to_np(dq_c), to_np(qb), rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(to_np(dv_c), to_np(vb), rtol=1e-6, atol=1e-9)

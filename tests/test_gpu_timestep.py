@@ -69,7 +69,7 @@ def test_changed_timestep_discards_only_the_warm_start():
     solver.velocity_increment.fill_(0.02)
     solver.refresh_tangent(state.particle_q)
     torch.cuda.synchronize()
-    np.testing.assert_array_equal(to_np(solver.velocity_increment), 0.02)
+    np.testing.assert_array_equal(to_np(solver.velocity_increment), np.float32(0.02))
     solver.refresh_tangent(state.particle_q, DT / 2)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(to_np(solver.velocity_increment), 0.0)
