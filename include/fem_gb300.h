@@ -203,6 +203,17 @@ int fem_force_vjp(FemHandle* handle, const float* q, const float* v, const float
  * plus the spring-damping term (implicit_predictor.py:9-41). */
 int fem_predictor_vjp(FemHandle* handle, const float* rhs_bar, float dt, float* v_bar, void* stream);
 
+/* Rebuild the constant matrix, the sparsity pattern, the slot map and the
+ * preconditioner after in-place edits of tet connectivity, poses, materials
+ * and masses (refresh_topology, solver.py:872-940; the sorted path, without
+ * streaming assembly).  d describes the model's current arrays with the same
+ * counts, scenes and fixed set as at creation; dt must equal the assembled
+ * timestep.  The tangent is then assembled at q (fixed nodes restored in
+ * place) and the velocity increment is cleared.  The handle's internal
+ * storage is rebuilt, so graphs captured before the call must be captured
+ * again. */
+int fem_refresh_topology(FemHandle* h, const FemDesc* d, float* q, float dt, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Prepared affine step.  Replaces the reference's PreparedFEMStep
  * (prepared_step.py:64-302; SolverFEM.prepare_step, solver.py:483-500).  The

@@ -108,6 +108,7 @@ SIGNATURES = [
     ("fem_destroy", _i32, [_p]),
     ("fem_step", _i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _f, _p]),
     ("fem_refresh_tangent", _i32, [_p, _p, _f, _p]),
+    ("fem_refresh_topology", _i32, [_p, ctypes.POINTER(FemDesc), _p, _f, _p]),
     ("fem_rebuild_element_blocks", _i32, [_p, _p, _f, _p]),
     ("fem_refresh_preconditioner", _i32, [_p, _p]),
     ("fem_set_tolerance", _i32, [_p, _f]),

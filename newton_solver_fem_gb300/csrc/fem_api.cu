@@ -639,6 +639,46 @@ int fem_get_timing(FemHandle* H, double* pcg_ms_total, int64_t* launches) {
     return cuda_status(err, &h);
 }
 
+int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, void* stream) {
+    if (H == nullptr || d == nullptr || q == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle, descriptor or positions");
+    Handle& h = H->h;
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return set_error(FEM_ERR_BAD_ARG, "dt must be finite and positive");
+    if (dt != h.dt) return set_error(FEM_ERR_BAD_ARG, "refresh_topology requires the currently assembled timestep");
+    if (h.precond != FEM_PRECOND_BLOCK_DIAG)
+        return set_error(FEM_ERR_BAD_ARG, "persistent topology updates require the block_diag preconditioner");
+    if (d->particle_count != h.P || d->tet_count != h.T || d->hex_count != h.H || d->spring_count != h.S ||
+        std::max(1, d->scene_count) != h.nscenes || d->fixed_count != h.nfixed)
+        return set_error(FEM_ERR_BAD_ARG, "topology updates must preserve the model's capacities");
+    DeviceGuard g(H->device);
+    cudaError_t e = cudaDeviceSynchronize();  // nothing may still use the storage being replaced
+    if (e != cudaSuccess) return cuda_status(e, &h);
+    FemDesc nd = *d;
+    nd.dt = dt;
+    nd.tolerance = h.tol;
+    nd.maxiter = h.maxiter;
+    nd.velocity_increment = h.dv_owned ? nullptr : h.dv;
+    FemHandle* fresh = nullptr;
+    int code = fem_create(&nd, &fresh);
+    if (code != FEM_OK) return code;
+    Handle& n = fresh->h;
+    n.wait_limit_ns = h.wait_limit_ns;
+    n.spmv_unroll = h.spmv_unroll;
+    n.l2_resident_bytes = h.l2_resident_bytes;
+    n.pcg_threads = h.pcg_threads;
+    n.grid_cap = h.grid_cap;
+    n.timing = h.timing;
+    n.mu_scale = h.mu_scale;
+    code = configure_launch(n);
+    if (code != FEM_OK) {
+        fem_destroy(fresh);
+        return code;
+    }
+    std::swap(H->h, fresh->h);
+    fresh->device = H->device;
+    fem_destroy(fresh);  // frees the previous storage
+    return fem_refresh_tangent(H, q, dt, stream);
+}
+
 int fem_refresh_tangent(FemHandle* H, float* q, float dt, void* stream) {
     if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
     Handle& h = H->h;

@@ -154,6 +154,24 @@ class SolverFEM:
 
     # ------------------------------------------------------------------ setup
     def _create(self, model, fixed, maxiter, tolerance, gke, gkd, gkf, gmu):
+        self._ground_params = (gke, gkd, gkf, gmu)
+        self._topology_storage = self._topology_signature()
+        d, keep = self._descriptor(model, fixed, maxiter, tolerance)
+        with torch.cuda.device(self.device):
+            torch.cuda.current_stream(self.device).synchronize()
+            _lib.check(self._lib.fem_create(ctypes.byref(d), ctypes.byref(self._handle)), "SolverFEM")
+        del keep
+
+    def _topology_signature(self):
+        """Capacities and storage of the arrays a topology refresh may rewrite in place."""
+        m = self.model
+        arrays = (m.particle_mass, m.particle_inv_mass, m.particle_flags, m.tet_indices, m.tet_poses, m.tet_materials)
+        counts = (m.particle_count, m.tet_count, self.hex_count, m.spring_count)
+        return counts, tuple(None if a is None else (a.data_ptr(), tuple(a.shape)) for a in arrays)
+
+    def _descriptor(self, model, fixed, maxiter, tolerance):
+        """The FemDesc of the model's current arrays (and the host copies it points into)."""
+        gke, gkd, gkf, gmu = self._ground_params
         keep = []
 
         def host(t, dtype):
@@ -212,9 +230,37 @@ class SolverFEM:
         d.maxiter = int(maxiter)
         d.tolerance = float(tolerance)
         d.velocity_increment = self.dv.data_ptr()
+        return d, keep
+
+    def refresh_topology(self, particle_q: torch.Tensor, dt: float | None = None, *, element_sources=None) -> None:
+        """Rebuild the pattern after in-place edits of tet connectivity and masses (reference ``solver.py:872-940``).
+
+        Particle and element capacities and the model's array storage must be
+        unchanged; unused tet slots carry zero materials and valid node
+        indices.  The constant matrix, the sparsity pattern, the slot map and
+        the preconditioner are rebuilt and the tangent is assembled at
+        ``particle_q`` (fixed nodes restored in place); the warm start is
+        cleared.  The handle's storage is rebuilt, so CUDA graphs captured
+        before the call must be captured again.
+        """
+        dt = self.dt if dt is None else float(dt)
+        if torch.cuda.is_current_stream_capturing():
+            raise RuntimeError("refresh_topology must run outside CUDA graph capture")
+        if self.preconditioner_type != "block_diag":
+            raise ValueError("Persistent topology updates require the block_diag preconditioner")
+        if dt != self.dt:
+            raise ValueError("refresh_topology requires the solver's currently assembled timestep")
+        if element_sources is not None:
+            raise NotImplementedError("element_sources belongs to streaming tetrahedral assembly, which is not built")
+        if self._topology_signature() != self._topology_storage:
+            raise ValueError("Topology updates must preserve model capacities and array storage")
+        _f32(particle_q, (self.model.particle_count, 3), "particle_q", self.device)
+        self._revision += 1
+        d, keep = self._descriptor(self.model, self.fixed_particle_indices, self.linear_solver_maxiter,
+                                   self.linear_solver_tolerance)
         with torch.cuda.device(self.device):
-            torch.cuda.current_stream(self.device).synchronize()
-            _lib.check(self._lib.fem_create(ctypes.byref(d), ctypes.byref(self._handle)), "SolverFEM")
+            _lib.check(self._lib.fem_refresh_topology(self._handle, ctypes.byref(d), particle_q.data_ptr(), dt,
+                                                      self._stream()), "refresh_topology")
         del keep
 
     def __del__(self):
