@@ -249,32 +249,67 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
     float3 xi = xyz(a.q4[i]), vi = xyz(a.v4[i]);
     float3 zero = f3(0.f, 0.f, 0.f);
     float3 fs = zero, ft = zero, fh = zero, fg = zero, fgr = zero, fd = zero;
+    // The incident springs and element corners are read kSpringBatch /
+    // kCornerBatch at a time (ids, then the data they index) before any is
+    // added, so that many independent loads are in flight; the sums keep the
+    // ascending incidence order.
     if (a.terms & FEM_TERM_SPRING) {
-        for (int e = a.spring_ptr[i]; e < a.spring_ptr[i + 1]; ++e) {
-            int ent = a.spring_ent[e];
-            int s = ent >> 1;
-            int ia = a.spring_idx[2 * s], ib = a.spring_idx[2 * s + 1];
-            if (ia < 0 || ib < 0) continue;
-            float3 xij = xyz(a.q4[ia]) - xyz(a.q4[ib]);
-            float3 vij = xyz(a.v4[ia]) - xyz(a.v4[ib]);
-            float L = len3(xij);
-            if (L < 1.0e-6f) continue;
-            float3 dir = f3(xij.x / L, xij.y / L, xij.z / L);
-            float c = L - a.spring_rest[s];
-            float dcdt = dot3(dir, vij);
-            float3 f = dir * (a.spring_ke[s] * c + a.spring_kd[s] * dcdt);
-            fs = (ent & 1) ? fs + f : fs - f;
+        constexpr int kSpringBatch = 4;
+        const int e1 = a.spring_ptr[i + 1];
+        for (int e0 = a.spring_ptr[i]; e0 < e1; e0 += kSpringBatch) {
+            int ent[kSpringBatch], ia[kSpringBatch], ib[kSpringBatch];
+#pragma unroll
+            for (int u = 0; u < kSpringBatch; ++u) ent[u] = e0 + u < e1 ? __ldg(a.spring_ent + e0 + u) : -1;
+#pragma unroll
+            for (int u = 0; u < kSpringBatch; ++u) {
+                const int sp = ent[u] < 0 ? 0 : ent[u] >> 1;
+                ia[u] = ent[u] < 0 ? -1 : __ldg(a.spring_idx + 2 * sp);
+                ib[u] = ent[u] < 0 ? -1 : __ldg(a.spring_idx + 2 * sp + 1);
+            }
+            float3 xij[kSpringBatch], vij[kSpringBatch];
+            float rest[kSpringBatch], ke[kSpringBatch], kd[kSpringBatch];
+#pragma unroll
+            for (int u = 0; u < kSpringBatch; ++u) {
+                const bool ok = ia[u] >= 0 && ib[u] >= 0;
+                const int ja = ok ? ia[u] : 0, jb = ok ? ib[u] : 0, sp = ok ? ent[u] >> 1 : 0;
+                xij[u] = xyz(a.q4[ja]) - xyz(a.q4[jb]);
+                vij[u] = xyz(a.v4[ja]) - xyz(a.v4[jb]);
+                rest[u] = a.spring_rest[sp];
+                ke[u] = a.spring_ke[sp];
+                kd[u] = a.spring_kd[sp];
+            }
+#pragma unroll
+            for (int u = 0; u < kSpringBatch; ++u) {
+                if (ia[u] < 0 || ib[u] < 0) continue;
+                const float L = len3(xij[u]);
+                if (L < 1.0e-6f) continue;
+                const float3 dir = f3(xij[u].x / L, xij[u].y / L, xij[u].z / L);
+                const float c = L - rest[u];
+                const float dcdt = dot3(dir, vij[u]);
+                const float3 f = dir * (ke[u] * c + kd[u] * dcdt);
+                fs = (ent[u] & 1) ? fs + f : fs - f;
+            }
         }
     }
     if (a.terms & (FEM_TERM_TET | FEM_TERM_HEX)) {
-        int tet_end = 4 * a.T;
-        for (int e = a.elem_ptr[i]; e < a.elem_ptr[i + 1]; ++e) {
-            int ent = a.elem_ent[e];
-            float3 f = xyz(a.elem_force[ent]);
-            if (ent < tet_end) {
-                if (a.terms & FEM_TERM_TET) ft = ft + f;
-            } else if (a.terms & FEM_TERM_HEX) {
-                fh = fh + f;
+        constexpr int kCornerBatch = 8;
+        const int tet_end = 4 * a.T;
+        const int e1 = a.elem_ptr[i + 1];
+        for (int e0 = a.elem_ptr[i]; e0 < e1; e0 += kCornerBatch) {
+            int ent[kCornerBatch];
+            float3 f[kCornerBatch];
+#pragma unroll
+            for (int u = 0; u < kCornerBatch; ++u) ent[u] = e0 + u < e1 ? __ldg(a.elem_ent + e0 + u) : -1;
+#pragma unroll
+            for (int u = 0; u < kCornerBatch; ++u) f[u] = xyz(a.elem_force[ent[u] < 0 ? 0 : ent[u]]);
+#pragma unroll
+            for (int u = 0; u < kCornerBatch; ++u) {
+                if (ent[u] < 0) continue;
+                if (ent[u] < tet_end) {
+                    if (a.terms & FEM_TERM_TET) ft = ft + f[u];
+                } else if (a.terms & FEM_TERM_HEX) {
+                    fh = fh + f[u];
+                }
             }
         }
     }

@@ -496,8 +496,9 @@ class SolverFEM:
         if m.tet_count and positions is not None:
             idx = m.tet_indices.long()
             p = positions.detach().double()
-            e = p[idx[:, 1:]] - p[idx[:, :1]]
-            vol = torch.linalg.det(e.transpose(1, 2)).abs() / 6.0
+            e = p[idx[:, 1:]] - p[idx[:, :1]]  # [T, 3 edges, 3]
+            # |e1 . (e2 x e3)| / 6, written out (no dependence on torch's linear-algebra backend)
+            vol = (e[:, 0] * torch.cross(e[:, 1], e[:, 2], dim=1)).sum(dim=1).abs() / 6.0
             if self._tet_volume_weights is not None:
                 vol = vol * torch.as_tensor(self._tet_volume_weights, device=vol.device).double()
             total += float(vol.sum())
