@@ -152,6 +152,8 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
 #define FEM_TUNE_CTA_THREADS 5       /* threads per PCG CTA: 256, 512, 1024, or 0 = automatic (default): 1024 when there are
                                         at least 32 slices per SM, else 256; the getter returns the size in use */
 #define FEM_TUNE_GRID_CAP 6          /* upper bound on the PCG grid (0 = as many CTAs as fit, the default) */
+#define FEM_TUNE_RESIDENT_STATE 7    /* read-only: 1 when each CTA keeps its rows' x, r, z and inverse diagonal
+                                        blocks in shared memory for the whole solve */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);

@@ -28,6 +28,7 @@ FEM_TUNE_RESIDENT_SLICES = 3
 FEM_TUNE_GRID = 4
 FEM_TUNE_CTA_THREADS = 5
 FEM_TUNE_GRID_CAP = 6
+FEM_TUNE_RESIDENT_STATE = 7
 
 FEM_TERM_SPRING = 1
 FEM_TERM_TET = 2

@@ -767,6 +767,7 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_GRID: *value = h.grid; return FEM_OK;
         case FEM_TUNE_CTA_THREADS: *value = h.pcg_threads_used; return FEM_OK;
         case FEM_TUNE_GRID_CAP: *value = h.grid_cap; return FEM_OK;
+        case FEM_TUNE_RESIDENT_STATE: *value = h.resident; return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
 }

@@ -87,6 +87,7 @@ struct PcgArgs {
     float4* zp1;
     float4* stage;   // [2P] (p_i, y_i) handed from phase A to phase B when not staged in shared memory
     int stage_smem;  // 1: the staging lives in the CTA's shared memory
+    int resident;    // 1: x, r, z and the inverse diagonal blocks of the CTA's rows live in shared memory
     // control
     unsigned* barrier;
     int* status;
@@ -181,6 +182,7 @@ struct Handle {
     float4 *zp0 = nullptr, *zp1 = nullptr;  // [2P] each: (z_i, p_i) records
     float4* stage = nullptr;                // [2P] (p_i, y_i) phase A -> phase B staging
     int stage_smem = 0;
+    int resident = 0;                       // row state resident in shared memory (see PcgArgs)
     float* dv = nullptr;
     bool dv_owned = true;
     // reductions / control

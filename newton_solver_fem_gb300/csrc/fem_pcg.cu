@@ -245,9 +245,33 @@ struct Smem {
     float4* stage;    // [L * 32 * 2] (p, y) per row, when staged in shared memory
     int* segb;        // [nsc + 1] slice bounds of this CTA's per-scene segments
     int* sseg;        // [S + 1] first segment of every scene (copy of scene_seg0)
+    float* res;       // [L * 32 * kResFloats] resident row state (x, r, z, inverse diagonal block)
+    int4* slc;        // [L] this CTA's slices: (first row, row count, scene, SELL base)
+    unsigned* rinfo;  // [L * 32] row length | fixed bit of this CTA's rows
     int nsc;          // scenes (segments) this CTA covers
     int segbase;      // this CTA's first segment
 };
+
+// Resident row state, per row of the CTA: x (0-2), r (3-5), z (6-8) and the
+// block-Jacobi inverse (9-17).  With it, the x/r/z update reads and writes
+// shared memory only; the (z, p) record is still written for the gathers.
+constexpr int kResFloats = 18;
+
+// The resident state of row `row` (lane `lane` of slice `sl`).
+__device__ __forceinline__ float* res_slot(const Smem& sm, int sl, int first, int lane) {
+    return sm.res + (size_t)((sl - first) * kSlice + lane) * kResFloats;
+}
+__device__ __forceinline__ float3 res3(const float* s, int k) { return f3(s[k], s[k + 1], s[k + 2]); }
+__device__ __forceinline__ void res3_store(float* s, int k, float3 v) {
+    s[k] = v.x;
+    s[k + 1] = v.y;
+    s[k + 2] = v.z;
+}
+__device__ __forceinline__ float3 res_minv_mul(const float* s, float3 r) {
+    const float* b = s + 9;
+    return f3(b[0] * r.x + b[1] * r.y + b[2] * r.z, b[3] * r.x + b[4] * r.y + b[5] * r.z,
+              b[6] * r.x + b[7] * r.y + b[8] * r.z);
+}
 
 // Scenes up to this count are reduced lane-parallel over their segments by one
 // warp; more scenes are reduced one scene per thread by the whole CTA.
@@ -264,18 +288,21 @@ __host__ __device__ __forceinline__ bool stage_in_smem(int L, int threads) {
 // a 16-byte boundary (the staging area holds float4).  One definition serves
 // the kernel and the host-side size.
 struct SmemLayout {
-    size_t part, st, tot, segb, sseg, stage, total;
+    size_t part, st, tot, segb, sseg, slc, rinfo, stage, res, total;
 };
 __host__ __device__ __forceinline__ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
-__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage) {
+__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage, bool resident) {
     SmemLayout m;
     m.part = 0;
     m.st = m.part + align16((size_t)L * 3 * sizeof(float));
     m.tot = m.st + align16((size_t)S * sizeof(SceneState));
     m.segb = m.tot + align16((size_t)S * 3 * sizeof(float));
     m.sseg = m.segb + align16((size_t)(L + 1) * sizeof(int));
-    m.stage = m.sseg + align16((size_t)(S + 1) * sizeof(int));
-    m.total = m.stage + (stage ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
+    m.slc = m.sseg + align16((size_t)(S + 1) * sizeof(int));
+    m.rinfo = m.slc + align16((size_t)L * sizeof(int4));
+    m.stage = m.rinfo + align16((size_t)L * kSlice * sizeof(unsigned));
+    m.res = m.stage + (stage ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
+    m.total = m.res + (resident ? (size_t)L * kSlice * kResFloats * sizeof(float) : 0);
     return m;
 }
 
@@ -389,13 +416,16 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const int S = a.nscenes;
     const int L = a.slices_per_cta;
     Smem sm;
-    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0);
+    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0, a.resident != 0);
     sm.part = reinterpret_cast<float*>(smem_raw + lay.part);
     sm.st = reinterpret_cast<SceneState*>(smem_raw + lay.st);
     sm.tot = reinterpret_cast<float*>(smem_raw + lay.tot);
     sm.stage = reinterpret_cast<float4*>(smem_raw + lay.stage);
     sm.segb = reinterpret_cast<int*>(smem_raw + lay.segb);
     sm.sseg = reinterpret_cast<int*>(smem_raw + lay.sseg);
+    sm.res = reinterpret_cast<float*>(smem_raw + lay.res);
+    sm.slc = reinterpret_cast<int4*>(smem_raw + lay.slc);
+    sm.rinfo = reinterpret_cast<unsigned*>(smem_raw + lay.rinfo);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int first = blockIdx.x * L;
@@ -409,17 +439,29 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         for (int t = threadIdx.x; t <= sm.nsc; t += blockDim.x)
             sm.segb[t] = t == 0 ? first : (t == sm.nsc ? last : a.scene_slice0[s0 + t]);
         for (int t = threadIdx.x; t <= S; t += blockDim.x) sm.sseg[t] = a.scene_seg0[t];
+        for (int t = threadIdx.x; t < last - first; t += blockDim.x) {
+            const int2 m = a.slice_meta[first + t];
+            sm.slc[t] = make_int4(m.x, m.y, a.slice_scene[first + t], a.slice_ptr[first + t]);
+        }
     }
+    __syncthreads();  // the slice table is complete before the row table reads it
+    for (int t = threadIdx.x; t < (last - first) * kSlice; t += blockDim.x) {
+        const int4 m = sm.slc[t / kSlice];
+        const int lane_t = t % kSlice;
+        sm.rinfo[t] = lane_t < m.y ? a.row_info[m.x + lane_t] : 0u;
+    }
+    __syncthreads();
     unsigned epoch = 0;
     const float h = a.dt;
 
     // ---------------- phase 0: RHS (predictor, springs, projection) and u = rhs - A x0
     for (int sl = first + warp; sl < last; sl += W) {
-        int2 meta = a.slice_meta[sl];
+        const int4 sl4 = sm.slc[sl - first];
+        const int2 meta = make_int2(sl4.x, sl4.y);
         float mx = 0.0f;
         if (lane < meta.y) {
             int row = meta.x + lane;
-            unsigned info = a.row_info[row];
+            unsigned info = sm.rinfo[(sl - first) * kSlice + lane];
             float3 rhs = f3(0.f, 0.f, 0.f), u = f3(0.f, 0.f, 0.f);
             if (a.solve_rhs != nullptr) {
                 // solve mode: A x = b, b given (projected at fixed rows), from x0 = 0 or the packed x
@@ -427,7 +469,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 u = rhs;
                 if (a.solve_warm && !(info & kFixedBit)) {
                     float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
-                    row_predictor<U>(a, a.slice_ptr[sl], (int)(info & ~kFixedBit), lane, xyz(a.v4[row]), cv, ax,
+                    row_predictor<U>(a, sl4.w, (int)(info & ~kFixedBit), lane, xyz(a.v4[row]), cv, ax,
                                      sl < a.resident_slices ? pol_last : pol_first);
                     u = rhs - ax;
                 }
@@ -436,7 +478,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                     int len = (int)(info & ~kFixedBit);
                     float3 vi = xyz(a.v4[row]);
                     float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
-                    row_predictor<U>(a, a.slice_ptr[sl], len, lane, vi, cv, ax,
+                    row_predictor<U>(a, sl4.w, len, lane, vi, cv, ax,
                                      sl < a.resident_slices ? pol_last : pol_first);
                     rhs = load3(a.f_ws, row) - cv;
                     for (int e = a.spring_ptr[row]; e < a.spring_ptr[row + 1]; ++e) {
@@ -451,7 +493,8 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 }
                 store3(a.f_ws, row, rhs);
             }
-            a.r[row] = f4(u);
+            if (a.resident) res3_store(res_slot(sm, sl, first, lane), 3, u);
+            else a.r[row] = f4(u);
             mx = fmaxf(fabsf(rhs.x), fmaxf(fabsf(rhs.y), fabsf(rhs.z)));
         }
         mx = warp_max(mx);
@@ -468,25 +511,37 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
 
     // ---------------- phase 1: normalise, initial residual and preconditioned residual
     for (int sl = first + warp; sl < last; sl += W) {
-        int2 meta = a.slice_meta[sl];
-        const SceneState& st = sm.st[a.slice_scene[sl]];
+        const int4 sl4 = sm.slc[sl - first];
+        const int2 meta = make_int2(sl4.x, sl4.y);
+        const SceneState& st = sm.st[sl4.z];
         float rr = 0.f, rz = 0.f, bb = 0.f;
         if (lane < meta.y) {
             int row = meta.x + lane;
             float sc = st.scale;
             float3 x = f3(0.f, 0.f, 0.f), r = f3(0.f, 0.f, 0.f);
+            float* rs = a.resident ? res_slot(sm, sl, first, lane) : nullptr;
             if (!st.zero) {
                 if (a.solve_rhs == nullptr || a.solve_warm) x = xyz(a.x[row]) * sc;  // else solve mode starts from zero
-                r = xyz(a.r[row]) * sc;
+                r = (a.resident ? res3(rs, 3) : xyz(a.r[row])) * sc;
             }
             float3 b;
             if (a.solve_rhs != nullptr)
-                b = (a.row_info[row] & kFixedBit) ? f3(0.f, 0.f, 0.f) : load3(a.solve_rhs, row) * sc;
+                b = (sm.rinfo[(sl - first) * kSlice + lane] & kFixedBit) ? f3(0.f, 0.f, 0.f)
+                                                                         : load3(a.solve_rhs, row) * sc;
             else
                 b = load3(a.f_ws, row) * sc;
-            float3 z = minv_mul(a.minv, row, r);
-            a.x[row] = f4(x);
-            a.r[row] = f4(r);
+            float3 z;
+            if (a.resident) {
+                for (int k = 0; k < 9; ++k) rs[9 + k] = a.minv[9 * (size_t)row + k];
+                z = res_minv_mul(rs, r);
+                res3_store(rs, 0, x);
+                res3_store(rs, 3, r);
+                res3_store(rs, 6, z);
+            } else {
+                z = minv_mul(a.minv, row, r);
+                a.x[row] = f4(x);
+                a.r[row] = f4(r);
+            }
             a.zp0[2 * (size_t)row] = f4(z);
             a.zp0[2 * (size_t)row + 1] = f4(f3(0.f, 0.f, 0.f));  // full record; p unused in the first iteration
             rr = dot3(r, r);
@@ -525,20 +580,27 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         float4* rec_next = (it & 1) ? a.zp0 : a.zp1;   // (z, p) for the next, written by phase B
         // phase A: p = z + beta p, y = (PAP + I - P) p, partial p.y
         for (int sl = first + warp; sl < last; sl += W) {
-            int2 meta = a.slice_meta[sl];
-            const SceneState& st = sm.st[a.slice_scene[sl]];
+            const int4 sl4 = sm.slc[sl - first];
+            const int2 meta = make_int2(sl4.x, sl4.y);
+            const SceneState& st = sm.st[sl4.z];
             float pap = 0.f;
             if (st.active && lane < meta.y) {
                 int row = meta.x + lane;
-                unsigned info = a.row_info[row];
+                unsigned info = sm.rinfo[(sl - first) * kSlice + lane];
                 const bool firstit = st.iters == 0;
                 const float beta = st.beta;
-                float4 zi = rec[2 * (size_t)row];
-                float3 pc = firstit ? xyz(zi) : next_p(zi, rec[2 * (size_t)row + 1], beta);
+                float3 pc;
+                if (a.resident) {  // own z resident, previous p in this row's staging slot
+                    const float3 zi = res3(res_slot(sm, sl, first, lane), 6);
+                    pc = firstit ? zi : next_p(f4(zi), stage_slot(a, sm, sl, first, lane, row)[0], beta);
+                } else {
+                    const float4 zi = rec[2 * (size_t)row];
+                    pc = firstit ? xyz(zi) : next_p(zi, rec[2 * (size_t)row + 1], beta);
+                }
                 float3 acc = pc;  // fixed rows: identity (their p is zero)
                 if (!(info & kFixedBit)) {
                     int len = (int)(info & ~kFixedBit);
-                    int base = a.slice_ptr[sl];
+                    int base = sl4.w;
                     unsigned long long pol = sl < a.resident_slices ? pol_last : pol_first;
                     acc = firstit ? row_times_p<U, true>(a, base, len, lane, rec, beta, pol)
                                   : row_times_p<U, false>(a, base, len, lane, rec, beta, pol);
@@ -558,20 +620,31 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         if (!reduce_across_grid(a, sm, buf0, 1, false, first, last, epoch, &s_ok, nullptr, set_alpha)) return;
         // phase B: x += alpha p, r -= alpha y, z = M r, partial r.r and r.z
         for (int sl = first + warp; sl < last; sl += W) {
-            int2 meta = a.slice_meta[sl];
-            const SceneState& st = sm.st[a.slice_scene[sl]];
+            const int4 sl4 = sm.slc[sl - first];
+            const int2 meta = make_int2(sl4.x, sl4.y);
+            const SceneState& st = sm.st[sl4.z];
             float rr = 0.f, rz = 0.f;
             if (st.active && lane < meta.y) {
                 int row = meta.x + lane;
                 float alpha = st.alpha;
                 const float4* stg = stage_slot(a, sm, sl, first, lane, row);
                 float3 p = xyz(stg[0]), yv = xyz(stg[1]);
-                float3 x = xyz(a.x[row]), r = xyz(a.r[row]);
+                float* rs = a.resident ? res_slot(sm, sl, first, lane) : nullptr;
+                float3 x = a.resident ? res3(rs, 0) : xyz(a.x[row]);
+                float3 r = a.resident ? res3(rs, 3) : xyz(a.r[row]);
                 x = x + p * alpha;
                 r = r - yv * alpha;
-                float3 z = minv_mul(a.minv, row, r);
-                a.x[row] = f4(x);
-                a.r[row] = f4(r);
+                float3 z;
+                if (a.resident) {
+                    z = res_minv_mul(rs, r);
+                    res3_store(rs, 0, x);
+                    res3_store(rs, 3, r);
+                    res3_store(rs, 6, z);
+                } else {
+                    z = minv_mul(a.minv, row, r);
+                    a.x[row] = f4(x);
+                    a.r[row] = f4(r);
+                }
                 rec_next[2 * (size_t)row] = f4(z);
                 rec_next[2 * (size_t)row + 1] = f4(p);
                 rr = dot3(r, r);
@@ -604,16 +677,17 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
 
     // ---------------- epilogue: restore scale, integrate, fixed restore
     for (int sl = first + warp; sl < last; sl += W) {
-        int2 meta = a.slice_meta[sl];
+        const int4 sl4 = sm.slc[sl - first];
+        const int2 meta = make_int2(sl4.x, sl4.y);
         if (lane >= meta.y) continue;
-        const SceneState& st = sm.st[a.slice_scene[sl]];
+        const SceneState& st = sm.st[sl4.z];
         int row = meta.x + lane;
-        float3 dv = xyz(a.x[row]);
+        float3 dv = a.resident ? res3(res_slot(sm, sl, first, lane), 0) : xyz(a.x[row]);
         float sc = st.scale;
         dv = f3(dv.x / sc, dv.y / sc, dv.z / sc);
         store3(a.dv, row, dv);
         if (a.write_state) {
-            bool fixed = (a.row_info[row] & kFixedBit) != 0;
+            bool fixed = (sm.rinfo[(sl - first) * kSlice + lane] & kFixedBit) != 0;
             float3 v = xyz(a.v4[row]) + dv;
             float3 q = xyz(a.q4[row]) + v * h;
             if (fixed) {
@@ -671,38 +745,71 @@ cudaError_t pcg_configure(Handle& h) {
     const int threads = h.pcg_threads > 0 ? h.pcg_threads : (h.nslices >= 32 * sms ? 1024 : 256);
     h.pcg_threads_used = threads;
     const int warps_per_cta = threads / 32;
-    int grid = (h.nslices + warps_per_cta - 1) / warps_per_cta;
-    if (grid < 1) grid = 1;
-    if (h.grid_cap > 0 && grid > h.grid_cap) grid = h.grid_cap;
-    for (int pass = 0;; ++pass) {
-        const int L = (h.nslices + grid - 1) / grid > 0 ? (h.nslices + grid - 1) / grid : 1;
-        bool stage = stage_in_smem(L, threads) && pass < 16;  // give up shared staging if it never settles
-        int per_sm = 0;
-        for (int attempt = 0; attempt < 2; ++attempt) {
-            const SmemLayout lay = smem_layout(L, h.nscenes, stage);
-            if ((lay.st | lay.tot | lay.segb | lay.sseg | lay.stage) & 15) return cudaErrorMisalignedAddress;
-            if (lay.total > 48 * 1024) {
-                err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
-                if (err != cudaSuccess) return err;
+    // One configuration: the grid only shrinks from pass to pass (a smaller grid
+    // means more slices per CTA and possibly more shared memory), and the loop
+    // ends with a layout whose occupancy covers the grid.  want_resident asks
+    // for the resident row state when the staging is in shared memory.
+    struct Config {
+        int grid, L, stage, resident;
+        size_t smem;
+    };
+    auto fit = [&](bool want_resident, Config& c) -> cudaError_t {
+        int grid = (h.nslices + warps_per_cta - 1) / warps_per_cta;
+        if (grid < 1) grid = 1;
+        if (h.grid_cap > 0 && grid > h.grid_cap) grid = h.grid_cap;
+        for (int pass = 0;; ++pass) {
+            const int L = (h.nslices + grid - 1) / grid > 0 ? (h.nslices + grid - 1) / grid : 1;
+            bool stage = stage_in_smem(L, threads) && pass < 16;  // give up shared staging if it never settles
+            bool res = want_resident && stage;
+            int per_sm = 0;
+            size_t smem = 0;
+            for (int attempt = 0; attempt < 3; ++attempt) {
+                const SmemLayout lay = smem_layout(L, h.nscenes, stage, res);
+                if ((lay.st | lay.tot | lay.segb | lay.sseg | lay.slc | lay.rinfo | lay.stage | lay.res) & 15)
+                    return cudaErrorMisalignedAddress;
+                if (lay.total > 227 * 1024) {
+                    per_sm = 0;
+                } else {
+                    if (lay.total > 48 * 1024) {
+                        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                             (int)lay.total);
+                        if (e != cudaSuccess) return e;
+                    }
+                    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, lay.total);
+                    if (e != cudaSuccess) return e;
+                }
+                smem = lay.total;
+                if (per_sm >= 1) break;
+                if (res) res = false;            // first drop the resident state,
+                else if (stage) stage = false;  // then the shared staging
+                else break;
             }
-            err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, lay.total);
-            if (err != cudaSuccess) return err;
-            if (per_sm >= 1 || !stage) {
-                h.pcg_smem = lay.total;
-                break;
+            if (per_sm < 1) return cudaErrorInvalidConfiguration;
+            const int cap = per_sm * sms;
+            if (grid <= cap) {
+                c = Config{grid, L, stage ? 1 : 0, res ? 1 : 0, smem};
+                return cudaSuccess;
             }
-            stage = false;  // staging does not fit at all: use the global buffer
+            grid = cap;
         }
-        if (per_sm < 1) return cudaErrorInvalidConfiguration;
-        const int cap = per_sm * sms;
-        if (grid <= cap) {
-            h.grid = grid;
-            h.slices_per_cta = L;
-            h.stage_smem = stage ? 1 : 0;
-            return cudaSuccess;
-        }
-        grid = cap;
+    };
+    Config plain{}, resident{};
+    err = fit(false, plain);
+    if (err != cudaSuccess) return err;
+    err = fit(true, resident);
+    if (err != cudaSuccess) return err;
+    // keep the resident state only when it costs no co-resident CTAs
+    const Config& c = (resident.resident && resident.grid == plain.grid) ? resident : plain;
+    if (c.smem > 48 * 1024) {
+        err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+        if (err != cudaSuccess) return err;
     }
+    h.grid = c.grid;
+    h.slices_per_cta = c.L;
+    h.stage_smem = c.stage;
+    h.resident = c.resident;
+    h.pcg_smem = c.smem;
+    return cudaSuccess;
 }
 
 cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float* v_out, float* f_ws, cudaStream_t s,
@@ -743,6 +850,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.zp1 = h.zp1;
     a.stage = h.stage;
     a.stage_smem = h.stage_smem;
+    a.resident = h.resident;
     a.barrier = h.barrier;
     a.status = h.status;
     a.scene_stats = h.scene_stats;
