@@ -441,7 +441,7 @@ __global__ void predictor_vjp_kernel(int nslices, const int* __restrict__ slice_
 using fem::Handle;
 
 namespace {
-int adj_cuda(cudaError_t e) { return e == cudaSuccess ? FEM_OK : FEM_ERR_CUDA; }
+int adj_cuda(cudaError_t e) { return fem::report_cuda(e); }
 struct AdjDeviceGuard {
     int prev = -1;
     explicit AdjDeviceGuard(int dev) {
@@ -458,14 +458,15 @@ struct AdjDeviceGuard {
 extern "C" {
 
 int fem_set_mu_scale(FemHandle* H, const float* scale) {
-    if (H == nullptr) return FEM_ERR_BAD_ARG;
+    if (H == nullptr) return fem::report(FEM_ERR_BAD_ARG, "fem_set_mu_scale: null handle");
     H->h.mu_scale = scale;
     return FEM_OK;
 }
 
 int fem_solve(FemHandle* H, const float* rhs, float* x, float tolerance, int32_t maxiter, void* stream) {
-    if (H == nullptr || rhs == nullptr || x == nullptr) return FEM_ERR_BAD_ARG;
-    if (!(tolerance > 0.0f) || maxiter < 0) return FEM_ERR_BAD_ARG;
+    if (H == nullptr || rhs == nullptr || x == nullptr) return fem::report(FEM_ERR_BAD_ARG, "fem_solve: null argument");
+    if (!(tolerance > 0.0f) || maxiter < 0)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_solve: tolerance must be positive and maxiter non-negative");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
     AdjDeviceGuard g(H->device);
@@ -477,7 +478,7 @@ int fem_force_vjp(FemHandle* H, const float* q, const float* v, const float* act
                   const float* force_bar, float* q_bar, float* v_bar, float* activation_bar, float* mu_scale_bar,
                   void* stream) {
     if (H == nullptr || q == nullptr || v == nullptr || force_bar == nullptr || q_bar == nullptr || v_bar == nullptr)
-        return FEM_ERR_BAD_ARG;
+        return fem::report(FEM_ERR_BAD_ARG, "fem_force_vjp: null argument");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
     AdjDeviceGuard g(H->device);
@@ -485,7 +486,7 @@ int fem_force_vjp(FemHandle* H, const float* q, const float* v, const float* act
     if (h.elem_grad == nullptr && (h.T > 0 || h.H > 0)) {  // first call: adjoint scratch
         void* p = nullptr;
         size_t n = 2 * (4 * (size_t)h.T + 8 * (size_t)h.H);
-        if (cudaMalloc(&p, n * sizeof(float4)) != cudaSuccess) return FEM_ERR_CUDA;
+        if (cudaError_t e = cudaMalloc(&p, n * sizeof(float4)); e != cudaSuccess) return fem::report_cuda(e);
         h.allocations.push_back(p);
         h.elem_grad = (float4*)p;
     }
@@ -536,7 +537,8 @@ int fem_force_vjp(FemHandle* H, const float* q, const float* v, const float* act
 }
 
 int fem_predictor_vjp(FemHandle* H, const float* rhs_bar, float dt, float* v_bar, void* stream) {
-    if (H == nullptr || rhs_bar == nullptr || v_bar == nullptr) return FEM_ERR_BAD_ARG;
+    if (H == nullptr || rhs_bar == nullptr || v_bar == nullptr)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_predictor_vjp: null argument");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
     AdjDeviceGuard g(H->device);

@@ -97,6 +97,22 @@ int set_error(int code, const std::string& msg) {
     return code;
 }
 
+}  // namespace
+
+namespace fem {
+int report(int code, const char* message) {
+    g_error = message;
+    return code;
+}
+int report_cuda(cudaError_t err) {
+    if (err == cudaSuccess) return FEM_OK;
+    g_error = std::string("CUDA error: ") + cudaGetErrorString(err);
+    return FEM_ERR_CUDA;
+}
+}  // namespace fem
+
+namespace {
+
 int cuda_status(cudaError_t e, Handle* h = nullptr) {
     if (e == cudaSuccess) return FEM_OK;
     std::string msg = std::string("CUDA error: ") + cudaGetErrorString(e);

@@ -209,6 +209,11 @@ struct Handle {
     std::string last_error;
 };
 
+// Status reporting shared by every entry point: the message is what
+// fem_status_string returns for the code (fem_api.cu).
+int report(int code, const char* message);
+int report_cuda(cudaError_t err);
+
 // dN_a/dxi at the 8 Gauss points (host copy, filled as the reference computes it)
 void fill_hex_reference_table(float table[8][8][3]);
 void upload_hex_reference_table();          // fem_elements.cu copy

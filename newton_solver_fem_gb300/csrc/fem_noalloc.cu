@@ -27,6 +27,11 @@
 #include "fem_gb300.h"
 #include "fem_math.cuh"
 
+namespace fem {  // status reporting shared with the other entry points (fem_api.cu)
+int report(int code, const char* message);
+int report_cuda(cudaError_t err);
+}  // namespace fem
+
 namespace {
 
 constexpr int kMaxRows = 65536;
@@ -343,19 +348,22 @@ DeviceSetup g_setup[64];
 // device address and the cooperative grid limit.
 int setup_device(DeviceSetup** out) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FEM_ERR_CUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return fem::report(FEM_ERR_CUDA, "fem_pcg_solve_noalloc: no current CUDA device");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     DeviceSetup& d = g_setup[dev];
     if (!d.ready) {
         void* ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || ptr == nullptr) return FEM_ERR_CUDA;
+        if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || ptr == nullptr)
+            return fem::report(FEM_ERR_CUDA, "fem_pcg_solve_noalloc: scratch symbol unavailable");
         int sms = 0, coop = 0, per_sm = 0;
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FEM_ERR_CUDA;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return fem::report(FEM_ERR_CUDA, "fem_pcg_solve_noalloc: device query failed");
         if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
-            return FEM_ERR_UNSUPPORTED;
+            return fem::report(FEM_ERR_UNSUPPORTED, "fem_pcg_solve_noalloc: cooperative launch unavailable");
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, noalloc_pcg_kernel, kThreads, 0) != cudaSuccess ||
             per_sm < 1)
-            return FEM_ERR_CUDA;
+            return fem::report(FEM_ERR_CUDA, "fem_pcg_solve_noalloc: occupancy query failed");
         d.scratch = static_cast<unsigned char*>(ptr);
         d.max_grid = per_sm * sms < kMaxBlocks ? per_sm * sms : kMaxBlocks;
         d.ready = true;
@@ -369,16 +377,20 @@ int setup_device(DeviceSetup** out) {
 extern "C" int fem_pcg_solve_noalloc(const int32_t* offsets, const int32_t* columns, const float* values,
                                      const float* rhs, float* x_inout, int32_t rows, float tolerance,
                                      int32_t maxiter, int32_t* info, void* stream) {
-    if (rows < 0 || rows > kMaxRows) return FEM_ERR_BAD_ARG;  // beyond the static scratch capacity
-    if (!(tolerance > 0.0f) || maxiter < 0) return FEM_ERR_BAD_ARG;
+    if (rows < 0 || rows > kMaxRows)  // beyond the static scratch capacity
+        return fem::report(FEM_ERR_BAD_ARG, "fem_pcg_solve_noalloc: rows outside [0, 65536]");
+    if (!(tolerance > 0.0f) || maxiter < 0)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_pcg_solve_noalloc: tolerance must be positive and maxiter non-negative");
     if (rows == 0) return FEM_OK;
-    if (!offsets || !columns || !values || !rhs || !x_inout) return FEM_ERR_BAD_ARG;
+    if (!offsets || !columns || !values || !rhs || !x_inout)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_pcg_solve_noalloc: null argument");
     DeviceSetup* d = nullptr;
     int code = setup_device(&d);
     if (code != FEM_OK) return code;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Scratch sc = carve(d->scratch);
-    if (cudaMemsetAsync(sc.barrier, 0, 128, s) != cudaSuccess) return FEM_ERR_CUDA;  // barrier + status
+    if (cudaError_t e = cudaMemsetAsync(sc.barrier, 0, 128, s); e != cudaSuccess)  // barrier + status
+        return fem::report_cuda(e);
     int rows_per_cta_min = 64;  // keep CTAs busy
     int grid = (rows + rows_per_cta_min - 1) / rows_per_cta_min;
     if (grid > d->max_grid) grid = d->max_grid;
@@ -404,5 +416,5 @@ extern "C" int fem_pcg_solve_noalloc(const int32_t* offsets, const int32_t* colu
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, noalloc_pcg_kernel, a) == cudaSuccess ? FEM_OK : FEM_ERR_CUDA;
+    return fem::report_cuda(cudaLaunchKernelEx(&cfg, noalloc_pcg_kernel, a));
 }

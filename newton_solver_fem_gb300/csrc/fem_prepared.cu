@@ -188,7 +188,6 @@ struct Guard {
     }
 };
 
-int status_of(cudaError_t e) { return e == cudaSuccess ? FEM_OK : FEM_ERR_CUDA; }
 
 cudaError_t launch_rhs(Handle& h, const FemPreparedWs* w, const float* ext, float dt, float* out, cudaStream_t s) {
     prepared_rhs_kernel<<<blocks(h.P, 256), 256, 0, s>>>(h.P, w->impulse, ext, dt, w->predictor, h.node_spring_ptr,
@@ -207,10 +206,12 @@ extern "C" {
 int fem_prepare(FemHandle* H, const FemPreparedWs* w, const float* q_in, const float* v_in,
                 const float* external_forces, const float* activations, const float* gravity, float dt,
                 void* stream) {
-    if (H == nullptr || !fem::ws_ok(w) || q_in == nullptr || v_in == nullptr) return FEM_ERR_BAD_ARG;
+    if (H == nullptr || !fem::ws_ok(w) || q_in == nullptr || v_in == nullptr)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_prepare: null handle, workspace array or state");
     Handle& h = H->h;
-    if (!(dt > 0.0f)) return FEM_ERR_BAD_ARG;
-    if (h.enable_act && h.T > 0 && activations == nullptr) return FEM_ERR_BAD_ARG;
+    if (!(dt > 0.0f)) return fem::report(FEM_ERR_BAD_ARG, "fem_prepare: dt must be positive");
+    if (h.enable_act && h.T > 0 && activations == nullptr)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_prepare: tet activations are enabled but none were passed");
     if (h.P == 0) return FEM_OK;
     fem::Guard g(H->device);
     cudaStream_t s = (cudaStream_t)stream;
@@ -229,41 +230,46 @@ int fem_prepare(FemHandle* H, const FemPreparedWs* w, const float* q_in, const f
     if (err == cudaSuccess) err = fem::launch_rhs(h, w, nullptr, dt, w->base_rhs, s);
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(w->increment, h.dv, sizeof(float) * 3 * (size_t)h.P, cudaMemcpyDeviceToDevice, s);
-    return fem::status_of(err);
+    return fem::report_cuda(err);
 }
 
 int fem_prepared_rhs(FemHandle* H, const FemPreparedWs* w, const float* external_forces, float dt, float* out,
                      void* stream) {
-    if (H == nullptr || !fem::ws_ok(w) || out == nullptr || out == external_forces) return FEM_ERR_BAD_ARG;
+    if (H == nullptr || !fem::ws_ok(w) || out == nullptr || out == external_forces)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_prepared_rhs: null argument or output aliasing the load");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
     fem::Guard g(H->device);
-    return fem::status_of(fem::launch_rhs(h, w, external_forces, dt, out, (cudaStream_t)stream));
+    return fem::report_cuda(fem::launch_rhs(h, w, external_forces, dt, out, (cudaStream_t)stream));
 }
 
 int fem_apply_operator(FemHandle* H, const float* x, float* y, void* stream) {
-    if (H == nullptr || x == nullptr || y == nullptr || x == y) return FEM_ERR_BAD_ARG;
+    if (H == nullptr || x == nullptr || y == nullptr || x == y)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_apply_operator: null or aliased vectors");
     Handle& h = H->h;
     if (h.P == 0 || h.nslices == 0) return FEM_OK;
     fem::Guard g(H->device);
     fem::apply_operator_kernel<<<fem::blocks((int64_t)h.nslices * 32, 256), 256, 0, (cudaStream_t)stream>>>(
         h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.scol, x, y);
-    return fem::status_of(cudaGetLastError());
+    return fem::report_cuda(cudaGetLastError());
 }
 
 int fem_apply_preconditioner(FemHandle* H, const float* r, float* z, void* stream) {
-    if (H == nullptr || r == nullptr || z == nullptr || r == z) return FEM_ERR_BAD_ARG;
+    if (H == nullptr || r == nullptr || z == nullptr || r == z)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_apply_preconditioner: null or aliased vectors");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
     fem::Guard g(H->device);
     fem::apply_preconditioner_kernel<<<fem::blocks(h.P, 256), 256, 0, (cudaStream_t)stream>>>(h.P, h.minv, r, z);
-    return fem::status_of(cudaGetLastError());
+    return fem::report_cuda(cudaGetLastError());
 }
 
 int fem_prepared_solve(FemHandle* H, const FemPreparedWs* w, const float* rhs, float tolerance, int32_t maxiter,
                        float dt, void* stream) {
-    if (H == nullptr || !fem::ws_ok(w) || rhs == nullptr) return FEM_ERR_BAD_ARG;
-    if (!(tolerance > 0.0f) || maxiter < 0) return FEM_ERR_BAD_ARG;
+    if (H == nullptr || !fem::ws_ok(w) || rhs == nullptr)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_prepared_solve: null handle, workspace array or rhs");
+    if (!(tolerance > 0.0f) || maxiter < 0)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_prepared_solve: tolerance must be positive and maxiter non-negative");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
     fem::Guard g(H->device);
@@ -273,19 +279,21 @@ int fem_prepared_solve(FemHandle* H, const FemPreparedWs* w, const float* rhs, f
     if (err == cudaSuccess)
         err = fem::launch_pcg(h, dt, 0, nullptr, nullptr, nullptr, s, rhs, w->increment, tolerance, maxiter,
                               /*solve_warm=*/true);
-    return fem::status_of(err);
+    return fem::report_cuda(err);
 }
 
 int fem_prepared_reconstruct(FemHandle* H, const FemPreparedWs* w, const float* dv, float dt, float* q_out,
                              float* v_out, void* stream) {
-    if (H == nullptr || !fem::ws_ok(w) || dv == nullptr || q_out == nullptr || v_out == nullptr) return FEM_ERR_BAD_ARG;
-    if (q_out == w->q || v_out == w->v) return FEM_ERR_BAD_ARG;
+    if (H == nullptr || !fem::ws_ok(w) || dv == nullptr || q_out == nullptr || v_out == nullptr)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_prepared_reconstruct: null argument");
+    if (q_out == w->q || v_out == w->v)
+        return fem::report(FEM_ERR_BAD_ARG, "fem_prepared_reconstruct: outputs must not be the prepared state");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
     fem::Guard g(H->device);
     fem::reconstruct_kernel<<<fem::blocks(h.P, 256), 256, 0, (cudaStream_t)stream>>>(
         h.P, dv, w->q, w->v, h.fixed_mask, h.rest, dt, q_out, v_out);
-    return fem::status_of(cudaGetLastError());
+    return fem::report_cuda(cudaGetLastError());
 }
 
 }  // extern "C"

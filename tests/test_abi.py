@@ -75,3 +75,36 @@ def test_bad_arguments_are_rejected_without_a_gpu(library):
     assert library.fem_create(None, ctypes.byref(h)) == _lib.FEM_ERR_BAD_ARG
     with pytest.raises(ValueError):
         _lib.check(code)
+
+
+def _message(library, code):
+    return library.fem_status_string(code).decode()
+
+
+def test_every_rejection_reports_its_own_message(library):
+    """Each entry point names itself in the status message of a host-side rejection, so
+    a message left over from an earlier call is never reported instead."""
+    ws = _lib.FemPreparedWs()
+    cases = [
+        ("fem_prepare", lambda: library.fem_prepare(None, ctypes.byref(ws), None, None, None, None, None, 0.01, None)),
+        ("fem_prepared_rhs", lambda: library.fem_prepared_rhs(None, ctypes.byref(ws), None, 0.01, None, None)),
+        ("fem_apply_operator", lambda: library.fem_apply_operator(None, None, None, None)),
+        ("fem_apply_preconditioner", lambda: library.fem_apply_preconditioner(None, None, None, None)),
+        ("fem_prepared_solve",
+         lambda: library.fem_prepared_solve(None, ctypes.byref(ws), None, 1e-6, 10, 0.01, None)),
+        ("fem_prepared_reconstruct",
+         lambda: library.fem_prepared_reconstruct(None, ctypes.byref(ws), None, 0.01, None, None, None)),
+        ("fem_set_mu_scale", lambda: library.fem_set_mu_scale(None, None)),
+        ("fem_solve", lambda: library.fem_solve(None, None, None, 1e-6, 10, None)),
+        ("fem_force_vjp", lambda: library.fem_force_vjp(*([None] * 11))),
+        ("fem_predictor_vjp", lambda: library.fem_predictor_vjp(None, None, 0.01, None, None)),
+        ("fem_pcg_solve_noalloc",
+         lambda: library.fem_pcg_solve_noalloc(None, None, None, None, None, 4, 1e-6, 10, None, None)),
+        ("rows outside", lambda: library.fem_pcg_solve_noalloc(None, None, None, None, None, -1, 1e-6, 10, None, None)),
+        ("tolerance", lambda: library.fem_pcg_solve_noalloc(None, None, None, None, None, 4, 0.0, 10, None, None)),
+    ]
+    for expected, call in cases:
+        assert library.fem_create(None, None) == _lib.FEM_ERR_BAD_ARG  # leaves a different message behind
+        code = call()
+        assert code == _lib.FEM_ERR_BAD_ARG, expected
+        assert expected in _message(library, code), (expected, _message(library, code))
