@@ -18,6 +18,7 @@
  *   fem_velocity_increment_ptr   SolverFEM.velocity_increment        solver.py:478-481
  *   fem_get_stats                SolverFEM.last_cg_iters             solver.py:279, 1333-1335
  *   fem_eval_forces              SolverFEM.eval_*_forces             solver.py:1357-1600
+ *   fem_set_soft_contacts        Contacts.soft_contact_* into step   solver.py:1540-1566
  *   fem_export_bsr               SolverFEM.A_bsr (Warp BsrMatrix)    solver.py:322-337
  *   fem_export_preconditioner    SolverFEM._pc_inv_diag              solver.py:1142-1201
  *   fem_matrix_info              A_bsr.nnz / nrow                    solver.py:322-328
@@ -62,6 +63,10 @@ extern "C" {
 #define FEM_TERM_GROUND 8
 #define FEM_TERM_GRAVITY 16
 #define FEM_TERM_DAMPING 32
+#define FEM_TERM_TRI 64           /* triangle membrane, kernels.py:876-960 */
+#define FEM_TERM_PARTICLE 128     /* hash-grid particle-particle contact, kernels.py:1036-1114 */
+#define FEM_TERM_SOFT_CONTACT 256 /* soft-rigid contact list, kernels.py:1198-1261 */
+#define FEM_TERM_ALL 511
 
 typedef struct FemHandle FemHandle;
 
@@ -104,6 +109,23 @@ typedef struct FemDesc {
     int32_t maxiter;
     float tolerance;
     float* velocity_increment; /* optional caller-owned DEVICE [P,3] buffer for dv; NULL = handle-owned */
+    /* Triangles (Newton tri_*): membrane + area + drag/lift force, lumped
+     * constant tangent h^2 (mu + lambda) A_rest / 3 on each vertex diagonal. */
+    int32_t tri_count;             /* Tri */
+    const int32_t* tri_indices;    /* [Tri,3] */
+    const float* tri_poses;        /* [Tri,2,2] inverse rest edge matrix in the triangle's own frame */
+    const float* tri_materials;    /* [Tri,5] (ke, ka, kd, drag, lift) */
+    /* Spring bend torque (solver.py:1437-1475): active when torque_stiffness > 0
+     * and spring_rest_direction is given. */
+    const float* spring_rest_direction; /* [S,3] unit rest directions or NULL */
+    float torque_stiffness, torque_damping;
+    /* Particle-particle self contact (solver.py:1477-1511): active when
+     * particle_contact != 0 (ke > 0, P > 1, max radius > 0 and a grid). */
+    int32_t particle_contact;
+    float particle_ke, particle_kd, particle_kf, particle_mu, particle_cohesion, particle_max_radius;
+    /* Soft-rigid contact material (Newton model.soft_contact_*); the contact
+     * list itself is registered per step with fem_set_soft_contacts. */
+    float soft_contact_ke, soft_contact_kd, soft_contact_kf, soft_contact_mu;
 } FemDesc;
 
 /* Per-solve statistics (one entry per scene, plus the sticky device status). */
@@ -168,6 +190,16 @@ int fem_get_stats(FemHandle* handle, FemStats* stats, int32_t* scene_iterations,
 int fem_set_timing(FemHandle* handle, int32_t enable);
 int fem_get_timing(FemHandle* handle, double* pcg_ms_total, int64_t* launches);
 
+/* Soft-rigid contacts for the following fem_step / fem_eval_forces / fem_prepare
+ * calls (SolverFEM.eval_soft_contact_forces, solver.py:1540-1566, over Newton's
+ * Contacts.soft_contact_*).  Device pointers: count [1] (read on the device, so
+ * no host sync), particle [capacity], body_pos / body_vel / normal
+ * [capacity,3]; entries at or past *count, or with a particle outside [0, P),
+ * are ignored.  capacity 0 (or NULL pointers) clears the registration.  A
+ * larger capacity than before allocates scratch, so register before capture. */
+int fem_set_soft_contacts(FemHandle* handle, const int32_t* count, const int32_t* particle, const float* body_pos,
+                          const float* body_vel, const float* normal, int32_t capacity);
+
 /* Selected force terms (FEM_TERM_* bits), unscaled, summed into out[P,3]. */
 int fem_eval_forces(FemHandle* handle, const float* q, const float* v, const float* activations,
                     const float* gravity, int32_t terms, float* out, void* stream);
@@ -177,7 +209,7 @@ int fem_eval_forces(FemHandle* handle, const float* q, const float* v, const flo
 int fem_matrix_info(FemHandle* handle, int64_t* nnzb, int64_t* triplet_count, int64_t* stored_blocks);
 int fem_export_bsr(FemHandle* handle, int32_t* offsets, int32_t* columns, float* values, void* stream);
 int fem_export_preconditioner(FemHandle* handle, float* inverse_blocks, void* stream);
-/* Raw element/constant blocks in the reference's triplet layout [P | 2S | 16T | 64H] (bsr_values). */
+/* Raw element/constant blocks in the reference's triplet layout [P | 2S | 3Tri | 16T | 64H] (bsr_values). */
 int fem_export_triplets(FemHandle* handle, int32_t* rows, int32_t* columns, float* values, void* stream);
 
 /* ---- Differentiation with the system matrix held fixed (the reference's

@@ -2,18 +2,21 @@
 
 Public names follow the reference package (``newton_solver_fem/__init__.py``):
 ``SolverFEM`` (alias ``SolverLinearFEM``), ``FEMBuilder`` and ``LinearFEMData``,
-plus the minimal ``Model`` / ``State`` / ``Control`` containers the solver reads.
+plus the minimal ``Model`` / ``State`` / ``Control`` / ``Contacts`` containers the solver reads.
 The numerical work runs in ``libfemgb300.so`` (``include/fem_gb300.h``).
 """
 
-from .builder import FEMBuilder, LinearFEMData, Model, State, Control, hex_gauss_data, model_from_arrays
+from .builder import (Contacts, Control, FEMBuilder, HashGrid, LinearFEMData, Model, State, hex_gauss_data,
+                      model_from_arrays, triangle_rest_data)
 from .prepared_step import PreparedFEMStep
 from .solver import BsrMatrix, SolverFEM, SolverLinearFEM
 
 __all__ = [
     "BsrMatrix",
+    "Contacts",
     "Control",
     "FEMBuilder",
+    "HashGrid",
     "LinearFEMData",
     "Model",
     "PreparedFEMStep",
@@ -22,4 +25,5 @@ __all__ = [
     "State",
     "hex_gauss_data",
     "model_from_arrays",
+    "triangle_rest_data",
 ]

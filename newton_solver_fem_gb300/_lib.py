@@ -36,6 +36,10 @@ FEM_TERM_HEX = 4
 FEM_TERM_GROUND = 8
 FEM_TERM_GRAVITY = 16
 FEM_TERM_DAMPING = 32
+FEM_TERM_TRI = 64
+FEM_TERM_PARTICLE = 128
+FEM_TERM_SOFT_CONTACT = 256
+FEM_TERM_ALL = 511
 
 _f = ctypes.c_float
 _i32 = ctypes.c_int32
@@ -84,6 +88,24 @@ class FemDesc(ctypes.Structure):
         ("maxiter", _i32),
         ("tolerance", _f),
         ("velocity_increment", _p),
+        ("tri_count", _i32),
+        ("tri_indices", _p),
+        ("tri_poses", _p),
+        ("tri_materials", _p),
+        ("spring_rest_direction", _p),
+        ("torque_stiffness", _f),
+        ("torque_damping", _f),
+        ("particle_contact", _i32),
+        ("particle_ke", _f),
+        ("particle_kd", _f),
+        ("particle_kf", _f),
+        ("particle_mu", _f),
+        ("particle_cohesion", _f),
+        ("particle_max_radius", _f),
+        ("soft_contact_ke", _f),
+        ("soft_contact_kd", _f),
+        ("soft_contact_kf", _f),
+        ("soft_contact_mu", _f),
     ]
 
 
@@ -120,6 +142,7 @@ SIGNATURES = [
     ("fem_reset", _i32, [_p, _p]),
     ("fem_velocity_increment_ptr", _p, [_p]),
     ("fem_get_stats", _i32, [_p, ctypes.POINTER(FemStats), _p, _p]),
+    ("fem_set_soft_contacts", _i32, [_p, _p, _p, _p, _p, _p, _i32]),
     ("fem_set_timing", _i32, [_p, _i32]),
     ("fem_get_timing", _i32, [_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]),
     ("fem_eval_forces", _i32, [_p, _p, _p, _p, _p, _i32, _p, _p]),

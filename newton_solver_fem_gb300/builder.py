@@ -7,15 +7,21 @@ this project, so this module provides the subset of that contract the solver
 hot path consumes, with PyTorch tensors on a CUDA device as storage:
 
 * ``Model``: particle_q/qd/mass/inv_mass/radius/flags, tet_indices/poses/
-  materials/activations, spring_indices/rest_length/stiffness/damping,
-  gravity, ``fem`` (``LinearFEMData`` with the Hex8 Gauss data), and optional
-  ``scene_offsets`` for independent batched scenes.
+  materials/activations, tri_indices/poses/materials, spring_indices/
+  rest_length/stiffness/damping, gravity, ``fem`` (``LinearFEMData`` with the
+  Hex8 Gauss data), the particle-contact and soft-contact coefficients,
+  ``particle_grid`` and optional ``scene_offsets`` for independent batched
+  scenes.
 * ``State``: particle_q, particle_qd, particle_f.  ``Control``: tet_activations.
+* ``Contacts``: the soft-rigid contact list (``soft_contact_*``) a collision
+  pipeline produces.
 
 Conventions follow Newton's: a tet pose is the inverse of the rest edge matrix
-``[x1-x0, x2-x0, x3-x0]`` (columns) and non-positive tets are rejected; Hex8
-``inv_J0`` / ``|det J0|`` are computed in float64 per Gauss point and stored as
-float32 (``builder.py:95-135``).
+``[x1-x0, x2-x0, x3-x0]`` (columns) and non-positive tets are rejected; a
+triangle pose is the inverse of the 2x2 rest edge matrix in the triangle's own
+orthonormal frame (e1 along x1-x0, e2 = n x e1) and degenerate triangles are
+rejected; Hex8 ``inv_J0`` / ``|det J0|`` are computed in float64 per Gauss
+point and stored as float32 (``builder.py:95-135``).
 """
 
 from __future__ import annotations
@@ -88,12 +94,81 @@ class Control:
         self.tet_activations = tet_activations
 
 
+def triangle_rest_data(x: np.ndarray, tris: np.ndarray):
+    """Rest pose ``inv(D)`` and area ``det(D)/2`` of triangles, D = [[e1.x10, e1.x20], [e2.x10, e2.x20]]
+    in the frame e1 = x10/|x10|, e2 = n x e1 (n the unit normal), in float64."""
+    tris = np.asarray(tris, np.int64).reshape(-1, 3)
+    x = np.asarray(x, np.float64)
+    x10 = x[tris[:, 1]] - x[tris[:, 0]]
+    x20 = x[tris[:, 2]] - x[tris[:, 0]]
+    n = np.cross(x10, x20)
+    nn = np.linalg.norm(n, axis=1, keepdims=True)
+    n = n / np.where(nn > 0, nn, 1.0)
+    e1 = x10 / np.maximum(np.linalg.norm(x10, axis=1, keepdims=True), 1e-300)
+    e2 = np.cross(n, e1)
+    e2 = e2 / np.maximum(np.linalg.norm(e2, axis=1, keepdims=True), 1e-300)
+    D = np.stack([np.stack([np.sum(e1 * x10, 1), np.sum(e1 * x20, 1)], 1),
+                  np.stack([np.sum(e2 * x10, 1), np.sum(e2 * x20, 1)], 1)], 1)
+    area = np.linalg.det(D) / 2.0 if len(D) else np.zeros(0)
+    poses = np.zeros_like(D)
+    ok = area > 0.0
+    if ok.any():
+        poses[ok] = np.linalg.inv(D[ok])
+    return poses, area
+
+
+class HashGrid:
+    """Marks a model as carrying a particle hash grid (Newton ``wp.HashGrid(dim_x, dim_y, dim_z)``).
+
+    The solver builds its own wrapped-bucket grid on the device from the
+    particle positions at every force evaluation; the dimensions here are
+    informational."""
+
+    def __init__(self, dim_x: int = 128, dim_y: int = 128, dim_z: int = 128):
+        self.dims = (int(dim_x), int(dim_y), int(dim_z))
+
+
+class Contacts:
+    """Soft-rigid contact list in the layout of Newton's ``Contacts.soft_contact_*``.
+
+    ``soft_contact_count`` is a device int32 tensor of shape [1] (read on the
+    device); the per-contact arrays have ``soft_contact_max`` entries: particle
+    [max] int32, body_pos / body_vel / normal [max, 3] float32 (world space)."""
+
+    def __init__(self, soft_contact_max: int, device="cuda"):
+        dev = torch.device(device)
+        self.soft_contact_max = int(soft_contact_max)
+        self.soft_contact_count = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.soft_contact_particle = torch.full((self.soft_contact_max,), -1, dtype=torch.int32, device=dev)
+        self.soft_contact_body_pos = torch.zeros((self.soft_contact_max, 3), dtype=torch.float32, device=dev)
+        self.soft_contact_body_vel = torch.zeros((self.soft_contact_max, 3), dtype=torch.float32, device=dev)
+        self.soft_contact_normal = torch.zeros((self.soft_contact_max, 3), dtype=torch.float32, device=dev)
+
+
 class Model:
-    """Finalised, device-resident model (the subset of Newton's ``Model`` the solver reads)."""
+    """Finalised, device-resident model (the subset of Newton's ``Model`` the solver reads).
+
+    Contact coefficients default to particle ke 1e3, kd 1e2, kf 1e2, mu 0.5,
+    cohesion 0 and soft-contact ke 1e3, kd 10, kf 1e3, mu 0.5; SolverFEM sets
+    ``particle_ke`` / ``particle_kd`` from ``self_contact_ke`` / ``self_contact_kd``."""
 
     def __init__(self, device: torch.device):
         self.device = torch.device(device)
         self.requires_grad = False
+        self.tri_indices = torch.zeros((0, 3), dtype=torch.int32, device=self.device)
+        self.tri_poses = torch.zeros((0, 2, 2), dtype=torch.float32, device=self.device)
+        self.tri_materials = torch.zeros((0, 5), dtype=torch.float32, device=self.device)
+        self.tri_areas = torch.zeros(0, dtype=torch.float32, device=self.device)
+        self.particle_grid = None
+        self.particle_ke = 1.0e3
+        self.particle_kd = 1.0e2
+        self.particle_kf = 1.0e2
+        self.particle_mu = 0.5
+        self.particle_cohesion = 0.0
+        self.soft_contact_ke = 1.0e3
+        self.soft_contact_kd = 10.0
+        self.soft_contact_kf = 1.0e3
+        self.soft_contact_mu = 0.5
 
     @property
     def particle_count(self) -> int:
@@ -109,7 +184,11 @@ class Model:
 
     @property
     def tri_count(self) -> int:
-        return 0
+        return int(self.tri_indices.shape[0])
+
+    @property
+    def particle_max_radius(self) -> float:
+        return float(self.particle_radius.max()) if self.particle_count else 0.0
 
     @property
     def scene_count(self) -> int:
@@ -138,6 +217,11 @@ class FEMBuilder:
     default_tet_k_mu = 1.0e3
     default_tet_k_lambda = 1.0e3
     default_tet_k_damp = 0.0
+    default_tri_ke = 100.0
+    default_tri_ka = 100.0
+    default_tri_kd = 10.0
+    default_tri_drag = 0.0
+    default_tri_lift = 0.0
 
     def __init__(self, gravity=(0.0, 0.0, -9.81), up_axis: str = "Z"):
         self.gravity = tuple(float(g) for g in gravity)
@@ -150,6 +234,8 @@ class FEMBuilder:
         self.tet_poses: list = []
         self.tet_materials: list = []
         self.tet_activations: list = []
+        self.tri_indices: list = []
+        self.tri_materials: list = []
         self.spring_indices: list = []
         self.spring_rest_length: list = []
         self.spring_stiffness: list = []
@@ -209,6 +295,20 @@ class FEMBuilder:
         self.tet_materials.append((float(k_mu), float(k_lambda), float(k_damp)))
         self.tet_activations.append(0.0)
         return volume
+
+    def add_triangle(self, i, j, k, tri_ke=None, tri_ka=None, tri_kd=None, tri_drag=None, tri_lift=None,
+                     **_ignored) -> float:
+        """Add a membrane triangle (materials ke, ka, kd, drag, lift); degenerate ones are skipped (returns area)."""
+        _, area = triangle_rest_data(np.asarray([self.particle_q[n] for n in (i, j, k)], np.float64),
+                                     np.array([[0, 1, 2]]))
+        if not area[0] > 0.0:
+            return 0.0
+        pick = lambda v, d: d if v is None else float(v)
+        self.tri_indices.append((int(i), int(j), int(k)))
+        self.tri_materials.append((pick(tri_ke, self.default_tri_ke), pick(tri_ka, self.default_tri_ka),
+                                   pick(tri_kd, self.default_tri_kd), pick(tri_drag, self.default_tri_drag),
+                                   pick(tri_lift, self.default_tri_lift)))
+        return float(area[0])
 
     def add_spring(self, i, j, ke, kd, control=0.0) -> None:
         """Linear spring with rest length from the current positions (Newton ``add_spring``)."""
@@ -290,6 +390,8 @@ class FEMBuilder:
         m.spring_stiffness = torch.tensor(np.asarray(self.spring_stiffness, np.float32), **f32)
         m.spring_damping = torch.tensor(np.asarray(self.spring_damping, np.float32), **f32)
         m.gravity = torch.tensor(np.asarray(self.gravity, np.float32), **f32)
+        _set_triangles(m, np.asarray(self.particle_q, np.float64).reshape(P, 3), self.tri_indices, self.tri_materials)
+        m.particle_grid = HashGrid() if P > 1 else None
         hexes = np.asarray(self.fem_hex_indices, np.int32).reshape(-1, 8)
         inv, det = hex_gauss_data(np.asarray(self.particle_q, np.float64).reshape(P, 3), hexes)
         m.fem = LinearFEMData(
@@ -305,12 +407,30 @@ class FEMBuilder:
         return m
 
 
+def _set_triangles(m: Model, x: np.ndarray, tris, materials) -> None:
+    tris = np.asarray(tris, np.int32).reshape(-1, 3)
+    poses, area = triangle_rest_data(x, tris)
+    if np.any(area <= 0.0):
+        raise ValueError("triangles must be non-degenerate")
+    mats = np.asarray(materials, np.float32).reshape(-1, 5) if len(tris) else np.zeros((0, 5), np.float32)
+    if mats.shape != (len(tris), 5):
+        raise ValueError("tri_materials must have shape (tri_count, 5): ke, ka, kd, drag, lift")
+    dev = m.device
+    m.tri_indices = torch.tensor(tris, dtype=torch.int32, device=dev)
+    m.tri_poses = torch.tensor(poses.astype(np.float32), dtype=torch.float32, device=dev)
+    m.tri_materials = torch.tensor(mats, dtype=torch.float32, device=dev)
+    m.tri_areas = torch.tensor(area.astype(np.float32), dtype=torch.float32, device=dev)
+
+
 def model_from_arrays(
     x,
     mass,
     *,
     tets=None,
     tet_materials=None,
+    tris=None,
+    tri_materials=None,
+    particle_grid=False,
     hexes=None,
     hex_materials=None,
     springs=None,
@@ -368,5 +488,8 @@ def model_from_arrays(
         torch.tensor(inv.astype(np.float32), **f32),
         torch.tensor(det.astype(np.float32), **f32),
     )
+    _set_triangles(m, x, np.zeros((0, 3), np.int32) if tris is None else tris,
+                   np.zeros((0, 5)) if tri_materials is None else tri_materials)
+    m.particle_grid = HashGrid() if particle_grid else None
     m.scene_offsets = None if scene_offsets is None else np.asarray(scene_offsets, np.int64)
     return m

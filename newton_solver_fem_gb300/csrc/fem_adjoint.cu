@@ -5,7 +5,8 @@
 // kernels give dL/dq, dL/dv (and dL/d activation, dL/d shear scale) of
 //   tet force      kernels.py:511-632 (+ activation 484-508)
 //   hex force      kernels.py:1481-1601
-//   springs        kernels.py:176-218
+//   springs        kernels.py:176-218 (+ bend torque 221-291)
+//   triangles      kernels.py:876-960
 //   ground         kernels.py:1132-1195
 //   damping        kernels.py:1289-1307
 // and of the elastic predictor rhs -= sum_j A_ij (v_j - v_i) plus the spring
@@ -16,6 +17,7 @@
 // regime of the differentiable workloads.
 // Element gradients go to per-element slots and are summed per node in a
 // fixed order, like the forward forces: no float atomics.
+#include "fem_generic.cuh"
 #include "fem_internal.cuh"
 #include "fem_math.cuh"
 
@@ -290,6 +292,69 @@ __global__ void hex_force_vjp_kernel(int H, const int* __restrict__ idx, const f
     }
 }
 
+__device__ __forceinline__ void seed(V3<Dual>& a, int k) {
+    if (k == 0) a.x.d = 1.0f;
+    else if (k == 1) a.y.d = 1.0f;
+    else a.z.d = 1.0f;
+}
+
+// Triangle VJP by forward-mode differentiation of the shared force: one dual
+// pass per input component (x0..x2, v0..v2) gives a Jacobian column, dotted
+// with the corners' force gradients.  Slots [corner][x-bar, v-bar].
+__global__ void tri_force_vjp_kernel(int Tri, const int* __restrict__ idx, const float4* __restrict__ pose,
+                                     const float* __restrict__ mat, const float4* __restrict__ q4,
+                                     const float4* __restrict__ v4, const float* __restrict__ g,
+                                     float4* __restrict__ grad) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= Tri) return;
+    int n[3];
+    float3 xs[3], vs[3], gs[3];
+    float m[5];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        n[c] = idx[3 * e + c];
+        xs[c] = xyz(q4[n[c]]);
+        vs[c] = xyz(v4[n[c]]);
+        gs[c] = ld3(g, n[c]);
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) m[k] = mat[5 * e + k];
+    const float4 Dm = pose[e];
+    float bar[18];  // [x0 x1 x2 v0 v1 v2] components
+    for (int dir = 0; dir < 18; ++dir) {
+        V3<Dual> x[3], v[3], f[3];
+        for (int c = 0; c < 3; ++c) {
+            x[c] = lift3<Dual>(xs[c]);
+            v[c] = lift3<Dual>(vs[c]);
+        }
+        seed(dir < 9 ? x[dir / 3] : v[(dir - 9) / 3], dir % 3);
+        triangle_force(x, v, Dm, m, f);
+        float acc = 0.0f;
+        for (int c = 0; c < 3; ++c) acc += gs[c].x * f[c].x.d + gs[c].y * f[c].y.d + gs[c].z * f[c].z.d;
+        bar[dir] = acc;
+    }
+    for (int c = 0; c < 3; ++c) {
+        grad[2 * (3 * (size_t)e + c)] = make_float4(bar[3 * c], bar[3 * c + 1], bar[3 * c + 2], 0.0f);
+        grad[2 * (3 * (size_t)e + c) + 1] = make_float4(bar[9 + 3 * c], bar[9 + 3 * c + 1], bar[9 + 3 * c + 2], 0.0f);
+    }
+}
+
+// VJP of one spring's bend torque wrt xij and vij (the torque enters node j
+// with + and node i with -): dual passes over the six inputs.
+__device__ void spring_torque_vjp(float3 xij, float3 vij, float3 dir0, float kt, float kwt, float3 tbar,
+                                  float3& xijb, float3& vijb) {
+    float bar[6];
+    for (int k = 0; k < 6; ++k) {
+        V3<Dual> x = lift3<Dual>(xij), v = lift3<Dual>(vij), out;
+        seed(k < 3 ? x : v, k % 3);
+        bar[k] = spring_torque_force(x, v, dir0, kt, kwt, out)
+                     ? tbar.x * out.x.d + tbar.y * out.y.d + tbar.z * out.z.d
+                     : 0.0f;
+    }
+    xijb = f3(bar[0], bar[1], bar[2]);
+    vijb = f3(bar[3], bar[4], bar[5]);
+}
+
 struct NodeVjpArgs {
     int P, T;
     const float4* q4;
@@ -304,6 +369,8 @@ struct NodeVjpArgs {
     const float* spring_rest;
     const float* spring_ke;
     const float* spring_kd;
+    const float* spring_dir;
+    float torque_ke, torque_kd;
     const float* mass;
     const float* inv_mass;
     const float* radius;
@@ -347,6 +414,13 @@ __global__ void node_vjp_kernel(NodeVjpArgs a) {
         dirb = dirb + vij * dcdtb;
         float3 vijb = dir * dcdtb;
         float3 xijb = (dirb - dir * dot3(dir, dirb)) * (1.0f / L) + dir * Lb;
+        if (a.spring_dir != nullptr) {
+            const float3 d0 = f3(a.spring_dir[3 * s], a.spring_dir[3 * s + 1], a.spring_dir[3 * s + 2]);
+            float3 txb, tvb;
+            spring_torque_vjp(xij, vij, d0, a.torque_ke, a.torque_kd, fsb, txb, tvb);
+            xijb = xijb + txb;
+            vijb = vijb + tvb;
+        }
         if (ent & 1) {
             xb = xb - xijb;
             vb = vb - vijb;
@@ -481,11 +555,14 @@ int fem_force_vjp(FemHandle* H, const float* q, const float* v, const float* act
         return fem::report(FEM_ERR_BAD_ARG, "fem_force_vjp: null argument");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
+    if (h.pcontact || h.sc_cap > 0)
+        return fem::report(FEM_ERR_UNSUPPORTED,
+                           "fem_force_vjp: particle and soft contacts are not differentiated (fixed-matrix contract)");
     AdjDeviceGuard g(H->device);
     cudaStream_t s = (cudaStream_t)stream;
-    if (h.elem_grad == nullptr && (h.T > 0 || h.H > 0)) {  // first call: adjoint scratch
+    if (h.elem_grad == nullptr && (h.T > 0 || h.H > 0 || h.Tri > 0)) {  // first call: adjoint scratch
         void* p = nullptr;
-        size_t n = 2 * (4 * (size_t)h.T + 8 * (size_t)h.H);
+        size_t n = 2 * (4 * (size_t)h.T + 8 * (size_t)h.H + 3 * (size_t)h.Tri);
         if (cudaError_t e = cudaMalloc(&p, n * sizeof(float4)); e != cudaSuccess) return fem::report_cuda(e);
         h.allocations.push_back(p);
         h.elem_grad = (float4*)p;
@@ -499,6 +576,10 @@ int fem_force_vjp(FemHandle* H, const float* q, const float* v, const float* act
         fem::hex_force_vjp_kernel<<<(int)((8 * (int64_t)h.H + 255) / 256), 256, 0, s>>>(
             h.H, h.hex_idx, h.hex_invJ, h.hex_detw, h.hex_mat, h.q4, h.v4, force_bar, h.min_stretch, h.max_stretch,
             h.elem_grad + 2 * 4 * (size_t)h.T);
+    if (err == cudaSuccess && h.Tri > 0)
+        fem::tri_force_vjp_kernel<<<(h.Tri + 127) / 128, 128, 0, s>>>(
+            h.Tri, h.tri_idx, h.tri_pose, h.tri_mat, h.q4, h.v4, force_bar,
+            h.elem_grad + 2 * (4 * (size_t)h.T + 8 * (size_t)h.H));
     if (err == cudaSuccess) err = cudaGetLastError();
     if (err == cudaSuccess) {
         fem::NodeVjpArgs a;
@@ -516,6 +597,9 @@ int fem_force_vjp(FemHandle* H, const float* q, const float* v, const float* act
         a.spring_rest = h.spring_rest;
         a.spring_ke = h.spring_ke;
         a.spring_kd = h.spring_kd;
+        a.spring_dir = h.spring_dir;
+        a.torque_ke = h.torque_ke;
+        a.torque_kd = h.torque_kd;
         a.mass = h.mass;
         a.inv_mass = h.inv_mass;
         a.radius = h.radius;

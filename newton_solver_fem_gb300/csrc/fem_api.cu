@@ -132,6 +132,37 @@ T* upload_plain(const std::vector<T>& v, std::vector<void*>& owned, cudaError_t&
     return (T*)p;
 }
 
+// Register (or clear, capacity 0) the caller's soft-contact list; grows the
+// per-contact scratch and allocates the per-node list heads on first use.
+int register_soft_contacts(Handle& h, const int32_t* count, const int32_t* particle, const float* body_pos,
+                           const float* body_vel, const float* normal, int32_t capacity) {
+    if (capacity < 0) return set_error(FEM_ERR_BAD_ARG, "soft contact capacity must be non-negative");
+    if (capacity > 0 && (!count || !particle || !body_pos || !body_vel || !normal))
+        return set_error(FEM_ERR_BAD_ARG, "soft contact arrays are required for a non-zero capacity");
+    if (capacity > 0 && h.P > 0) {
+        auto grab = [&](size_t bytes, void** out) {
+            cudaError_t e = cudaMalloc(out, bytes);
+            if (e == cudaSuccess) h.allocations.push_back(*out);
+            return e;
+        };
+        cudaError_t e = cudaSuccess;
+        if (h.sc_head == nullptr) e = grab(sizeof(int) * (size_t)h.P, (void**)&h.sc_head);
+        if (e == cudaSuccess && capacity > h.sc_alloc) {
+            e = grab(sizeof(int) * (size_t)capacity, (void**)&h.sc_next);
+            if (e == cudaSuccess) e = grab(sizeof(float4) * (size_t)capacity, (void**)&h.sc_force);
+            if (e == cudaSuccess) h.sc_alloc = capacity;
+        }
+        if (e != cudaSuccess) return cuda_status(e, &h);
+    }
+    h.sc_count = count;
+    h.sc_particle = particle;
+    h.sc_pos = body_pos;
+    h.sc_vel = body_vel;
+    h.sc_normal = normal;
+    h.sc_cap = capacity > 0 ? capacity : 0;
+    return FEM_OK;
+}
+
 // (Re)compute the PCG grid for the handle's kernel variant, the per-(CTA,
 // scene) segment tables of the deterministic reductions and the L2-resident
 // slice count.  Allocates (at construction and on a tuning change only).
@@ -207,8 +238,8 @@ const char* fem_status_string(int status) {
 int fem_create(const FemDesc* d, FemHandle** out) {
     if (d == nullptr || out == nullptr) return set_error(FEM_ERR_BAD_ARG, "null descriptor or output");
     *out = nullptr;
-    const int P = d->particle_count, T = d->tet_count, Hn = d->hex_count, S = d->spring_count;
-    if (P < 0 || T < 0 || Hn < 0 || S < 0) return set_error(FEM_ERR_BAD_ARG, "negative element count");
+    const int P = d->particle_count, T = d->tet_count, Hn = d->hex_count, S = d->spring_count, Tri = d->tri_count;
+    if (P < 0 || T < 0 || Hn < 0 || S < 0 || Tri < 0) return set_error(FEM_ERR_BAD_ARG, "negative element count");
     if (P > 0 && (d->particle_q == nullptr || d->particle_mass == nullptr || d->particle_inv_mass == nullptr))
         return set_error(FEM_ERR_BAD_ARG, "particle arrays are required");
     if (T > 0 && (d->tet_indices == nullptr || d->tet_poses == nullptr || d->tet_materials == nullptr))
@@ -219,12 +250,19 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     if (S > 0 && (d->spring_indices == nullptr || d->spring_rest_length == nullptr ||
                   d->spring_stiffness == nullptr || d->spring_damping == nullptr))
         return set_error(FEM_ERR_BAD_ARG, "spring arrays are required");
+    if (Tri > 0 && (d->tri_indices == nullptr || d->tri_poses == nullptr || d->tri_materials == nullptr))
+        return set_error(FEM_ERR_BAD_ARG, "triangle arrays are required");
+    const bool torque = S > 0 && d->spring_rest_direction != nullptr && d->torque_stiffness > 0.0f;
+    if (d->particle_contact && !(2.0f * d->particle_max_radius + d->particle_cohesion > 0.0f))
+        return set_error(FEM_ERR_BAD_ARG, "particle contact needs 2 max_radius + cohesion > 0");
     if (!(d->tolerance > 0.0f) || !std::isfinite(d->tolerance))
         return set_error(FEM_ERR_BAD_ARG, "linear_solver_tolerance must be finite and positive");
     if (d->maxiter < 0) return set_error(FEM_ERR_BAD_ARG, "linear_solver_maxiter must be non-negative");
     if (d->preconditioner != FEM_PRECOND_BLOCK_DIAG && d->preconditioner != FEM_PRECOND_DIAG)
         return set_error(FEM_ERR_UNSUPPORTED, "preconditioner must be block_diag or diag");
-    const int64_t ntrip = (int64_t)P + 2 * (int64_t)S + 16 * (int64_t)T + 64 * (int64_t)Hn;
+    const int64_t ntrip = (int64_t)P + 2 * (int64_t)S + 3 * (int64_t)Tri + 16 * (int64_t)T + 64 * (int64_t)Hn;
+    if (4 * (int64_t)T + 8 * (int64_t)Hn + 3 * (int64_t)Tri >= (int64_t)INT32_MAX)
+        return set_error(FEM_ERR_BAD_ARG, "problem too large for int32 element slots");
     if (ntrip >= (int64_t)INT32_MAX) return set_error(FEM_ERR_BAD_ARG, "problem too large for int32 triplet ids");
     for (int64_t k = 0; k < 4 * (int64_t)T; ++k)
         if (d->tet_indices[k] < 0 || d->tet_indices[k] >= P) return set_error(FEM_ERR_BAD_ARG, "tet index out of range");
@@ -233,6 +271,9 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     for (int64_t k = 0; k < 2 * (int64_t)S; ++k)
         if (d->spring_indices[k] >= P || d->spring_indices[k] < -1)
             return set_error(FEM_ERR_BAD_ARG, "spring index out of range");
+    for (int64_t k = 0; k < 3 * (int64_t)Tri; ++k)
+        if (d->tri_indices[k] < 0 || d->tri_indices[k] >= P)
+            return set_error(FEM_ERR_BAD_ARG, "triangle index out of range");
     std::vector<unsigned char> fixed_mask(P, 0);
     for (int k = 0; k < d->fixed_count; ++k) {
         int i = d->fixed_indices[k];
@@ -267,8 +308,11 @@ int fem_create(const FemDesc* d, FemHandle** out) {
             }
             return true;
         };
-        if (!same(d->tet_indices, 4, T) || !same(d->hex_indices, 8, Hn) || !same(d->spring_indices, 2, S))
+        if (!same(d->tet_indices, 4, T) || !same(d->hex_indices, 8, Hn) || !same(d->spring_indices, 2, S) ||
+            !same(d->tri_indices, 3, Tri))
             return set_error(FEM_ERR_BAD_ARG, "an element or spring couples two scenes");
+        if (d->particle_contact && nscenes > 1)
+            return set_error(FEM_ERR_UNSUPPORTED, "particle contact couples scenes; use one scene");
     }
 
     int device = 0;
@@ -282,6 +326,7 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     h.T = T;
     h.H = Hn;
     h.S = S;
+    h.Tri = Tri;
     h.nscenes = nscenes;
     h.ntrip = ntrip;
     h.dt = d->dt;
@@ -299,6 +344,19 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     h.maxiter = d->maxiter;
     h.tol = d->tolerance;
     h.nfixed = d->fixed_count;
+    h.torque_ke = d->torque_stiffness;
+    h.torque_kd = d->torque_damping;
+    h.pcontact = d->particle_contact != 0 && P > 1;
+    h.pke = d->particle_ke;
+    h.pkd = d->particle_kd;
+    h.pkf = d->particle_kf;
+    h.pmu = d->particle_mu;
+    h.pcoh = d->particle_cohesion;
+    h.pmaxr = d->particle_max_radius;
+    h.ske = d->soft_contact_ke;
+    h.skd = d->soft_contact_kd;
+    h.skf = d->soft_contact_kf;
+    h.smu = d->soft_contact_mu;
     fem::upload_hex_reference_table();
     fem::upload_hex_reference_table_adjoint();
 
@@ -307,16 +365,20 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     for (int t = 0; t < T; ++t)
         tet_empty[t] = d->tet_materials[3 * t] == 0.0f && d->tet_materials[3 * t + 1] == 0.0f &&
                        d->tet_materials[3 * t + 2] == 0.0f;
-    const int64_t off_spring = P, off_tet = (int64_t)P + 2 * (int64_t)S, off_hex = off_tet + 16 * (int64_t)T;
+    // triplet regions [P | 2S | 3Tri | 16T | 64H] (solver.py:312-321, 1015-1136)
+    const int64_t off_spring = P, off_tri = (int64_t)P + 2 * (int64_t)S, off_tet = off_tri + 3 * (int64_t)Tri,
+                  off_hex = off_tet + 16 * (int64_t)T;
     auto trip_rc = [&](int64_t t, int& r, int& c) {
         if (t < off_spring) {
             r = c = (int)t;
-        } else if (t < off_tet) {
+        } else if (t < off_tri) {
             int64_t k = t - off_spring;
             int s = (int)(k >> 1);
             int a = d->spring_indices[2 * s], bb = d->spring_indices[2 * s + 1];
             if (k & 1) { r = bb; c = a; } else { r = a; c = bb; }
             if (r < 0 || c < 0) r = c = -1;
+        } else if (t < off_tet) {
+            r = c = d->tri_indices[t - off_tri];
         } else if (t < off_hex) {
             int64_t k = t - off_tet;
             int e = (int)(k >> 4), ab = (int)(k & 15);
@@ -429,6 +491,7 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     std::vector<int> elem_ptr(P + 1, 0), spring_ptr(P + 1, 0);
     for (int64_t k = 0; k < 4 * (int64_t)T; ++k) elem_ptr[d->tet_indices[k] + 1]++;
     for (int64_t k = 0; k < 8 * (int64_t)Hn; ++k) elem_ptr[d->hex_indices[k] + 1]++;
+    for (int64_t k = 0; k < 3 * (int64_t)Tri; ++k) elem_ptr[d->tri_indices[k] + 1]++;
     for (int s = 0; s < S; ++s) {
         int a = d->spring_indices[2 * s], bb = d->spring_indices[2 * s + 1];
         if (a >= 0) spring_ptr[a + 1]++;
@@ -443,6 +506,8 @@ int fem_create(const FemDesc* d, FemHandle** out) {
         std::vector<int> pos(elem_ptr.begin(), elem_ptr.end() - 1);
         for (int64_t k = 0; k < 4 * (int64_t)T; ++k) elem_ent[pos[d->tet_indices[k]]++] = (int)k;
         for (int64_t k = 0; k < 8 * (int64_t)Hn; ++k) elem_ent[pos[d->hex_indices[k]]++] = (int)(4 * (int64_t)T + k);
+        const int64_t tri0 = 4 * (int64_t)T + 8 * (int64_t)Hn;
+        for (int64_t k = 0; k < 3 * (int64_t)Tri; ++k) elem_ent[pos[d->tri_indices[k]]++] = (int)(tri0 + k);
         std::vector<int> sp(spring_ptr.begin(), spring_ptr.end() - 1);
         for (int s = 0; s < S; ++s) {
             int a = d->spring_indices[2 * s], bb = d->spring_indices[2 * s + 1];
@@ -475,11 +540,25 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     h.spring_rest = b.upload(d->spring_rest_length, S);
     h.spring_ke = b.upload(d->spring_stiffness, S);
     h.spring_kd = b.upload(d->spring_damping, S);
+    if (torque) h.spring_dir = b.upload(d->spring_rest_direction, 3 * (size_t)S);
+    h.tri_idx = b.upload(d->tri_indices, 3 * (size_t)Tri);
+    h.tri_pose = reinterpret_cast<float4*>(b.upload(d->tri_poses, 4 * (size_t)Tri));
+    h.tri_mat = b.upload(d->tri_materials, 5 * (size_t)Tri);
+    if (h.pcontact) {
+        h.grid_dim = fem::particle_grid_dim(P);
+        const int64_t nb = (int64_t)h.grid_dim * h.grid_dim * h.grid_dim;
+        h.grid_count = b.alloc<int>((size_t)nb);
+        h.grid_start = b.alloc<int>((size_t)nb + 1);
+        h.grid_part = b.alloc<int>((size_t)(nb + 4095) / 4096);
+        h.grid_items = b.alloc<int>(P);
+        h.cell_of = b.alloc<int>(P);
+        h.pforce = b.alloc<float4>(P);
+    }
     h.node_elem_ptr = b.upload(elem_ptr);
     h.node_elem_ent = b.upload(elem_ent);
     h.node_spring_ptr = b.upload(spring_ptr);
     h.node_spring_ent = b.upload(spring_ent);
-    h.elem_force = b.alloc<float4>(4 * (size_t)T + 8 * (size_t)Hn);
+    h.elem_force = b.alloc<float4>(4 * (size_t)T + 8 * (size_t)Hn + 3 * (size_t)Tri);
     h.q4 = b.alloc<float4>(P);
     h.v4 = b.alloc<float4>(P);
     h.trip.a = b.alloc<float4>((size_t)ntrip);
@@ -606,7 +685,7 @@ int fem_step(FemHandle* H, float* q_in, float* v_in, float* q_out, float* v_out,
     cudaError_t err = fem::launch_node_prepare(h, q_in, v_in, true, true, true, s);
     if (err == cudaSuccess) err = fem::launch_element_forces(h, activations, s);
     if (err == cudaSuccess)
-        err = fem::launch_node_forces(h, external_forces, gravity, dt, 0x3f, true, f_ws, s);
+        err = fem::launch_node_forces(h, external_forces, gravity, dt, FEM_TERM_ALL, true, f_ws, s);
     bool timed = false;
     if (err == cudaSuccess && h.timing) {
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -624,6 +703,13 @@ int fem_step(FemHandle* H, float* q_in, float* v_in, float* q_out, float* v_out,
     if (err == cudaSuccess) err = fem::launch_pcg(h, dt, 1, q_out, v_out, f_ws, s);
     if (timed) cudaEventRecord(h.timing_events.back(), s);
     return cuda_status(err, &h);
+}
+
+int fem_set_soft_contacts(FemHandle* H, const int32_t* count, const int32_t* particle, const float* body_pos,
+                          const float* body_vel, const float* normal, int32_t capacity) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "fem_set_soft_contacts: null handle");
+    DeviceGuard g(H->device);
+    return register_soft_contacts(H->h, count, particle, body_pos, body_vel, normal, capacity);
 }
 
 int fem_set_timing(FemHandle* H, int32_t enable) {
@@ -663,7 +749,7 @@ int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, voi
     if (h.precond != FEM_PRECOND_BLOCK_DIAG)
         return set_error(FEM_ERR_BAD_ARG, "persistent topology updates require the block_diag preconditioner");
     if (d->particle_count != h.P || d->tet_count != h.T || d->hex_count != h.H || d->spring_count != h.S ||
-        std::max(1, d->scene_count) != h.nscenes || d->fixed_count != h.nfixed)
+        d->tri_count != h.Tri || std::max(1, d->scene_count) != h.nscenes || d->fixed_count != h.nfixed)
         return set_error(FEM_ERR_BAD_ARG, "topology updates must preserve the model's capacities");
     DeviceGuard g(H->device);
     cudaError_t e = cudaDeviceSynchronize();  // nothing may still use the storage being replaced
@@ -684,7 +770,8 @@ int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, voi
     n.grid_cap = h.grid_cap;
     n.timing = h.timing;
     n.mu_scale = h.mu_scale;
-    code = configure_launch(n);
+    code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
+    if (code == FEM_OK) code = configure_launch(n);
     if (code != FEM_OK) {
         fem_destroy(fresh);
         return code;

@@ -2,12 +2,17 @@
 //   node_prepare      fixed-node restore + float4 packing of q, v and the CG warm start
 //   tet_force         Stable Neo-Hookean Tet4 force + Rayleigh damping (+ activation), per element
 //   hex_force         Q1 Hex8 force, 8 lanes per element (one per Gauss point)
-//   node_forces       deterministic element->node gather + springs, ground, gravity, damping,
-//                     and the h-scaled sum in the reference's term order
-//   constant_blocks   mass + spring diagonal and spring off-diagonal triplet blocks
+//   tri_force         triangle membrane + area + drag/lift force, per element
+//   node_forces       deterministic element->node gather + springs (with bend torque), particle
+//                     and soft contacts, ground, gravity, damping, and the h-scaled sum in the
+//                     reference's term order
+//   constant_blocks   mass + spring diagonal, spring off-diagonal and lumped triangle blocks
 //   tet_tangent       16 PSD blocks per tet (per-tet factors staged in shared memory)
 //   hex_tangent       64 PSD blocks per hex (Gauss-point data computed once per element)
 // No float atomics anywhere: every sum runs in a fixed order.
+#include <climits>
+
+#include "fem_generic.cuh"
 #include "fem_internal.cuh"
 #include "fem_math.cuh"
 
@@ -212,8 +217,31 @@ __global__ void __launch_bounds__(256, 3) hex_force_kernel(int H, const int* __r
     if (live) out[8 * h + g] = f4(-mine);
 }
 
+// Reference kernels.py:876-960: one thread per triangle writes its three
+// corner forces to the element-force slots 3e..3e+2 (after the Tet4/Hex8 slots).
+__global__ void tri_force_kernel(int Tri, const int* __restrict__ idx, const float4* __restrict__ pose,
+                                 const float* __restrict__ mat, const float4* __restrict__ q4,
+                                 const float4* __restrict__ v4, float4* __restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= Tri) return;
+    V3<float> x[3], v[3], f[3];
+    float m[5];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int n = idx[3 * e + c];
+        const float4 qn = q4[n], vn = v4[n];
+        x[c] = v3(qn.x, qn.y, qn.z);
+        v[c] = v3(vn.x, vn.y, vn.z);
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) m[k] = mat[5 * e + k];
+    triangle_force(x, v, pose[e], m, f);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[3 * e + c] = make_float4(f[c].x, f[c].y, f[c].z, 0.0f);
+}
+
 struct NodeForceArgs {
-    int P, T;
+    int P, T, H;
     const float4* q4;
     const float4* v4;
     const int* elem_ptr;
@@ -225,6 +253,12 @@ struct NodeForceArgs {
     const float* spring_rest;
     const float* spring_ke;
     const float* spring_kd;
+    const float* spring_dir;  // rest directions when the bend torque is active
+    float torque_ke, torque_kd;
+    const float4* pforce;     // particle-contact force per node, or null
+    const int* sc_head;       // soft-contact list per node, or null
+    const int* sc_next;
+    const float4* sc_force;
     const float* mass;
     const float* inv_mass;
     const float* radius;
@@ -242,13 +276,15 @@ struct NodeForceArgs {
 };
 
 // Reference solver.py:542-589 (term order), kernels.py:176-218 (springs),
-// 1132-1195 (ground), 1273-1307 (gravity, damping).
+// 221-291 (bend torque), 1132-1195 (ground), 1198-1261 (soft contacts),
+// 1273-1307 (gravity, damping).  Term order: spring, tet, hex, tri, particle,
+// ground, soft contact, gravity, damping.
 __global__ void node_forces_kernel(NodeForceArgs a) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.P) return;
     float3 xi = xyz(a.q4[i]), vi = xyz(a.v4[i]);
     float3 zero = f3(0.f, 0.f, 0.f);
-    float3 fs = zero, ft = zero, fh = zero, fg = zero, fgr = zero, fd = zero;
+    float3 fs = zero, ft = zero, fh = zero, ftri = zero, fp = zero, fg = zero, fsc = zero, fgr = zero, fd = zero;
     // The incident springs and element corners are read kSpringBatch /
     // kCornerBatch at a time (ids, then the data they index) before any is
     // added, so that many independent loads are in flight; the sums keep the
@@ -288,12 +324,20 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
                 const float dcdt = dot3(dir, vij[u]);
                 const float3 f = dir * (ke[u] * c + kd[u] * dcdt);
                 fs = (ent[u] & 1) ? fs + f : fs - f;
+                if (a.spring_dir != nullptr) {  // kernels.py:266-291
+                    const int sp = ent[u] >> 1;
+                    const float3 d0 = f3(a.spring_dir[3 * sp], a.spring_dir[3 * sp + 1], a.spring_dir[3 * sp + 2]);
+                    V3<float> tq;
+                    if (spring_torque_force(v3(xij[u].x, xij[u].y, xij[u].z), v3(vij[u].x, vij[u].y, vij[u].z), d0,
+                                            a.torque_ke, a.torque_kd, tq))
+                        fs = (ent[u] & 1) ? fs + f3(tq.x, tq.y, tq.z) : fs - f3(tq.x, tq.y, tq.z);
+                }
             }
         }
     }
-    if (a.terms & (FEM_TERM_TET | FEM_TERM_HEX)) {
+    if (a.terms & (FEM_TERM_TET | FEM_TERM_HEX | FEM_TERM_TRI)) {
         constexpr int kCornerBatch = 8;
-        const int tet_end = 4 * a.T;
+        const int tet_end = 4 * a.T, hex_end = 4 * a.T + 8 * a.H;
         const int e1 = a.elem_ptr[i + 1];
         for (int e0 = a.elem_ptr[i]; e0 < e1; e0 += kCornerBatch) {
             int ent[kCornerBatch];
@@ -307,12 +351,15 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
                 if (ent[u] < 0) continue;
                 if (ent[u] < tet_end) {
                     if (a.terms & FEM_TERM_TET) ft = ft + f[u];
-                } else if (a.terms & FEM_TERM_HEX) {
-                    fh = fh + f[u];
+                } else if (ent[u] < hex_end) {
+                    if (a.terms & FEM_TERM_HEX) fh = fh + f[u];
+                } else if (a.terms & FEM_TERM_TRI) {
+                    ftri = ftri + f[u];
                 }
             }
         }
     }
+    if ((a.terms & FEM_TERM_PARTICLE) && a.pforce != nullptr) fp = xyz(a.pforce[i]);
     bool active = (a.flags[i] & 1) != 0;
     float3 grav = f3(a.gravity[0], a.gravity[1], a.gravity[2]);
     if ((a.terms & FEM_TERM_GROUND) && a.has_ground && active) {
@@ -335,6 +382,19 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
             fg = zero - n * fn - vt * ftan;
         }
     }
+    if ((a.terms & FEM_TERM_SOFT_CONTACT) && a.sc_head != nullptr) {
+        // the list holds this node's penetrating contacts in arbitrary order: add
+        // them in ascending contact id (repeated minimum search, lists are short)
+        int last = -1;
+        for (;;) {
+            int next = INT_MAX;
+            for (int c = a.sc_head[i]; c >= 0; c = a.sc_next[c])
+                if (c > last && c < next) next = c;
+            if (next == INT_MAX) break;
+            fsc = fsc + xyz(a.sc_force[next]);
+            last = next;
+        }
+    }
     if ((a.terms & FEM_TERM_GRAVITY) && active) {
         float m = a.mass[i];
         fgr = f3(grav.x * m, grav.y * m, grav.z * m);
@@ -348,12 +408,15 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
         f = fs * h;
         f = f + ft * h;
         f = f + fh * h;
+        f = f + ftri * h;
+        f = f + fp * h;
         f = f + fg * h;
+        f = f + fsc * h;
         f = f + fgr * h;
         f = f + fd * h;
         if (a.ext != nullptr) f = f + load3(a.ext, i) * h;
     } else {
-        f = fs + ft + fh + fg + fgr + fd;
+        f = fs + ft + fh + ftri + fp + fg + fsc + fgr + fd;
     }
     store3(a.out, i, f);
 }
@@ -381,6 +444,23 @@ __global__ void constant_offdiag_kernel(int P, int S, const float* __restrict__ 
     float neg_off = -(dt * kd[s] + dt * dt * ke[s]);
     const float o[9] = {neg_off, 0.f, 0.f, 0.f, neg_off, 0.f, 0.f, 0.f, neg_off};
     for (int k = 0; k < 2; ++k) store_block(vals, (int64_t)P + 2 * (int64_t)s + k, o);
+}
+
+// Reference kernels.py:963-1012: h^2 (mu + lambda) A_rest / 3 on each vertex's
+// diagonal (zero blocks for a degenerate rest triangle), position independent.
+__global__ void constant_tri_kernel(int Tri, const float4* __restrict__ pose, const float* __restrict__ mat, float dt,
+                                    int64_t trip_off, TripletPlanes vals) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= Tri) return;
+    const float4 Dm = pose[e];
+    const float inv_rest_area = (Dm.x * Dm.w - Dm.y * Dm.z) * 2.0f;
+    float d = 0.0f;
+    if (inv_rest_area > 0.0f) {
+        const float rest_area = 1.0f / inv_rest_area;
+        d = dt * dt * (mat[5 * e] * rest_area + mat[5 * e + 1] * rest_area) / 3.0f;
+    }
+    const float o[9] = {d, 0.f, 0.f, 0.f, d, 0.f, 0.f, 0.f, d};
+    for (int c = 0; c < 3; ++c) store_block(vals, trip_off + 3 * (int64_t)e + c, o);
 }
 
 constexpr int kTetTangentThreads = 128;
@@ -584,8 +664,6 @@ __global__ void __launch_bounds__(256) hex_tangent_kernel(int H, const int* __re
     store_block(vals, trip_off + 64 * (int64_t)h + 8 * ra + cb, K);
 }
 
-inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
-
 }  // namespace
 
 void upload_hex_reference_table() {
@@ -636,6 +714,9 @@ cudaError_t launch_element_forces(Handle& h, const float* activations, cudaStrea
             h.H, h.hex_idx, h.hex_invJ, h.hex_detw, h.hex_mat, h.q4, h.v4, h.min_stretch, h.max_stretch,
             h.elem_force + 4 * (int64_t)h.T);
     }
+    if (h.Tri > 0)
+        tri_force_kernel<<<blocks_for(h.Tri, 128), 128, 0, s>>>(h.Tri, h.tri_idx, h.tri_pose, h.tri_mat, h.q4, h.v4,
+                                                                h.elem_force + 4 * (int64_t)h.T + 8 * (int64_t)h.H);
     return cudaGetLastError();
 }
 
@@ -643,8 +724,25 @@ cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity
                                float* out, cudaStream_t s) {
     if (h.P == 0) return cudaSuccess;
     NodeForceArgs a;
+    a.pforce = nullptr;
+    a.sc_head = nullptr;
+    a.sc_next = nullptr;
+    a.sc_force = nullptr;
+    if ((terms & FEM_TERM_PARTICLE) && h.pcontact) {
+        cudaError_t err = launch_particle_contacts(h, s);
+        if (err != cudaSuccess) return err;
+        a.pforce = h.pforce;
+    }
+    if ((terms & FEM_TERM_SOFT_CONTACT) && h.sc_cap > 0) {
+        cudaError_t err = launch_soft_contacts(h, s);
+        if (err != cudaSuccess) return err;
+        a.sc_head = h.sc_head;
+        a.sc_next = h.sc_next;
+        a.sc_force = h.sc_force;
+    }
     a.P = h.P;
     a.T = h.T;
+    a.H = h.H;
     a.q4 = h.q4;
     a.v4 = h.v4;
     a.elem_ptr = h.node_elem_ptr;
@@ -656,6 +754,9 @@ cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity
     a.spring_rest = h.spring_rest;
     a.spring_ke = h.spring_ke;
     a.spring_kd = h.spring_kd;
+    a.spring_dir = h.spring_dir;
+    a.torque_ke = h.torque_ke;
+    a.torque_kd = h.torque_kd;
     a.mass = h.mass;
     a.inv_mass = h.inv_mass;
     a.radius = h.radius;
@@ -684,11 +785,14 @@ cudaError_t launch_constant_blocks(Handle& h, float dt, cudaStream_t s) {
     if (h.S > 0)
         constant_offdiag_kernel<<<blocks_for(h.S, 256), 256, 0, s>>>(h.P, h.S, h.spring_ke, h.spring_kd, dt,
                                                                      h.trip);
+    if (h.Tri > 0)
+        constant_tri_kernel<<<blocks_for(h.Tri, 256), 256, 0, s>>>(h.Tri, h.tri_pose, h.tri_mat, dt,
+                                                                   (int64_t)h.P + 2 * (int64_t)h.S, h.trip);
     return cudaGetLastError();
 }
 
 cudaError_t launch_element_tangent(Handle& h, float dt, cudaStream_t s) {
-    int64_t tet_off = (int64_t)h.P + 2 * (int64_t)h.S;
+    int64_t tet_off = tet_triplet_offset(h);
     if (h.T > 0)
         tet_tangent_kernel<<<blocks_for(h.T, kTetTangentThreads), kTetTangentThreads, 0, s>>>(
             h.T, h.tet_idx, h.tet_pose, h.tet_mat, h.mu_scale, h.q4, h.min_stretch, h.max_stretch, dt, tet_off,

@@ -105,7 +105,7 @@ struct PcgArgs {
 
 struct Handle {
     // sizes
-    int P = 0, T = 0, H = 0, S = 0, nfixed = 0, nscenes = 1;
+    int P = 0, T = 0, H = 0, S = 0, Tri = 0, nfixed = 0, nscenes = 1;
     int64_t ntrip = 0, nnzb = 0, nsell = 0;
     int nslices = 0;
     // options
@@ -142,18 +142,44 @@ struct Handle {
     float* hex_detw = nullptr;  // [H*8]
     float* hex_mat = nullptr;   // [H*3]
     const float* mu_scale = nullptr;  // optional caller-owned per-tet shear scale [T]
-    float4* elem_grad = nullptr;      // adjoint scratch [2 * (4T + 8H)], allocated on first VJP
+    float4* elem_grad = nullptr;      // adjoint scratch [2 * (4T + 8H + 3Tri)], allocated on first VJP
+    int* tri_idx = nullptr;     // [Tri*3]
+    float4* tri_pose = nullptr; // [Tri] (Dm00, Dm01, Dm10, Dm11)
+    float* tri_mat = nullptr;   // [Tri*5] (ke, ka, kd, drag, lift)
     int* spring_idx = nullptr;  // [2S]
     float* spring_rest = nullptr;
     float* spring_ke = nullptr;
     float* spring_kd = nullptr;
+    float* spring_dir = nullptr;  // [3S] rest directions when the bend torque is active, else null
+    float torque_ke = 0.f, torque_kd = 0.f;
+    // particle-particle contact (hash grid rebuilt at every force evaluation)
+    int pcontact = 0;
+    float pke = 0.f, pkd = 0.f, pkf = 0.f, pmu = 0.f, pcoh = 0.f, pmaxr = 0.f;
+    int grid_dim = 0;              // buckets per axis (power of two); grid_dim^3 buckets
+    int* grid_count = nullptr;     // [nb] particles per bucket (zero between evaluations)
+    int* grid_start = nullptr;     // [nb+1] exclusive scan of grid_count
+    int* grid_part = nullptr;      // scan block sums
+    int* grid_items = nullptr;     // [P] particle ids by bucket, ascending within a bucket
+    int* cell_of = nullptr;        // [P] bucket of each active particle or -1
+    float4* pforce = nullptr;      // [P] particle-contact force
+    // soft-rigid contacts (caller-owned list registered per step)
+    float ske = 0.f, skd = 0.f, skf = 0.f, smu = 0.f;
+    const int* sc_count = nullptr;
+    const int* sc_particle = nullptr;
+    const float* sc_pos = nullptr;
+    const float* sc_vel = nullptr;
+    const float* sc_normal = nullptr;
+    int sc_cap = 0, sc_alloc = 0;
+    int* sc_head = nullptr;        // [P] first contact of each particle's list or -1
+    int* sc_next = nullptr;        // [sc_alloc]
+    float4* sc_force = nullptr;    // [sc_alloc]
     // incidence
     int* node_elem_ptr = nullptr;  // [P+1]
     int* node_elem_ent = nullptr;  // element-force slots
     int* node_spring_ptr = nullptr;
     int* node_spring_ent = nullptr;
     // per-step scratch
-    float4* elem_force = nullptr;  // [4T + 8H]
+    float4* elem_force = nullptr;  // [4T + 8H + 3Tri]
     float4* q4 = nullptr;
     float4* v4 = nullptr;
     // assembly
@@ -226,6 +252,15 @@ cudaError_t launch_element_forces(Handle& h, const float* activations, cudaStrea
 cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity, float dt, int terms, bool scale_by_dt,
                                float* out, cudaStream_t s);
 cudaError_t launch_constant_blocks(Handle& h, float dt, cudaStream_t s);
+inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
+// first triplet of the Tet4 region: [P | 2S | 3Tri | 16T | 64H]
+inline int64_t tet_triplet_offset(const Handle& h) {
+    return (int64_t)h.P + 2 * (int64_t)h.S + 3 * (int64_t)h.Tri;
+}
+// --- launchers (fem_contacts.cu) ---
+int particle_grid_dim(int P);
+cudaError_t launch_particle_contacts(Handle& h, cudaStream_t s);  // grid build + per-particle force into h.pforce
+cudaError_t launch_soft_contacts(Handle& h, cudaStream_t s);      // per-contact force + per-particle lists
 cudaError_t launch_element_tangent(Handle& h, float dt, cudaStream_t s);
 // --- launchers (fem_assembly.cu) ---
 cudaError_t launch_gather(Handle& h, cudaStream_t s);

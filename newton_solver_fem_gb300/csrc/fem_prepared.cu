@@ -220,7 +220,7 @@ int fem_prepare(FemHandle* H, const FemPreparedWs* w, const float* q_in, const f
     cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess) err = fem::launch_element_forces(h, activations, s);
     if (err == cudaSuccess)
-        err = fem::launch_node_forces(h, external_forces, gravity, dt, 0x3f, true, w->impulse, s);
+        err = fem::launch_node_forces(h, external_forces, gravity, dt, FEM_TERM_ALL, true, w->impulse, s);
     if (err == cudaSuccess && h.nslices > 0) {
         fem::predictor_diag_kernel<<<fem::blocks((int64_t)h.nslices * 32, 256), 256, 0, s>>>(
             h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.scol, h.v4, w->predictor,

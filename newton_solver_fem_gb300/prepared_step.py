@@ -80,6 +80,7 @@ class PreparedFEMStep:
         if external_forces is not None:
             self._vectors(external_forces, "external_forces")
         act = self.solver._activations(control)
+        self.solver._register_contacts(contacts)
         self._revision = None
         lib = self.solver._lib
         self._call(lib.fem_prepare, ctypes.byref(self._ws), state_in.particle_q.data_ptr(),

@@ -12,10 +12,12 @@ model's CUDA device, enqueued on the current torch stream; tensors are only
 buffers.  There is no CPU path: a CPU model is rejected.
 
 Implemented hot-path options: ``solver_type="cg"`` with ``preconditioner_type``
-``"block_diag"`` or ``"diag"``; Tet4, Hex8, springs, analytic ground, gravity,
-linear damping, tet activations, fixed nodes, batched independent scenes
-(``model.scene_offsets``).  Other Krylov types, triangles, particle-particle
-contact, torque springs and soft/surface contacts are outside this path.
+``"block_diag"`` or ``"diag"``; Tet4, Hex8, triangle membranes, springs with
+the optional bend torque, hash-grid particle-particle contact, soft-rigid
+contacts (``contacts.soft_contact_*``), analytic ground, gravity, linear
+damping, tet activations, fixed nodes, batched independent scenes
+(``model.scene_offsets``).  Other Krylov types and the mesh-BVH surface
+contacts are outside this path.
 """
 
 from __future__ import annotations
@@ -112,8 +114,17 @@ class SolverFEM:
             raise NotImplementedError(f"solver_type={solver_type!r}: the GB300 hot path implements 'cg'")
         if preconditioner_type not in ("block_diag", "diag"):
             raise NotImplementedError(f"preconditioner_type={preconditioner_type!r} is not implemented")
-        if torque_stiffness > 0.0 and spring_rest_direction is not None:
-            raise NotImplementedError("spring bend torque is outside the GB300 hot path")
+        self.torque_stiffness = float(torque_stiffness)
+        self.torque_damping = float(torque_damping)
+        if spring_rest_direction is None:
+            self.spring_rest_direction = np.zeros((model.spring_count, 3), np.float32)
+        else:
+            srd = spring_rest_direction
+            srd = srd.detach().cpu().numpy() if isinstance(srd, torch.Tensor) else np.asarray(srd)
+            if srd.shape != (model.spring_count, 3):
+                raise ValueError(f"spring_rest_direction shape {srd.shape} != (spring_count={model.spring_count}, 3)")
+            self.spring_rest_direction = np.ascontiguousarray(srd, dtype=np.float32)
+        self._torque = self.torque_stiffness > 0.0 and spring_rest_direction is not None and model.spring_count > 0
         if differentiable:
             raise NotImplementedError("use newton_solver_fem_gb300.adjoint for differentiable rollouts")
         if tet_volume_weights is not None:
@@ -139,6 +150,11 @@ class SolverFEM:
         self._ground_plane = None if ground_plane is None else tuple(float(v) for v in ground_plane)
         model.particle_ke = float(self_contact_ke)
         model.particle_kd = float(self_contact_kd)
+        # solver.py:1477-1488: the hash-grid contact runs only with a positive stiffness,
+        # more than one particle, a positive maximum radius and a model particle grid
+        self._particle_contact = (model.particle_ke > 0.0 and model.particle_count > 1 and
+                                  model.particle_max_radius > 0.0 and getattr(model, "particle_grid", None) is not None)
+        self._contacts_key = None
         self._lib = _lib.load()
         self._handle = ctypes.c_void_p()
         self._revision = 0  # matrix revision (refresh_tangent, rebuild_element_blocks, model changes)
@@ -165,8 +181,9 @@ class SolverFEM:
     def _topology_signature(self):
         """Capacities and storage of the arrays a topology refresh may rewrite in place."""
         m = self.model
-        arrays = (m.particle_mass, m.particle_inv_mass, m.particle_flags, m.tet_indices, m.tet_poses, m.tet_materials)
-        counts = (m.particle_count, m.tet_count, self.hex_count, m.spring_count)
+        arrays = (m.particle_mass, m.particle_inv_mass, m.particle_flags, m.tet_indices, m.tet_poses, m.tet_materials,
+                  m.tri_indices, m.tri_poses, m.tri_materials)
+        counts = (m.particle_count, m.tet_count, self.hex_count, m.spring_count, m.tri_count)
         return counts, tuple(None if a is None else (a.data_ptr(), tuple(a.shape)) for a in arrays)
 
     def _descriptor(self, model, fixed, maxiter, tolerance):
@@ -208,6 +225,22 @@ class SolverFEM:
             d.spring_rest_length = host(model.spring_rest_length, np.float32)
             d.spring_stiffness = host(model.spring_stiffness, np.float32)
             d.spring_damping = host(model.spring_damping, np.float32)
+        if model.tri_count:
+            d.tri_count = model.tri_count
+            d.tri_indices = host(model.tri_indices, np.int32)
+            d.tri_poses = host(model.tri_poses, np.float32)
+            d.tri_materials = host(model.tri_materials, np.float32)
+        if self._torque:
+            d.spring_rest_direction = host(self.spring_rest_direction, np.float32)
+            d.torque_stiffness = self.torque_stiffness
+            d.torque_damping = self.torque_damping
+        d.particle_contact = int(self._particle_contact)
+        d.particle_ke, d.particle_kd = float(model.particle_ke), float(model.particle_kd)
+        d.particle_kf, d.particle_mu = float(model.particle_kf), float(model.particle_mu)
+        d.particle_cohesion = float(model.particle_cohesion)
+        d.particle_max_radius = float(model.particle_max_radius)
+        d.soft_contact_ke, d.soft_contact_kd = float(model.soft_contact_ke), float(model.soft_contact_kd)
+        d.soft_contact_kf, d.soft_contact_mu = float(model.soft_contact_kf), float(model.soft_contact_mu)
         d.fixed_indices = host(fixed, np.int32) if fixed.size else None
         d.fixed_count = int(fixed.size)
         offsets = getattr(model, "scene_offsets", None)
@@ -323,6 +356,7 @@ class SolverFEM:
                         ("state_out.particle_qd", state_out.particle_qd), ("state_in.particle_f", state_in.particle_f)):
             _f32(t, (P, 3), name, dev)
         act = self._activations(control)
+        self._register_contacts(contacts)
         code = self._lib.fem_step(
             self._handle, state_in.particle_q.data_ptr(), state_in.particle_qd.data_ptr(),
             state_out.particle_q.data_ptr(), state_out.particle_qd.data_ptr(), state_in.particle_f.data_ptr(),
@@ -332,6 +366,40 @@ class SolverFEM:
             stats = self.stats()
             self.last_cg_iters = stats["max_iterations"]
         return state_out
+
+    def _register_contacts(self, contacts) -> None:
+        """Point the library at ``contacts.soft_contact_*`` (or clear it) for the following launches.
+
+        Re-registers only when the arrays change; a larger capacity than any
+        registered before allocates scratch, which cannot happen under capture.
+        """
+        if contacts is None or not hasattr(contacts, "soft_contact_count"):
+            key = None
+        else:
+            cap = int(contacts.soft_contact_max)
+            arrays = (contacts.soft_contact_count, contacts.soft_contact_particle, contacts.soft_contact_body_pos,
+                      contacts.soft_contact_body_vel, contacts.soft_contact_normal)
+            shapes = ((1,), (cap,), (cap, 3), (cap, 3), (cap, 3))
+            dtypes = (torch.int32, torch.int32, torch.float32, torch.float32, torch.float32)
+            for a, shape, dtype in zip(arrays, shapes, dtypes):
+                if not isinstance(a, torch.Tensor) or a.dtype != dtype or tuple(a.shape) != shape or \
+                        a.device != self.device or not a.is_contiguous():
+                    raise ValueError("contacts.soft_contact_* must be contiguous device arrays of soft_contact_max "
+                                     "entries (count int32[1], particle int32, body_pos/body_vel/normal float32 [.,3])")
+            key = (cap,) + tuple(a.data_ptr() for a in arrays)
+        if key == self._contacts_key:
+            return
+        if key is not None and key[0] > getattr(self, "_contacts_capacity", 0) and \
+                torch.cuda.is_current_stream_capturing():
+            raise RuntimeError("register soft contacts of this capacity before CUDA graph capture")
+        if key is None:
+            code = self._lib.fem_set_soft_contacts(self._handle, None, None, None, None, None, 0)
+        else:
+            code = self._lib.fem_set_soft_contacts(self._handle, *key[1:], key[0])
+        _lib.check(code, "soft contacts")
+        if key is not None:
+            self._contacts_capacity = max(key[0], getattr(self, "_contacts_capacity", 0))
+        self._contacts_key = key
 
     def _activations(self, control):
         """The per-tet activations the force kernels read (None unless enabled)."""
@@ -478,6 +546,16 @@ class SolverFEM:
 
     def eval_spring_forces(self, model, state) -> torch.Tensor:
         return self._forces(state, _lib.FEM_TERM_SPRING)
+
+    def eval_triangle_forces(self, model, control, state) -> torch.Tensor:
+        return self._forces(state, _lib.FEM_TERM_TRI)
+
+    def eval_particle_particle_forces(self, model, control, state) -> torch.Tensor:
+        return self._forces(state, _lib.FEM_TERM_PARTICLE)
+
+    def eval_soft_contact_forces(self, model, state, contacts) -> torch.Tensor:
+        self._register_contacts(contacts)
+        return self._forces(state, _lib.FEM_TERM_SOFT_CONTACT)
 
     def eval_particle_ground_contact_forces(self, model, control, state) -> torch.Tensor:
         return self._forces(state, _lib.FEM_TERM_GROUND)

@@ -237,6 +237,146 @@ def spring_forces(x, v, springs, rest, ke, kd):
     return f
 
 
+def _normalize(a):
+    """Row-wise a / |a| with zero rows for |a| = 0 (Warp's normalize)."""
+    n = np.linalg.norm(a, axis=-1, keepdims=True)
+    return np.where(n > 0, a / np.where(n > 0, n, 1.0), 0.0)
+
+
+def spring_torque_forces(x, v, springs, rest_direction, kt, kwt):
+    """Bend-torque part of the torque springs: + on node j, - on node i (kernels.py:221-291)."""
+    f = np.zeros_like(x, dtype=np.float64)
+    if len(springs) == 0 or kt <= 0.0:
+        return f
+    d0 = -np.asarray(rest_direction, np.float64)
+    i, j = springs[:, 0], springs[:, 1]
+    xij = x[i].astype(np.float64) - x[j]
+    vij = v[i].astype(np.float64) - v[j]
+    L = np.linalg.norm(xij, axis=1)
+    ok = (i >= 0) & (j >= 0) & (L >= 1.0e-6) & (np.linalg.norm(d0, axis=1) >= 0.5)
+    d = xij / np.where(L > 0, L, 1.0)[:, None]
+    theta = np.arccos(np.clip(np.sum(d * d0, 1), -1.0, 1.0))
+    axis = np.cross(d0, d)
+    alen = np.linalg.norm(axis, axis=1)
+    ok &= alen >= 1.0e-6
+    axis = axis / np.where(alen > 0, alen, 1.0)[:, None]
+    d_dot = (vij - d * np.sum(d * vij, 1)[:, None]) / np.where(L > 0, L, 1.0)[:, None]
+    omega = np.sum(np.cross(d, d_dot) * axis, 1)
+    tau = -(kt * theta + kwt * omega) * L
+    ft = np.cross(axis * tau[:, None], d) / np.where(L > 0, L, 1.0)[:, None]
+    np.subtract.at(f, i[ok], ft[ok])
+    np.add.at(f, j[ok], ft[ok])
+    return f
+
+
+def triangle_forces(x, v, tris, poses, mats):
+    """Triangle membrane + area + drag/lift force (kernels.py:876-960)."""
+    f = np.zeros_like(x, dtype=np.float64)
+    if len(tris) == 0:
+        return f
+    x = x.astype(np.float64)
+    v = v.astype(np.float64)
+    Dm = np.asarray(poses, np.float64).reshape(-1, 2, 2)
+    mats = np.asarray(mats, np.float64)
+    inv_rest_area = np.linalg.det(Dm) * 2.0
+    rest_area = 1.0 / inv_rest_area
+    k_mu, k_lambda, k_damp = mats[:, 0] * rest_area, mats[:, 1] * rest_area, mats[:, 2] * rest_area
+    k_drag, k_lift = mats[:, 3], mats[:, 4]
+    i, j, k = tris[:, 0], tris[:, 1], tris[:, 2]
+    x10, x20 = x[j] - x[i], x[k] - x[i]
+    v10, v20 = v[j] - v[i], v[k] - v[i]
+    F1 = x10 * Dm[:, 0, 0, None] + x20 * Dm[:, 1, 0, None]
+    F2 = x10 * Dm[:, 0, 1, None] + x20 * Dm[:, 1, 1, None]
+    dF1 = v10 * Dm[:, 0, 0, None] + v20 * Dm[:, 1, 0, None]
+    dF2 = v10 * Dm[:, 0, 1, None] + v20 * Dm[:, 1, 1, None]
+    Ic = np.sum(F1 * F1, 1) + np.sum(F2 * F2, 1)
+    dev = (Ic - 2.0) / Ic
+    P1 = F1 * (k_mu * dev)[:, None] + dF1 * k_damp[:, None]
+    P2 = F2 * (k_mu * dev)[:, None] + dF2 * k_damp[:, None]
+    f1 = P1 * Dm[:, 0, 0, None] + P2 * Dm[:, 0, 1, None]
+    f2 = P1 * Dm[:, 1, 0, None] + P2 * Dm[:, 1, 1, None]
+    n = np.cross(x10, x20)
+    area = np.linalg.norm(n, axis=1) * 0.5
+    c = area * inv_rest_area - 1.0
+    n = _normalize(n)
+    dcdq = np.cross(x20, n) * (inv_rest_area * 0.5)[:, None]
+    dcdr = np.cross(n, x10) * (inv_rest_area * 0.5)[:, None]
+    dcdt = np.sum(dcdq * v[j], 1) + np.sum(dcdr * v[k], 1) - np.sum((dcdq + dcdr) * v[i], 1)
+    s = k_lambda * c + k_damp * dcdt
+    f1 = f1 + dcdq * s[:, None]
+    f2 = f2 + dcdr * s[:, None]
+    f0 = f1 + f2
+    vmid = (v[i] + v[j] + v[k]) * 0.3333
+    vdir = _normalize(vmid)
+    f_drag = vmid * (k_drag * area * np.abs(np.sum(n * vmid, 1)))[:, None]
+    lift = k_lift * area * (np.pi / 2 - np.arccos(np.clip(np.sum(n * vdir, 1), -1.0, 1.0)))
+    f_lift = n * (lift * np.sum(vmid * vmid, 1))[:, None]
+    np.add.at(f, i, f0 - f_drag - f_lift)
+    np.subtract.at(f, j, f1 + f_drag + f_lift)
+    np.subtract.at(f, k, f2 + f_drag + f_lift)
+    return f
+
+
+def particle_contact_forces(x, v, radius, flags, ke, kd, kf, mu, cohesion):
+    """Particle-particle penalty + damping + Coulomb over all pairs with d - r_i - r_j <= cohesion.
+
+    Brute force over pairs: the neighbour set of the reference's hash-grid
+    query after its filter (kernels.py:1036-1114, particle_force 1050-1076).
+    """
+    x = np.asarray(x, np.float64)
+    v = np.asarray(v, np.float64)
+    radius = np.asarray(radius, np.float64)
+    active = (np.asarray(flags) & PARTICLE_FLAG_ACTIVE) != 0
+    f = np.zeros_like(x)
+    P = len(x)
+    for lo in range(0, P, 512):
+        hi = min(P, lo + 512)
+        n = x[lo:hi, None, :] - x[None, :, :]
+        d = np.linalg.norm(n, axis=2)
+        err = d - radius[lo:hi, None] - radius[None, :]
+        ok = (err <= cohesion) & (d >= 1.0e-10) & active[lo:hi, None] & active[None, :]
+        ok[np.arange(hi - lo), np.arange(lo, hi)] = False
+        ii, jj = np.nonzero(ok)
+        if len(ii) == 0:
+            continue
+        nn = n[ii, jj] / d[ii, jj][:, None]
+        vrel = v[lo + ii] - v[jj]
+        vn = np.sum(nn * vrel, 1)
+        fn = err[ii, jj] * ke + np.minimum(vn, 0.0) * kd
+        vt = vrel - nn * vn[:, None]
+        vs = np.linalg.norm(vt, axis=1)
+        vt = np.where(vs[:, None] > 0, vt / np.where(vs > 0, vs, 1.0)[:, None], vt)
+        ft = np.minimum(vs * kf, mu * np.abs(fn))
+        np.add.at(f, lo + ii, -nn * fn[:, None] - vt * ft[:, None])
+    return f
+
+
+def soft_contact_forces(x, v, radius, count, particle, body_pos, body_vel, normal, ke, kd, kf, mu):
+    """Force-based soft-rigid contacts of the first ``count`` list entries (kernels.py:1198-1261)."""
+    x = np.asarray(x, np.float64)
+    v = np.asarray(v, np.float64)
+    f = np.zeros_like(x)
+    for c in range(int(count)):
+        p = int(particle[c])
+        if p < 0 or p >= len(x):
+            continue
+        n = np.asarray(normal[c], np.float64)
+        pen = radius[p] - np.dot(x[p] - body_pos[c], n)
+        if not pen > 0.0:
+            continue
+        rel = v[p] - body_vel[c]
+        vn = np.dot(rel, n)
+        vt = rel - vn * n
+        fn = ke * pen - kd * min(vn, 0.0)
+        vt_mag = np.linalg.norm(vt)
+        if vt_mag > 1.0e-6:
+            ft = min(kf * vt_mag, mu * max(0.0, fn))
+            f[p] += fn * n - ft * (vt / vt_mag)
+        else:
+            f[p] += fn * n
+    return f
+
+
 def ground_forces(x, v, radius, inv_mass, flags, ke, kd, kf, mu, plane, gravity):
     """Analytic ground penalty + weight-capped Coulomb friction (kernels.py:1132-1195)."""
     x = x.astype(np.float64)
@@ -373,6 +513,20 @@ def constant_triplets(mass, springs, ke, kd, dt):
         cols.append(cc)
         vals.append(np.repeat(off, 2)[:, None, None] * np.eye(3))
     return np.concatenate(rows), np.concatenate(cols), np.concatenate(vals)
+
+
+def triangle_triplets(tris, poses, mats, dt):
+    """Lumped triangle blocks h^2 (mu + lambda) A_rest / 3 per vertex, zero when degenerate (kernels.py:963-1012)."""
+    if len(tris) == 0:
+        return np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros((0, 3, 3))
+    Dm = np.asarray(poses, np.float64).reshape(-1, 2, 2)
+    inv_rest_area = np.linalg.det(Dm) * 2.0
+    ok = inv_rest_area > 0.0
+    rest_area = np.where(ok, 1.0 / np.where(ok, inv_rest_area, 1.0), 0.0)
+    mats = np.asarray(mats, np.float64)
+    d = np.where(ok, dt * dt * (mats[:, 0] * rest_area + mats[:, 1] * rest_area) / 3.0, 0.0)
+    rows = np.asarray(tris, np.int64).reshape(-1)
+    return rows, rows.copy(), np.repeat(d, 3)[:, None, None] * np.eye(3)
 
 
 def assemble_bsr(rows, cols, vals, n):
@@ -563,7 +717,16 @@ class OracleFEM:
         preconditioner="block_diag",
         mu_scale=None,
         scene_offsets=None,
+        tris=None,
+        tri_poses=None,
+        tri_materials=None,
+        spring_rest_direction=None,
+        torque_stiffness=0.0,
+        torque_damping=0.0,
+        particle_contact=None,
+        soft_contact=(1.0e3, 10.0, 1.0e3, 0.5),
     ):
+        """``particle_contact`` = (ke, kd, kf, mu, cohesion) enables the particle-particle term."""
         self.rest = np.asarray(x, np.float64).copy()
         self.n = len(self.rest)
         self.mass = np.asarray(mass, np.float64)
@@ -598,6 +761,14 @@ class OracleFEM:
         self.scene_offsets = (
             np.array([0, self.n], np.int64) if scene_offsets is None else np.asarray(scene_offsets, np.int64)
         )
+        self.tris = np.zeros((0, 3), np.int64) if tris is None else np.asarray(tris, np.int64).reshape(-1, 3)
+        self.tri_poses = np.zeros((0, 2, 2)) if tri_poses is None else np.asarray(tri_poses, np.float64)
+        self.tri_materials = np.zeros((0, 5)) if tri_materials is None else np.asarray(tri_materials, np.float64)
+        self.spring_rest_direction = None if spring_rest_direction is None else \
+            np.asarray(spring_rest_direction, np.float64)
+        self.torque = (float(torque_stiffness), float(torque_damping))
+        self.particle_contact = particle_contact
+        self.soft_contact = soft_contact
         self.dv = np.zeros((self.n, 3))
         self.last_iterations = []
         self.last_rr_bb = []
@@ -605,8 +776,9 @@ class OracleFEM:
 
     # -- assembly -----------------------------------------------------------
     def triplets(self, q, dt):
-        """All triplets in the reference layout [P | 2S | 16T | 64H] (solver.py:312-321)."""
+        """All triplets in the reference layout [P | 2S | 3Tri | 16T | 64H] (solver.py:312-321)."""
         parts = [constant_triplets(self.mass, self.springs, self.spring_ke, self.spring_kd, dt)]
+        parts.append(triangle_triplets(self.tris, self.tri_poses, self.tri_materials, dt))
         parts.append(
             tet_tangent(q, self.tets, self.tet_poses, self.tet_materials, self.min_stretch, self.max_stretch, dt,
                         self.mu_scale)
@@ -644,17 +816,31 @@ class OracleFEM:
         return dense(self.offsets, self.columns, self.values, self.n)
 
     # -- forces --------------------------------------------------------------
-    def forces(self, q, v, *, activation=None, terms=("spring", "tet", "hex", "ground", "gravity", "damping")):
-        """Per-term forces in the reference's accumulation order (solver.py:571-582)."""
+    TERMS = ("spring", "tet", "hex", "tri", "particle", "ground", "soft_contact", "gravity", "damping")
+
+    def forces(self, q, v, *, activation=None, terms=TERMS, contacts=None):
+        """Per-term forces in the reference's accumulation order (solver.py:571-582).
+
+        ``contacts`` = (count, particle, body_pos, body_vel, normal) NumPy arrays."""
         out = {}
         if "spring" in terms:
             out["spring"] = spring_forces(q, v, self.springs, self.spring_rest, self.spring_ke, self.spring_kd)
+            if self.spring_rest_direction is not None and self.torque[0] > 0.0:
+                out["spring"] += spring_torque_forces(q, v, self.springs, self.spring_rest_direction, *self.torque)
         if "tet" in terms:
             out["tet"] = tet_forces(q, v, self.tets, self.tet_poses, self.tet_materials, self.min_stretch,
                                     self.max_stretch, activation, self.mu_scale)
         if "hex" in terms:
             out["hex"] = hex_forces(q, v, self.hexes, self.hex_inv_J0, self.hex_det_J0_w, self.hex_materials,
                                     self.min_stretch, self.max_stretch) if len(self.hexes) else np.zeros((self.n, 3))
+        if "tri" in terms:
+            out["tri"] = triangle_forces(q, v, self.tris, self.tri_poses, self.tri_materials)
+        if "particle" in terms:
+            out["particle"] = np.zeros((self.n, 3)) if self.particle_contact is None else \
+                particle_contact_forces(q, v, self.radius, self.flags, *self.particle_contact)
+        if "soft_contact" in terms:
+            out["soft_contact"] = np.zeros((self.n, 3)) if contacts is None else \
+                soft_contact_forces(q, v, self.radius, *contacts, *self.soft_contact)
         if "ground" in terms:
             if self.ground_plane is None:
                 out["ground"] = np.zeros((self.n, 3))
@@ -682,7 +868,7 @@ class OracleFEM:
     def apply_M(self, r):
         return np.einsum("nij,nj->ni", self.minv, r)
 
-    def step(self, q, v, dt, *, external=None, activation=None, fixed_iterations=None):
+    def step(self, q, v, dt, *, external=None, activation=None, fixed_iterations=None, contacts=None):
         """One substep: returns (q_out, v_out, rhs) (solver.py:942-1002, 1254-1351).
 
         ``fixed_iterations`` runs exactly that many CG updates (tolerance 0),
@@ -692,9 +878,9 @@ class OracleFEM:
         v = np.asarray(v, np.float64).copy()
         q[self.fixed] = self.rest[self.fixed]  # fixed_particles.py:11-15
         v[self.fixed] = 0.0
-        terms = self.forces(q, v, activation=activation)
+        terms = self.forces(q, v, activation=activation, contacts=contacts)
         f = np.zeros((self.n, 3))
-        for key in ("spring", "tet", "hex", "ground", "gravity", "damping"):
+        for key in self.TERMS:
             f += dt * terms[key]
         if external is not None:
             f += dt * np.asarray(external, np.float64)

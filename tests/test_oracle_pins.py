@@ -212,3 +212,123 @@ def test_synthetic_config_sizes():
     assert hx.shape == (8, 8)
     _, det = O.hex_builder_data(xg, hx)
     np.testing.assert_allclose(det.sum(), 0.1**3)
+
+
+# ---------------------------------------------------------------- triangles, torque springs, contacts
+
+
+def _membrane():
+    from newton_solver_fem_gb300.builder import triangle_rest_data
+
+    g = np.stack(np.meshgrid(np.arange(4) * 0.02, np.arange(3) * 0.02, indexing="ij"), -1).reshape(-1, 2)
+    x = np.column_stack([g, np.full(len(g), 0.1)])
+    tris = []
+    for i in range(3):
+        for j in range(2):
+            a, b, c, d = 3 * i + j, 3 * (i + 1) + j, 3 * (i + 1) + j + 1, 3 * i + j + 1
+            tris += [(a, b, c), (a, c, d)]
+    tris = np.asarray(tris)
+    poses, area = triangle_rest_data(x, tris)
+    mats = np.tile([[30.0, 50.0, 0.0, 0.0, 0.0]], (len(tris), 1))
+    return x, tris, poses, area, mats
+
+
+def test_triangle_pose_is_the_inverse_rest_edge_matrix_in_the_triangle_frame():
+    """Newton's triangle pose: inv([[e1.x10, e1.x20], [e2.x10, e2.x20]]) with e1 along x10 and area det/2."""
+    from newton_solver_fem_gb300.builder import triangle_rest_data
+
+    x = np.array([[0.0, 0.0, 0.0], [0.1, 0.0, 0.0], [0.0, 0.1, 0.0], [0.1, 0.1, 0.0]])
+    poses, area = triangle_rest_data(x, [[0, 1, 2], [0, 1, 3]])
+    np.testing.assert_allclose(poses[0], np.diag([10.0, 10.0]), atol=1e-12)
+    np.testing.assert_allclose(poses[1], [[10.0, -10.0], [0.0, 10.0]], atol=1e-12)
+    np.testing.assert_allclose(area, [0.005, 0.005])
+    # the kernels' rest area 1 / (2 det pose) is the same area
+    np.testing.assert_allclose(1.0 / (2.0 * np.linalg.det(poses)), area)
+
+
+def test_triangle_membrane_force_is_the_energy_gradient_and_conserves_momentum():
+    """f = -dE/dx for E = mu' (I_C/2 - ln I_C) + lambda' c^2 / 2 per triangle (rest-area scaled), zero at rest."""
+    x, tris, poses, area, mats = _membrane()
+    rng = np.random.default_rng(0)
+    np.testing.assert_allclose(O.triangle_forces(x, np.zeros_like(x), tris, poses, mats), 0.0, atol=1e-12)
+    q = x + rng.normal(0, 2e-3, x.shape)
+
+    def energy_of(p):
+        e = 0.0
+        for t, Dm, m, a0 in zip(tris, poses, mats, area):
+            F = np.column_stack([p[t[1]] - p[t[0]], p[t[2]] - p[t[0]]]) @ Dm
+            Ic = np.sum(F * F)
+            c = 0.5 * np.linalg.norm(np.cross(p[t[1]] - p[t[0]], p[t[2]] - p[t[0]])) / a0 - 1.0
+            e += a0 * m[0] * (0.5 * Ic - np.log(Ic)) + 0.5 * a0 * m[1] * c * c
+        return e
+
+    f = O.triangle_forces(q, np.zeros_like(q), tris, poses, mats)
+    eps = 1e-7
+    for _ in range(3):
+        d = rng.normal(size=q.shape)
+        de = (energy_of(q + eps * d) - energy_of(q - eps * d)) / (2 * eps)
+        np.testing.assert_allclose(np.sum(f * d), -de, rtol=1e-5)
+    np.testing.assert_allclose(f.sum(0), 0.0, atol=1e-10)
+    # drag and lift act along the mean velocity and the normal only
+    mats_air = mats.copy()
+    mats_air[:, 3:] = (0.4, 0.3)
+    v = np.tile([[0.0, 0.0, 1.0]], (len(x), 1))
+    f_air = O.triangle_forces(x, v, tris, poses, mats_air)
+    np.testing.assert_allclose(f_air[:, :2], 0.0, atol=1e-12)
+    assert f_air[:, 2].min() < 0.0  # the 0.3333 mean-velocity drag and the lift oppose upward motion at corner 0
+
+
+def test_triangle_lumped_blocks():
+    """h^2 (mu + lambda) A_rest / 3 I on each vertex, zero for a degenerate triangle (kernels.py:963-1012)."""
+    x, tris, poses, area, mats = _membrane()
+    rows, cols, vals = O.triangle_triplets(tris, poses, mats, 0.01)
+    np.testing.assert_array_equal(rows, tris.reshape(-1))
+    np.testing.assert_allclose(vals[0], 1e-4 * (30.0 + 50.0) * area[0] / 3.0 * np.eye(3))
+    _, _, degenerate = O.triangle_triplets(tris[:1], np.zeros((1, 2, 2)), mats[:1], 0.01)
+    assert not degenerate.any()
+
+
+def test_spring_torque_vanishes_at_rest_and_conserves_momentum():
+    rng = np.random.default_rng(1)
+    x = np.cumsum(rng.normal(0, 0.02, (6, 3)) + (0.03, 0, 0), axis=0)
+    springs = np.array([(0, 1), (1, 2), (2, 3), (3, 4), (4, 5)])
+    d = x[springs[:, 1]] - x[springs[:, 0]]
+    rest = d / np.linalg.norm(d, axis=1, keepdims=True)
+    np.testing.assert_allclose(O.spring_torque_forces(x, np.zeros_like(x), springs, rest, 2.0, 0.1), 0.0, atol=1e-12)
+    q = x + rng.normal(0, 3e-3, x.shape)
+    v = rng.normal(0, 0.2, x.shape)
+    f = O.spring_torque_forces(q, v, springs, rest, 2.0, 0.1)
+    assert np.abs(f).max() > 0
+    np.testing.assert_allclose(f.sum(0), 0.0, atol=1e-12)
+    # transverse: no component along each spring (a single spring isolates its own force)
+    one = O.spring_torque_forces(q, v, springs[:1], rest[:1], 2.0, 0.1)
+    axis = q[0] - q[1]
+    assert abs(np.dot(one[1], axis)) < 1e-10 * np.linalg.norm(one[1]) * np.linalg.norm(axis)
+
+
+def test_particle_contact_pairs_are_equal_and_opposite():
+    rng = np.random.default_rng(2)
+    x = rng.uniform(0, 0.1, (60, 3))
+    radius = rng.uniform(0.005, 0.01, 60)
+    v = rng.normal(0, 0.3, (60, 3))
+    flags = np.ones(60, np.int32)
+    f = O.particle_contact_forces(x, v, radius, flags, 1e3, 1e2, 1e2, 0.5, 0.0)
+    assert (np.abs(f).sum(1) > 0).sum() > 10
+    np.testing.assert_allclose(f.sum(0), 0.0, atol=1e-9 * np.abs(f).max())
+    # two particles: penalty along the line of centres, err = d - r_i - r_j
+    two = O.particle_contact_forces(np.array([[0, 0, 0], [0.015, 0, 0]]), np.zeros((2, 3)), np.array([0.01, 0.01]),
+                                    np.ones(2, np.int32), 1e3, 1e2, 1e2, 0.5, 0.0)
+    np.testing.assert_allclose(two, [[-5.0, 0, 0], [5.0, 0, 0]])
+
+
+def test_soft_contact_known_answer():
+    """One penetrating contact: fn = ke pen - kd min(vn, 0); friction capped by mu max(fn, 0) (kernels.py:1198-1261)."""
+    x = np.array([[0.0, 0.0, 0.009]])
+    v = np.array([[0.3, 0.0, -0.2]])
+    f = O.soft_contact_forces(x, v, np.array([0.01]), 1, np.array([0]), np.zeros((1, 3)), np.zeros((1, 3)),
+                              np.array([[0.0, 0.0, 1.0]]), 1e3, 10.0, 1e3, 0.5)
+    fn = 1e3 * 0.001 + 10.0 * 0.2
+    np.testing.assert_allclose(f, [[-min(1e3 * 0.3, 0.5 * fn), 0.0, fn]])
+    none = O.soft_contact_forces(x + (0, 0, 0.01), v, np.array([0.01]), 1, np.array([0]), np.zeros((1, 3)),
+                                 np.zeros((1, 3)), np.array([[0.0, 0.0, 1.0]]), 1e3, 10.0, 1e3, 0.5)
+    assert not none.any()
