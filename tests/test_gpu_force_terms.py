@@ -278,10 +278,11 @@ def test_triangle_and_torque_force_vjp_match_oracle_differences():
     v = rounded(rng.normal(0, 0.3, x.shape))
     g = rounded(rng.normal(0, 1.0, x.shape))
     lib = _lib.load()
+    qt, vt, gt = tensor(q), tensor(v), tensor(g)  # held: the library reads them asynchronously
     qb, vb = torch.zeros(x.shape, device=DEVICE), torch.zeros(x.shape, device=DEVICE)
-    _lib.check(lib.fem_force_vjp(solver._handle, tensor(q).data_ptr(), tensor(v).data_ptr(), None,
-                                 model.gravity.data_ptr(), tensor(g).data_ptr(), qb.data_ptr(), vb.data_ptr(), None,
-                                 None, torch.cuda.current_stream().cuda_stream))
+    _lib.check(lib.fem_force_vjp(solver._handle, qt.data_ptr(), vt.data_ptr(), None, model.gravity.data_ptr(),
+                                 gt.data_ptr(), qb.data_ptr(), vb.data_ptr(), None, None,
+                                 torch.cuda.current_stream().cuda_stream))
     torch.cuda.synchronize()
     qb, vb = to_np(qb), to_np(vb)
 
