@@ -4,7 +4,7 @@
 // sorts them (bsr_set_from_triplets) or scatters them with float atomics into
 // precomputed slots (sparse_update.py:9-59).  Here the setup builds, once, the
 // list of contributing triplets of every matrix slot in ascending triplet order
-// (the reference layout [P | 2S | 16T | 64H]), and each refresh sums that list
+// (the reference layout [P | 2S | 3Tri | 16T | 64H]), and each refresh sums that list
 // in order: no atomics, bit-identical results run to run.  The thread that
 // owns a diagonal slot also writes that row's preconditioner block
 // (kernels.py:1836-1849 fused into the assembly epilogue).

@@ -18,7 +18,7 @@ constexpr unsigned kFixedBit = 0x80000000u;  // row_info: fixed-node flag; low b
 constexpr int kStatusTimeout = 1 << 2;
 constexpr int kStatusNonFinite = 1 << 1;
 
-// Triplet blocks (the reference layout [P | 2S | 16T | 64H]) stored in three
+// Triplet blocks (the reference layout [P | 2S | 3Tri | 16T | 64H]) stored in three
 // planes, the same split as the SELL matrix: block i is (a[i], b[i], c[i]) =
 // ((a00 a01 a02 a10), (a11 a12 a20 a21), a22), so that a block is written and
 // read with two aligned 16-byte accesses and one 4-byte access.
