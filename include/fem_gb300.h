@@ -19,6 +19,8 @@
  *   fem_get_stats                SolverFEM.last_cg_iters             solver.py:279, 1333-1335
  *   fem_eval_forces              SolverFEM.eval_*_forces             solver.py:1357-1600
  *   fem_set_soft_contacts        Contacts.soft_contact_* into step   solver.py:1540-1566
+ *   fem_prepare_tet_updates      SolverFEM.prepare_tetrahedral_updates solver.py:693-719
+ *   fem_update_tet_topology      refresh_topology(element_sources=)   solver.py:872-940, streaming.py:549-700
  *   fem_export_bsr               SolverFEM.A_bsr (Warp BsrMatrix)    solver.py:322-337
  *   fem_export_preconditioner    SolverFEM._pc_inv_diag              solver.py:1142-1201
  *   fem_matrix_info              A_bsr.nnz / nrow                    solver.py:322-328
@@ -247,6 +249,39 @@ int fem_predictor_vjp(FemHandle* handle, const float* rhs_bar, float dt, float* 
  * storage is rebuilt, so graphs captured before the call must be captured
  * again. */
 int fem_refresh_topology(FemHandle* h, const FemDesc* d, float* q, float dt, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Streaming Tet4 assembly (streaming.py, StreamingTetAssembly;
+ * SolverFEM.prepare_tetrahedral_updates solver.py:693-719, refresh_topology
+ * with element_sources solver.py:872-940).  The particle pool holds equal
+ * copies of N0 original nodes (pool node i represents original node i % N0);
+ * tetrahedra may move their corners onto any copy of their original corners.
+ * Requires Tet4 elements only, block_diag, no fixed nodes and one scene.
+ * ------------------------------------------------------------------------- */
+typedef struct FemTopologyUpdate {
+    int32_t dirty_elements;             /* active elements whose blocks changed */
+    int32_t removed_elements;           /* previous elements whose contribution was withdrawn */
+    int32_t reused_elements;            /* unchanged connectivity, positions, pose and material */
+    int32_t active_elements;
+    int32_t touched_rows;               /* rows whose sparse structure changed */
+    int32_t topology_inserted_elements;
+    int32_t topology_removed_elements;
+    int32_t full_numeric_refresh;       /* more than half the active elements were dirty */
+} FemTopologyUpdate;
+
+/* Reserve the candidate pattern (row r: r and every copy of every original
+ * neighbour of r mod N0 over the enabled tets of d) and assemble at the
+ * construction positions.  Rebuilds the handle's storage once; call before
+ * capturing graphs.  d describes the model's arrays as at creation. */
+int fem_prepare_tet_updates(FemHandle* h, const FemDesc* d, int32_t original_node_count, void* stream);
+/* Apply edited tet connectivity, poses, materials, masses and flags (from d)
+ * at positions q without moving any device storage: a graph captured before
+ * the call replays after it.  element_sources (device int32 [T], or NULL for
+ * the identity) gives each slot's previous element or -1.  Validation runs
+ * before any change; a rejected update returns FEM_ERR_BAD_ARG and leaves the
+ * assembly untouched.  Clears the warm start; synchronises the stream. */
+int fem_update_tet_topology(FemHandle* h, const FemDesc* d, float* q, float dt, const int32_t* element_sources,
+                            FemTopologyUpdate* update, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Prepared affine step.  Replaces the reference's PreparedFEMStep

@@ -109,6 +109,12 @@ class FemDesc(ctypes.Structure):
     ]
 
 
+class FemTopologyUpdate(ctypes.Structure):
+    _fields_ = [(name, _i32) for name in (
+        "dirty_elements", "removed_elements", "reused_elements", "active_elements", "touched_rows",
+        "topology_inserted_elements", "topology_removed_elements", "full_numeric_refresh")]
+
+
 class FemStats(ctypes.Structure):
     _fields_ = [
         ("status", _i32),
@@ -155,6 +161,9 @@ SIGNATURES = [
     ("fem_solve", _i32, [_p, _p, _p, _f, _i32, _p]),
     ("fem_force_vjp", _i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     ("fem_predictor_vjp", _i32, [_p, _p, _f, _p, _p]),
+    ("fem_prepare_tet_updates", _i32, [_p, ctypes.POINTER(FemDesc), _i32, _p]),
+    ("fem_update_tet_topology", _i32, [_p, ctypes.POINTER(FemDesc), _p, _f, _p, ctypes.POINTER(FemTopologyUpdate),
+                                        _p]),
     ("fem_prepare", _i32, [_p, ctypes.POINTER(FemPreparedWs), _p, _p, _p, _p, _p, _f, _p]),
     ("fem_prepared_rhs", _i32, [_p, ctypes.POINTER(FemPreparedWs), _p, _f, _p, _p]),
     ("fem_apply_operator", _i32, [_p, _p, _p, _p]),

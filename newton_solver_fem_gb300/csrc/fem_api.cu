@@ -235,7 +235,12 @@ const char* fem_status_string(int status) {
     }
 }
 
-int fem_create(const FemDesc* d, FemHandle** out) {
+}  // extern "C"
+
+// Construction.  `candidate` (streaming Tet4 assembly) gives, per row, the sorted
+// columns the pattern reserves; every triplet's column must be among them, and
+// reserved entries without contributors hold exact zeros.
+int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* candidate, FemHandle** out) {
     if (d == nullptr || out == nullptr) return set_error(FEM_ERR_BAD_ARG, "null descriptor or output");
     *out = nullptr;
     const int P = d->particle_count, T = d->tet_count, Hn = d->hex_count, S = d->spring_count, Tri = d->tri_count;
@@ -412,17 +417,32 @@ int fem_create(const FemDesc* d, FemHandle** out) {
             if (trip_rows[t] >= 0) contrib[pos[trip_rows[t]]++] = (int)t;
     }
     std::vector<int> row_nnz(P, 0);
+    std::vector<unsigned char> outside(P, 0);
     parallel_for(P, [&](int64_t lo, int64_t hi) {
         for (int64_t i = lo; i < hi; ++i) {
             int* beg = contrib.data() + row_ptr[i];
             int* end = contrib.data() + row_ptr[i + 1];
             std::stable_sort(beg, end, [&](int x, int y) { return trip_cols[x] < trip_cols[y]; });
+            if (candidate != nullptr) {
+                const std::vector<int>& cc = (*candidate)[i];
+                size_t k = 0;
+                for (int* p = beg; p != end; ++p) {
+                    while (k < cc.size() && cc[k] < trip_cols[*p]) ++k;
+                    if (k == cc.size() || cc[k] != trip_cols[*p]) outside[i] = 1;
+                }
+                row_nnz[i] = (int)cc.size();
+                continue;
+            }
             int n = 0, prev = -1;
             for (int* p = beg; p != end; ++p)
                 if (trip_cols[*p] != prev) { ++n; prev = trip_cols[*p]; }
             row_nnz[i] = n;
         }
     });
+    if (std::find(outside.begin(), outside.end(), 1) != outside.end()) {
+        fem_destroy(H);
+        return set_error(FEM_ERR_BAD_ARG, "a block lies outside the reserved sparse pattern");
+    }
     std::vector<int> bsr_offsets(P + 1, 0);
     for (int i = 0; i < P; ++i) bsr_offsets[i + 1] = bsr_offsets[i] + row_nnz[i];
     const int64_t nnzb = bsr_offsets[P];
@@ -431,6 +451,17 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     slot_cptr[nnzb] = (int)nvalid;
     parallel_for(P, [&](int64_t lo, int64_t hi) {
         for (int64_t i = lo; i < hi; ++i) {
+            if (candidate != nullptr) {
+                const std::vector<int>& cc = (*candidate)[i];
+                int64_t p = row_ptr[i];
+                for (size_t k = 0; k < cc.size(); ++k) {
+                    const int slot = bsr_offsets[i] + (int)k;
+                    bsr_columns[slot] = cc[k];
+                    slot_cptr[slot] = (int)p;
+                    while (p < row_ptr[i + 1] && trip_cols[contrib[p]] == cc[k]) ++p;
+                }
+                continue;
+            }
             int slot = bsr_offsets[i] - 1, prev = -1;
             for (int64_t p = row_ptr[i]; p < row_ptr[i + 1]; ++p) {
                 int c = trip_cols[contrib[p]];
@@ -549,7 +580,7 @@ int fem_create(const FemDesc* d, FemHandle** out) {
         const int64_t nb = (int64_t)h.grid_dim * h.grid_dim * h.grid_dim;
         h.grid_count = b.alloc<int>((size_t)nb);
         h.grid_start = b.alloc<int>((size_t)nb + 1);
-        h.grid_part = b.alloc<int>((size_t)(nb + 4095) / 4096);
+        h.grid_part = b.alloc<int>((size_t)fem::scan_partial_count(nb));
         h.grid_items = b.alloc<int>(P);
         h.cell_of = b.alloc<int>(P);
         h.pforce = b.alloc<float4>(P);
@@ -661,6 +692,10 @@ int fem_create(const FemDesc* d, FemHandle** out) {
     return FEM_OK;
 }
 
+extern "C" {
+
+int fem_create(const FemDesc* d, FemHandle** out) { return fem::create_handle(d, nullptr, out); }
+
 int fem_destroy(FemHandle* H) {
     if (H == nullptr) return FEM_OK;
     DeviceGuard g(H->device);
@@ -741,8 +776,92 @@ int fem_get_timing(FemHandle* H, double* pcg_ms_total, int64_t* launches) {
     return cuda_status(err, &h);
 }
 
+int fem_prepare_tet_updates(FemHandle* H, const FemDesc* d, int32_t original_node_count, void* stream) {
+    if (H == nullptr || d == nullptr) return set_error(FEM_ERR_BAD_ARG, "fem_prepare_tet_updates: null handle or descriptor");
+    Handle& h = H->h;
+    const int N0 = original_node_count;
+    if (h.streaming) return set_error(FEM_ERR_BAD_ARG, "Tetrahedral updates are already prepared");
+    if (N0 < 1 || h.P % N0 != 0)
+        return set_error(FEM_ERR_BAD_ARG, "The particle pool must contain whole copies of the original node set");
+    if (h.T < 1 || h.H || h.S || h.Tri)
+        return set_error(FEM_ERR_BAD_ARG, "Streaming assembly requires tetrahedral elements only");
+    if (h.precond != FEM_PRECOND_BLOCK_DIAG)
+        return set_error(FEM_ERR_BAD_ARG, "Streaming assembly requires the block_diag preconditioner");
+    if (h.nfixed) return set_error(FEM_ERR_BAD_ARG, "Streaming topology is not supported with fixed_particle_indices");
+    if (h.nscenes != 1) return set_error(FEM_ERR_UNSUPPORTED, "Streaming assembly supports one scene");
+    if (d->particle_count != h.P || d->tet_count != h.T || d->hex_count || d->spring_count || d->tri_count)
+        return set_error(FEM_ERR_BAD_ARG, "the descriptor must describe the solver's model");
+    std::vector<std::vector<int>> cand;
+    std::string why;
+    int code = fem::streaming_candidate(d, N0, cand, why);
+    if (code != FEM_OK) return set_error(code, why);
+    DeviceGuard g(H->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_status(e, &h);
+    FemDesc nd = *d;
+    nd.dt = h.dt;
+    nd.tolerance = h.tol;
+    nd.maxiter = h.maxiter;
+    nd.velocity_increment = h.dv_owned ? nullptr : h.dv;
+    FemHandle* fresh = nullptr;
+    code = fem::create_handle(&nd, &cand, &fresh);
+    if (code != FEM_OK) return code;
+    Handle& n = fresh->h;
+    n.wait_limit_ns = h.wait_limit_ns;
+    n.spmv_unroll = h.spmv_unroll;
+    n.l2_resident_bytes = h.l2_resident_bytes;
+    n.pcg_threads = h.pcg_threads;
+    n.grid_cap = h.grid_cap;
+    n.timing = h.timing;
+    n.mu_scale = h.mu_scale;
+    code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
+    if (code == FEM_OK) code = configure_launch(n);
+    if (code == FEM_OK) {
+        std::vector<int> diag(h.P);
+        for (int r = 0; r < h.P; ++r) {
+            const auto& c = cand[r];
+            const int k = (int)(std::lower_bound(c.begin(), c.end(), r) - c.begin());
+            diag[r] = (n.host_slice_ptr[r / fem::kSlice] + k) * fem::kSlice + (r % fem::kSlice);
+        }
+        code = cuda_status(fem::streaming_allocate(n, N0, diag), &n);
+    }
+    if (code != FEM_OK) {
+        fem_destroy(fresh);
+        return code;
+    }
+    std::swap(H->h, fresh->h);
+    fresh->device = H->device;
+    fem_destroy(fresh);
+    // assemble at the construction positions with the identity lineage (streaming.py:515-516)
+    FemTopologyUpdate u;
+    code = fem::streaming_update(H->h, d, H->h.rest, nullptr, &u, (cudaStream_t)stream, why);
+    if (code == FEM_ERR_BAD_ARG) return set_error(code, why);
+    return code;
+}
+
+int fem_update_tet_topology(FemHandle* H, const FemDesc* d, float* q, float dt, const int32_t* element_sources,
+                            FemTopologyUpdate* update, void* stream) {
+    if (H == nullptr || d == nullptr || q == nullptr)
+        return set_error(FEM_ERR_BAD_ARG, "fem_update_tet_topology: null handle, descriptor or positions");
+    Handle& h = H->h;
+    if (!h.streaming) return set_error(FEM_ERR_BAD_ARG, "Prepare tetrahedral updates before applying element sources");
+    if (!(dt > 0.0f) || dt != h.dt)
+        return set_error(FEM_ERR_BAD_ARG, "refresh_topology requires the currently assembled timestep");
+    if (d->particle_count != h.P || d->tet_count != h.T || d->hex_count || d->spring_count || d->tri_count ||
+        d->tet_indices == nullptr || d->tet_poses == nullptr || d->tet_materials == nullptr ||
+        d->particle_mass == nullptr || d->particle_inv_mass == nullptr)
+        return set_error(FEM_ERR_BAD_ARG, "topology updates must preserve the model's capacities");
+    DeviceGuard g(H->device);
+    std::string why;
+    FemTopologyUpdate u;
+    int code = fem::streaming_update(h, d, q, element_sources, update ? update : &u, (cudaStream_t)stream, why);
+    if (code == FEM_ERR_BAD_ARG) return set_error(code, why);
+    return code;
+}
+
 int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, void* stream) {
     if (H == nullptr || d == nullptr || q == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle, descriptor or positions");
+    if (H->h.streaming) return fem_update_tet_topology(H, d, q, dt, nullptr, nullptr, stream);
     Handle& h = H->h;
     if (!(dt > 0.0f) || !std::isfinite(dt)) return set_error(FEM_ERR_BAD_ARG, "dt must be finite and positive");
     if (dt != h.dt) return set_error(FEM_ERR_BAD_ARG, "refresh_topology requires the currently assembled timestep");
@@ -791,6 +910,8 @@ int fem_refresh_tangent(FemHandle* H, float* q, float dt, void* stream) {
         return FEM_OK;
     }
     if (q == nullptr) return set_error(FEM_ERR_BAD_ARG, "null positions");
+    if (h.streaming && dt != h.dt)
+        return set_error(FEM_ERR_BAD_ARG, "Streaming tangent refresh requires the construction timestep");
     DeviceGuard g(H->device);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t err = cudaSuccess;
@@ -801,6 +922,8 @@ int fem_refresh_tangent(FemHandle* H, float* q, float dt, void* stream) {
     if (err == cudaSuccess) err = fem::launch_node_prepare(h, q, nullptr, true, false, false, s);
     if (err == cudaSuccess) err = fem::launch_element_tangent(h, dt, s);
     if (err == cudaSuccess) err = fem::launch_gather(h, s);
+    if (err == cudaSuccess && h.streaming)  // the linearisation the next topology update compares against
+        err = cudaMemcpyAsync(h.lin_q, q, sizeof(float) * 3 * (size_t)h.P, cudaMemcpyDeviceToDevice, s);
     if (err == cudaSuccess) h.dt = dt;
     return cuda_status(err, &h);
 }
@@ -811,6 +934,7 @@ int fem_rebuild_element_blocks(FemHandle* H, float* q, float dt, void* stream) {
     if (!(dt > 0.0f) || !std::isfinite(dt)) return set_error(FEM_ERR_BAD_ARG, "dt must be finite and positive");
     if (h.P == 0) return FEM_OK;
     if (q == nullptr) return set_error(FEM_ERR_BAD_ARG, "null positions");
+    if (h.streaming) return fem_refresh_tangent(H, q, dt, stream);  // solver.py:672-674
     DeviceGuard g(H->device);
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t err = fem::launch_node_prepare(h, q, nullptr, true, false, false, s);

@@ -22,11 +22,20 @@ constexpr int kGatherBatch = 4;
 __global__ void gather_kernel(int64_t nsell, const int* __restrict__ cptr, const int* __restrict__ contrib,
                               const int* __restrict__ sell_row, const int* __restrict__ scol,
                               const TripletPlanes trip, float4* __restrict__ valA, float4* __restrict__ valB,
-                              float* __restrict__ valC, float* __restrict__ minv, int precond) {
+                              float* __restrict__ valC, float* __restrict__ minv, int precond, int clear_empty) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nsell) return;
     const int c0 = cptr[e], c1 = cptr[e + 1];
-    if (c0 == c1) return;  // padding: zero since setup
+    if (c0 == c1) {
+        // padding is zero since setup; a reserved entry whose last contributor
+        // left (streaming assembly) is cleared to an exact zero
+        if (clear_empty) {
+            valA[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+            valB[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+            valC[e] = 0.0f;
+        }
+        return;
+    }
     float b[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) b[k] = 0.0f;
@@ -97,7 +106,7 @@ cudaError_t launch_gather(Handle& h, cudaStream_t s) {
     int64_t blocks = (h.nsell + threads - 1) / threads;
     gather_kernel<<<(unsigned)blocks, threads, 0, s>>>(h.nsell, h.sell_cptr, h.sell_contrib, h.sell_row, h.scol,
                                                        h.trip, h.valA, h.valB, h.valC, h.minv,
-                                                       h.precond);
+                                                       h.precond, h.streaming);
     return cudaGetLastError();
 }
 

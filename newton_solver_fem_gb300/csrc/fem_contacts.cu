@@ -24,9 +24,6 @@ namespace fem {
 
 namespace {
 
-constexpr int kScanThreads = 1024;
-constexpr int kScanItems = 4;  // per thread
-constexpr int kScanTile = kScanThreads * kScanItems;
 
 __device__ __forceinline__ int cell_coord(float x, float inv_w) {
     const float c = floorf(x * inv_w);
@@ -51,6 +48,14 @@ __global__ void grid_count_kernel(int P, const float4* __restrict__ q4, const in
     cell_of[i] = b;
     atomicAdd(count + b, 1);
 }
+
+}  // namespace
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;  // per thread
+constexpr int kScanTile = kScanThreads * kScanItems;
 
 // Exclusive scan of count[0, n) into start[0, n]: tile sums, a one-CTA scan of
 // the tile sums, then each tile's scan plus its offset.
@@ -132,6 +137,21 @@ __global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(int n, const i
     }
     if (grand_total_slot && blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) start[n] = run;
 }
+
+}  // namespace
+
+int scan_partial_count(int64_t n) { return (int)((n + kScanTile - 1) / kScanTile); }
+
+cudaError_t launch_exclusive_scan(const int* count, int* start, int n, int* part, cudaStream_t s) {
+    if (n <= 0) return cudaMemsetAsync(start, 0, sizeof(int), s);
+    const int tiles = scan_partial_count(n);
+    scan_tile_sums_kernel<<<tiles, kScanThreads, 0, s>>>(n, count, part);
+    scan_part_kernel<<<1, kScanThreads, 0, s>>>(tiles, part);
+    scan_tiles_kernel<<<tiles, kScanThreads, 0, s>>>(n, count, part, start, 1);
+    return cudaGetLastError();
+}
+
+namespace {
 
 // Scatter: each particle takes a position in its bucket by decrementing the
 // bucket count, which leaves every count at zero for the next evaluation.
@@ -279,14 +299,12 @@ cudaError_t launch_particle_contacts(Handle& h, cudaStream_t s) {
     if (h.P == 0) return cudaSuccess;
     const float w = 2.0f * h.pmaxr + h.pcoh;
     const int nb = h.grid_dim * h.grid_dim * h.grid_dim;
-    const int tiles = (nb + kScanTile - 1) / kScanTile;
     cudaError_t err = cudaMemsetAsync(h.grid_count, 0, sizeof(int) * (size_t)nb, s);
     if (err != cudaSuccess) return err;
     grid_count_kernel<<<blocks_for(h.P, 256), 256, 0, s>>>(h.P, h.q4, h.flags, 1.0f / w, h.grid_dim, h.cell_of,
                                                            h.grid_count);
-    scan_tile_sums_kernel<<<tiles, kScanThreads, 0, s>>>(nb, h.grid_count, h.grid_part);
-    scan_part_kernel<<<1, kScanThreads, 0, s>>>(tiles, h.grid_part);
-    scan_tiles_kernel<<<tiles, kScanThreads, 0, s>>>(nb, h.grid_count, h.grid_part, h.grid_start, 1);
+    err = launch_exclusive_scan(h.grid_count, h.grid_start, nb, h.grid_part, s);
+    if (err != cudaSuccess) return err;
     grid_scatter_kernel<<<blocks_for(h.P, 256), 256, 0, s>>>(h.P, h.cell_of, h.grid_start, h.grid_count,
                                                              h.grid_items);
     grid_sort_kernel<<<blocks_for(nb, 256), 256, 0, s>>>(nb, h.grid_start, h.grid_items);

@@ -178,6 +178,29 @@ struct Handle {
     int* node_elem_ent = nullptr;  // element-force slots
     int* node_spring_ptr = nullptr;
     int* node_spring_ent = nullptr;
+    // streaming Tet4 assembly (reserved candidate pattern, topology updates on the device)
+    int streaming = 0;
+    int orig_nodes = 0;            // nodes per copy of the original node set
+    int4* st_idx = nullptr;        // [T] staged connectivity of an update
+    float* st_pose = nullptr;      // [9T]
+    float* st_mat = nullptr;       // [3T]
+    int4* old_idx = nullptr;       // [T] published connectivity of the previous update
+    float* old_pose = nullptr;     // [9T]
+    float* old_mat = nullptr;      // [3T]
+    int* old_active = nullptr;     // [T]
+    float* lin_q = nullptr;        // [3P] positions of the last linearisation
+    int* st_active = nullptr;      // [T]
+    int* st_same = nullptr;        // [T] corners equal to the source's
+    int* st_slot = nullptr;        // [16T] SELL entry of each block of an active element
+    int* topo_winner = nullptr;    // [T] per source: lowest element keeping its topology
+    int* reuse_src = nullptr;      // [T] per source: numeric block reusable
+    int* topo_src = nullptr;       // [T] per source: topology kept
+    int* touched = nullptr;        // [P]
+    int* counters = nullptr;       // [8] error code and lineage counters
+    int* entry_count = nullptr;    // [nsell] zero between updates
+    int* node_count = nullptr;     // [P] zero between updates
+    int* diag_entry = nullptr;     // [P] SELL entry of each diagonal block
+    int* scan_part = nullptr;
     // per-step scratch
     float4* elem_force = nullptr;  // [4T + 8H + 3Tri]
     float4* q4 = nullptr;
@@ -235,6 +258,9 @@ struct Handle {
     std::string last_error;
 };
 
+// Handle construction (fem_api.cu); `candidate` reserves per-row sorted columns (streaming Tet4 assembly).
+int create_handle(const FemDesc* d, const std::vector<std::vector<int>>* candidate, FemHandle** out);
+
 // Status reporting shared by every entry point: the message is what
 // fem_status_string returns for the code (fem_api.cu).
 int report(int code, const char* message);
@@ -257,8 +283,17 @@ inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) /
 inline int64_t tet_triplet_offset(const Handle& h) {
     return (int64_t)h.P + 2 * (int64_t)h.S + 3 * (int64_t)h.Tri;
 }
+// --- streaming Tet4 assembly (fem_streaming.cu) ---
+int streaming_candidate(const FemDesc* d, int original_nodes, std::vector<std::vector<int>>& rows, std::string& why);
+cudaError_t streaming_allocate(Handle& h, int original_nodes, const std::vector<int>& diag_entry);
+int streaming_update(Handle& h, const FemDesc* d, const float* q, const int* sources, FemTopologyUpdate* out,
+                     cudaStream_t s, std::string& why);
 // --- launchers (fem_contacts.cu) ---
 int particle_grid_dim(int P);
+// Exclusive scan of count[0, n) into start[0, n] (start[n] = total); part holds
+// scan_partial_count(n) ints.
+int scan_partial_count(int64_t n);
+cudaError_t launch_exclusive_scan(const int* count, int* start, int n, int* part, cudaStream_t s);
 cudaError_t launch_particle_contacts(Handle& h, cudaStream_t s);  // grid build + per-particle force into h.pforce
 cudaError_t launch_soft_contacts(Handle& h, cudaStream_t s);      // per-contact force + per-particle lists
 cudaError_t launch_element_tangent(Handle& h, float dt, cudaStream_t s);

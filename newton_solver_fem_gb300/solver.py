@@ -64,6 +64,19 @@ class BsrMatrix:
         return out
 
 
+class StreamingTetAssembly:
+    """State of prepared tetrahedral updates (reference ``streaming.py`` ``StreamingTetAssembly``).
+
+    The reserved pattern and every update live in the library handle; this
+    object keeps the pool layout and the counters of the last update."""
+
+    def __init__(self, original_node_count: int, node_count: int, element_count: int):
+        self.original_node_count = int(original_node_count)
+        self.copies = node_count // self.original_node_count
+        self.node_count, self.element_count = node_count, element_count
+        self.last_update: dict = {}
+
+
 class SolverFEM:
     """Linearly implicit Backward-Euler FEM solver (reference ``SolverFEM``) on one GB300."""
 
@@ -159,6 +172,8 @@ class SolverFEM:
         self._handle = ctypes.c_void_p()
         self._revision = 0  # matrix revision (refresh_tangent, rebuild_element_blocks, model changes)
         self._prepared_step = None
+        self._streaming = None
+        self._stepped = False
         P = model.particle_count
         # persistent velocity increment, owned here so it is visible as a tensor
         self.dv = torch.zeros((P, 3), dtype=torch.float32, device=self.device)
@@ -275,6 +290,14 @@ class SolverFEM:
         ``particle_q`` (fixed nodes restored in place); the warm start is
         cleared.  The handle's storage is rebuilt, so CUDA graphs captured
         before the call must be captured again.
+
+        After :meth:`prepare_tetrahedral_updates` the edit is applied instead
+        to the reserved pattern in fixed device storage (captured graphs stay
+        valid), validated before anything changes, with ``element_sources`` (a
+        device int32 array of previous element ids per slot, -1 for new
+        elements; default: equal slot ids) for the lineage counters in
+        ``self._streaming.last_update``.  Without prepared updates
+        ``element_sources`` is ignored, as in the reference.
         """
         dt = self.dt if dt is None else float(dt)
         if torch.cuda.is_current_stream_capturing():
@@ -283,18 +306,61 @@ class SolverFEM:
             raise ValueError("Persistent topology updates require the block_diag preconditioner")
         if dt != self.dt:
             raise ValueError("refresh_topology requires the solver's currently assembled timestep")
-        if element_sources is not None:
-            raise NotImplementedError("element_sources belongs to streaming tetrahedral assembly, which is not built")
         if self._topology_signature() != self._topology_storage:
             raise ValueError("Topology updates must preserve model capacities and array storage")
         _f32(particle_q, (self.model.particle_count, 3), "particle_q", self.device)
         self._revision += 1
         d, keep = self._descriptor(self.model, self.fixed_particle_indices, self.linear_solver_maxiter,
                                    self.linear_solver_tolerance)
+        if self._streaming is not None:
+            T = self.model.tet_count
+            if element_sources is not None:
+                src = element_sources
+                if not isinstance(src, torch.Tensor) or src.dtype != torch.int32 or src.ndim != 1 or \
+                        src.numel() < T:
+                    raise ValueError("Element sources must be a capacity-sized int32 array")
+                if src.device != self.device:
+                    raise ValueError("Element sources must reside on the solver device")
+                src = src.contiguous()
+            u = _lib.FemTopologyUpdate()
+            with torch.cuda.device(self.device):
+                _lib.check(self._lib.fem_update_tet_topology(
+                    self._handle, ctypes.byref(d), particle_q.data_ptr(), dt,
+                    None if element_sources is None else src.data_ptr(), ctypes.byref(u), self._stream()),
+                    "refresh_topology")
+            del keep
+            self._streaming.last_update = {name: int(getattr(u, name)) for name, _ in u._fields_}
+            self._streaming.last_update["full_numeric_refresh"] = bool(u.full_numeric_refresh)
+            return
         with torch.cuda.device(self.device):
             _lib.check(self._lib.fem_refresh_topology(self._handle, ctypes.byref(d), particle_q.data_ptr(), dt,
                                                       self._stream()), "refresh_topology")
         del keep
+
+    def prepare_tetrahedral_updates(self, original_node_count: int) -> None:
+        """Reserve persistent sparse connections for duplicated Tet4 basis nodes (reference ``solver.py:693-719``).
+
+        Pool node ``i`` represents original node ``i % original_node_count``;
+        later tetrahedra may use any copy of their original corners.  Needs
+        tetrahedra only, ``block_diag`` and no fixed nodes; call before
+        capturing graphs or stepping.  Afterwards ``refresh_topology`` applies
+        edits to fixed device storage (graphs captured earlier stay valid) and
+        accepts ``element_sources``.
+        """
+        if self.fixed_particle_indices.size:
+            raise ValueError("Streaming topology is not supported with fixed_particle_indices")
+        if torch.cuda.is_current_stream_capturing() or self._stepped:
+            raise RuntimeError("Prepare tetrahedral updates before capturing or stepping the solver")
+        if self._streaming is not None:
+            raise RuntimeError("Tetrahedral updates are already prepared")
+        d, keep = self._descriptor(self.model, self.fixed_particle_indices, self.linear_solver_maxiter,
+                                   self.linear_solver_tolerance)
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.fem_prepare_tet_updates(self._handle, ctypes.byref(d), int(original_node_count),
+                                                         self._stream()), "prepare_tetrahedral_updates")
+        del keep
+        self._revision += 1
+        self._streaming = StreamingTetAssembly(original_node_count, self.model.particle_count, self.model.tet_count)
 
     def __del__(self):
         handle = getattr(self, "_handle", None)
@@ -357,6 +423,7 @@ class SolverFEM:
             _f32(t, (P, 3), name, dev)
         act = self._activations(control)
         self._register_contacts(contacts)
+        self._stepped = True
         code = self._lib.fem_step(
             self._handle, state_in.particle_q.data_ptr(), state_in.particle_qd.data_ptr(),
             state_out.particle_q.data_ptr(), state_out.particle_qd.data_ptr(), state_in.particle_f.data_ptr(),

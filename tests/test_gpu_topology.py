@@ -100,8 +100,8 @@ def test_refresh_topology_rejections():
     solver = make(model, fixed)
     with pytest.raises(ValueError, match="currently assembled timestep"):
         solver.refresh_topology(model.particle_q, DT / 2)
-    with pytest.raises(NotImplementedError, match="streaming"):
-        solver.refresh_topology(model.particle_q, element_sources=torch.zeros(1, dtype=torch.int32, device=DEVICE))
+    # element lineage only matters to prepared (streaming) updates; the sorted path ignores it
+    solver.refresh_topology(model.particle_q, element_sources=torch.zeros(1, dtype=torch.int32, device=DEVICE))
     model.tet_materials = model.tet_materials.clone()  # new storage: not an in-place edit
     with pytest.raises(ValueError, match="capacities and array storage"):
         solver.refresh_topology(model.particle_q)
