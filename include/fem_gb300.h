@@ -176,8 +176,15 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
 #define FEM_TUNE_CTA_THREADS 5       /* threads per PCG CTA: 256, 512, 1024, or 0 = automatic (default): 1024 when there are
                                         at least 32 slices per SM, else 256; the getter returns the size in use */
 #define FEM_TUNE_GRID_CAP 6          /* upper bound on the PCG grid (0 = as many CTAs as fit, the default) */
-#define FEM_TUNE_RESIDENT_STATE 7    /* read-only: 1 when each CTA keeps its rows' x, r, z and inverse diagonal
-                                        blocks in shared memory for the whole solve */
+#define FEM_TUNE_RESIDENT_STATE 7    /* read-only: the resident layout in use (0 none, 1 x/r/z, 2 x/r/z and the
+                                        inverse diagonal blocks kept in each CTA's shared memory for the whole solve) */
+#define FEM_TUNE_BALANCE 8           /* 1: split the rows over the PCG CTAs by each CTA's measured SpMV speed (a few
+                                        10-iteration calibration solves, host-synchronous; results stay deterministic
+                                        for the handle); 0 (default): split by stored blocks only */
+#define FEM_TUNE_RESIDENT_LAYOUT 9   /* requested resident layout: -1 automatic (default), 0, 1 or 2 (see above); taken
+                                        only when it costs no co-resident CTAs */
+#define FEM_TUNE_SPLIT_HEADROOM 10   /* percent more slices than the even share a calibrated split may give one CTA
+                                        (more shared memory per CTA); default 0 */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);

@@ -29,6 +29,9 @@ FEM_TUNE_GRID = 4
 FEM_TUNE_CTA_THREADS = 5
 FEM_TUNE_GRID_CAP = 6
 FEM_TUNE_RESIDENT_STATE = 7
+FEM_TUNE_BALANCE = 8
+FEM_TUNE_RESIDENT_LAYOUT = 9
+FEM_TUNE_SPLIT_HEADROOM = 10
 
 FEM_TERM_SPRING = 1
 FEM_TERM_TET = 2

@@ -163,6 +163,45 @@ int register_soft_contacts(Handle& h, const int32_t* count, const int32_t* parti
     return FEM_OK;
 }
 
+// Contiguous split of the slices over the CTAs that minimises the largest
+// cost / speed, with at most Lmax slices per CTA: bisection on the makespan,
+// each CTA taking (in order) every slice that still fits.
+std::vector<int> split_slices(const std::vector<int64_t>& cost, const std::vector<double>& speed, int Lmax) {
+    const int n = (int)cost.size(), G = (int)speed.size();
+    std::vector<int> start(G + 1, n);
+    auto place = [&](double T, std::vector<int>* out) {
+        int sl = 0;
+        for (int c = 0; c < G; ++c) {
+            if (out) (*out)[c] = sl;
+            const double budget = T * speed[c];
+            double acc = 0.0;
+            int taken = 0;
+            while (sl < n && taken < Lmax && acc + (double)cost[sl] <= budget) {
+                acc += (double)cost[sl];
+                ++sl;
+                ++taken;
+            }
+        }
+        if (out) (*out)[G] = n;
+        return sl == n;
+    };
+    double total = 0.0, vmin = 1e300;
+    for (int64_t c : cost) total += (double)c;
+    for (double v : speed) vmin = std::min(vmin, v);
+    double lo = 0.0, hi = (total + 1.0) / std::max(vmin, 1e-30);
+    if (!place(hi, nullptr)) {  // the slice cap binds: fall back to even counts
+        for (int c = 0; c <= G; ++c) start[c] = (int)((int64_t)n * c / G);
+        return start;
+    }
+    for (int it = 0; it < 64; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (place(mid, nullptr)) hi = mid;
+        else lo = mid;
+    }
+    place(hi, &start);
+    return start;
+}
+
 // (Re)compute the PCG grid for the handle's kernel variant, the per-(CTA,
 // scene) segment tables of the deterministic reductions and the L2-resident
 // slice count.  Allocates (at construction and on a tuning change only).
@@ -174,11 +213,23 @@ int configure_launch(Handle& h) {
     if (err != cudaSuccess) return cuda_status(err, &h);
     const std::vector<int>& slice_scene = h.host_slice_scene;
     const int nscenes = h.nscenes;
+    // slices per CTA: by calibrated speed (FEM_TUNE_BALANCE), else by slice cost
+    // alone; at most slices_per_cta each
+    {
+        std::vector<double> speed(h.grid, 1.0);
+        if (h.balance && (int)h.cta_speed.size() == h.grid) speed = h.cta_speed;
+        h.host_cta_slice0 = split_slices(h.host_slice_cost, speed, h.slices_per_cta);
+        int widest = 0;
+        for (int c = 0; c < h.grid; ++c)
+            widest = std::max(widest, h.host_cta_slice0[c + 1] - h.host_cta_slice0[c]);
+        if (widest > h.slices_per_cta) return set_error(FEM_ERR_CUDA, "slice split exceeds the per-CTA capacity");
+        h.cta_slice0 = upload_plain(h.host_cta_slice0, h.launch_allocations, err);
+    }
     std::vector<int> cta_seg_base(h.grid, 0), cta_first_scene(h.grid, nscenes), scene_seg0(nscenes + 1, 0);
-    int nseg = 0, L = h.slices_per_cta;
+    int nseg = 0;
     std::vector<int> count(nscenes, 0);
     for (int c = 0; c < h.grid; ++c) {
-        int first = c * L, last = std::min(first + L, h.nslices);
+        int first = h.host_cta_slice0[c], last = h.host_cta_slice0[c + 1];
         cta_seg_base[c] = nseg;
         if (first >= last) continue;
         cta_first_scene[c] = slice_scene[first];
@@ -214,6 +265,62 @@ int configure_launch(Handle& h) {
     }
     h.resident_slices = rs;
     return FEM_OK;
+}
+
+// Measure each CTA's SpMV-phase speed on 10-iteration solves of a synthetic
+// right-hand side and re-split the slices by it; a few rounds, keeping the
+// split with the smallest slowest-CTA time.  Host-synchronous; runs on the
+// legacy stream.
+int calibrate_balance(Handle& h) {
+    if (h.P == 0 || h.grid < 2) return FEM_OK;
+    const int rounds = 4;
+    std::vector<float> ones(3 * (size_t)h.P, 1.0f);
+    float *rhs = nullptr, *x = nullptr;
+    unsigned long long* times = nullptr;
+    cudaError_t e = cudaMalloc(&rhs, sizeof(float) * ones.size());
+    if (e == cudaSuccess) e = cudaMalloc(&x, sizeof(float) * ones.size());
+    if (e == cudaSuccess) e = cudaMalloc(&times, sizeof(unsigned long long) * 2 * (size_t)h.grid);
+    if (e == cudaSuccess) e = cudaMemcpy(rhs, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice);
+    std::vector<double> speed(h.grid, 1.0), best_speed = speed;
+    double best = 1e300;
+    int code = FEM_OK;
+    for (int round = 0; round < rounds && e == cudaSuccess && code == FEM_OK; ++round) {
+        h.cta_speed = speed;
+        code = configure_launch(h);
+        if (code != FEM_OK) break;
+        e = cudaMemset(times, 0, sizeof(unsigned long long) * 2 * (size_t)h.grid);
+        if (e != cudaSuccess) break;
+        h.cta_time = times;
+        e = fem::launch_pcg(h, h.dt, 0, nullptr, nullptr, nullptr, nullptr, rhs, x, 1e-30f, 10, false);
+        h.cta_time = nullptr;
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        std::vector<unsigned long long> t(2 * (size_t)h.grid);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(t.data(), times, sizeof(unsigned long long) * t.size(), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) break;
+        double worst = 0.0;
+        std::vector<double> next = speed;
+        for (int c = 0; c < h.grid; ++c) {
+            int64_t cost = 0;
+            for (int sl = h.host_cta_slice0[c]; sl < h.host_cta_slice0[c + 1]; ++sl) cost += h.host_slice_cost[sl];
+            if (cost == 0 || t[2 * c + 1] == 0) continue;
+            const double per_iter = (double)t[2 * c] / (double)t[2 * c + 1];
+            worst = std::max(worst, per_iter);
+            if (per_iter > 0.0) next[c] = (double)cost / per_iter;
+        }
+        if (worst < best) {
+            best = worst;
+            best_speed = speed;
+        }
+        speed = next;
+    }
+    cudaFree(rhs);
+    cudaFree(x);
+    cudaFree(times);
+    if (e != cudaSuccess) return cuda_status(e, &h);
+    if (code != FEM_OK) return code;
+    h.cta_speed = best_speed;
+    return configure_launch(h);
 }
 
 }  // namespace
@@ -668,6 +775,9 @@ int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* ca
     // ---- launch configuration and deterministic-reduction segment tables
     h.host_slice_scene = slice_scene;
     h.host_slice_ptr = slice_ptr;
+    h.host_slice_cost.assign(h.nslices, 0);
+    for (int sl = 0; sl < h.nslices; ++sl)
+        for (int l = 0; l < slice_meta[sl].y; ++l) h.host_slice_cost[sl] += row_nnz[slice_meta[sl].x + l] + 4;
     int code = configure_launch(h);
     if (code != FEM_OK) {
         g_error = h.last_error;
@@ -814,6 +924,10 @@ int fem_prepare_tet_updates(FemHandle* H, const FemDesc* d, int32_t original_nod
     n.grid_cap = h.grid_cap;
     n.timing = h.timing;
     n.mu_scale = h.mu_scale;
+    n.balance = h.balance;
+    n.split_headroom = h.split_headroom;
+    n.resident_pref = h.resident_pref;
+    n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
     if (code == FEM_OK) code = configure_launch(n);
     if (code == FEM_OK) {
@@ -889,6 +1003,10 @@ int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, voi
     n.grid_cap = h.grid_cap;
     n.timing = h.timing;
     n.mu_scale = h.mu_scale;
+    n.balance = h.balance;
+    n.split_headroom = h.split_headroom;
+    n.resident_pref = h.resident_pref;
+    n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
     if (code == FEM_OK) code = configure_launch(n);
     if (code != FEM_OK) {
@@ -976,6 +1094,21 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
     } else if (key == FEM_TUNE_GRID_CAP) {
         if (value < 0 || value > (1 << 20)) return set_error(FEM_ERR_BAD_ARG, "grid cap must be in [0, 2^20]");
         h.grid_cap = (int)value;
+    } else if (key == FEM_TUNE_RESIDENT_LAYOUT) {
+        if (value < -1 || value > 2) return set_error(FEM_ERR_BAD_ARG, "resident layout must be -1, 0, 1 or 2");
+        h.resident_pref = (int)value;
+    } else if (key == FEM_TUNE_SPLIT_HEADROOM) {
+        if (value < 0 || value > 50) return set_error(FEM_ERR_BAD_ARG, "split headroom must be 0..50 percent");
+        h.split_headroom = (int)value;
+    } else if (key == FEM_TUNE_BALANCE) {
+        if (value != 0 && value != 1) return set_error(FEM_ERR_BAD_ARG, "balance must be 0 or 1");
+        h.balance = (int)value;
+        h.cta_speed.clear();
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_status(e, &h);
+        int code = configure_launch(h);
+        if (code == FEM_OK && h.balance) code = calibrate_balance(h);
+        return code;
     } else {
         return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
@@ -995,6 +1128,9 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_CTA_THREADS: *value = h.pcg_threads_used; return FEM_OK;
         case FEM_TUNE_GRID_CAP: *value = h.grid_cap; return FEM_OK;
         case FEM_TUNE_RESIDENT_STATE: *value = h.resident; return FEM_OK;
+        case FEM_TUNE_BALANCE: *value = h.balance; return FEM_OK;
+        case FEM_TUNE_RESIDENT_LAYOUT: *value = h.resident_pref; return FEM_OK;
+        case FEM_TUNE_SPLIT_HEADROOM: *value = h.split_headroom; return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
 }

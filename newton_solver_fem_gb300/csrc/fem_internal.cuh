@@ -57,7 +57,9 @@ struct PcgArgs {
     const unsigned* __restrict__ row_info;  // [P] length | kFixedBit
     const float* __restrict__ minv;  // [P*9]
     int nslices;
-    int slices_per_cta;  // L
+    int slices_per_cta;  // L: the most slices any CTA owns (shared-memory sizing)
+    const int* __restrict__ cta_slice0;  // [grid+1] CTA c owns slices [cta_slice0[c], cta_slice0[c+1])
+    unsigned long long* cta_time;        // [2*grid] SpMV-phase ns and iterations per CTA, or null
     // segment tables for deterministic per-scene reductions
     const int* __restrict__ cta_seg_base;     // [grid]
     const int* __restrict__ cta_first_scene;  // [grid]
@@ -87,7 +89,7 @@ struct PcgArgs {
     float4* zp1;
     float4* stage;   // [2P] (p_i, y_i) handed from phase A to phase B when not staged in shared memory
     int stage_smem;  // 1: the staging lives in the CTA's shared memory
-    int resident;    // 1: x, r, z and the inverse diagonal blocks of the CTA's rows live in shared memory
+    int resident;    // rows' state in shared memory: 0 none, 1 x/r/z, 2 x/r/z and the inverse diagonal blocks
     // control
     unsigned* barrier;
     int* status;
@@ -120,6 +122,14 @@ struct Handle {
     int spmv_unroll = 4;          // block columns in flight per thread in the PCG SpMV (1, 2 or 4)
     int64_t l2_resident_bytes = 0;   // matrix bytes loaded evict_last (-1: 60% of L2); measured slower, so off
     int pcg_threads = 0;             // threads per PCG CTA (256, 512, 1024; 0 = chosen from the problem size)
+    int balance = 0;                 // 1: slices split by calibrated per-CTA speed (FEM_TUNE_BALANCE)
+    int split_headroom = 0;          // % more slices per CTA than the even share a calibrated split may use
+    int resident_pref = -1;          // resident row-state layout: -1 automatic, 0 none, 1 x/r/z, 2 x/r/z + inverse
+    std::vector<double> cta_speed;   // calibrated SpMV speed per CTA index (cost units per ns)
+    std::vector<int64_t> host_slice_cost;  // stored blocks + 4 per live row, per slice
+    std::vector<int> host_cta_slice0;      // the partition in use
+    int* cta_slice0 = nullptr;
+    unsigned long long* cta_time = nullptr;  // set only while calibrating
     int pcg_threads_used = 0;        // the CTA size of the current configuration
     int grid_cap = 0;                // upper bound on the PCG grid (0: co-residency limit only)
     int resident_slices = 0;

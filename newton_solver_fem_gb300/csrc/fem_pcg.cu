@@ -26,6 +26,8 @@
 // record write covers full sectors.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "fem_internal.cuh"
 #include "fem_math.cuh"
 
@@ -245,21 +247,22 @@ struct Smem {
     float4* stage;    // [L * 32 * 2] (p, y) per row, when staged in shared memory
     int* segb;        // [nsc + 1] slice bounds of this CTA's per-scene segments
     int* sseg;        // [S + 1] first segment of every scene (copy of scene_seg0)
-    float* res;       // [L * 32 * kResFloats] resident row state (x, r, z, inverse diagonal block)
+    float* res;       // [L * 32 * res_floats] resident row state (x, r, z[, inverse diagonal block])
     int4* slc;        // [L] this CTA's slices: (first row, row count, scene, SELL base)
     unsigned* rinfo;  // [L * 32] row length | fixed bit of this CTA's rows
     int nsc;          // scenes (segments) this CTA covers
     int segbase;      // this CTA's first segment
 };
 
-// Resident row state, per row of the CTA: x (0-2), r (3-5), z (6-8) and the
-// block-Jacobi inverse (9-17).  With it, the x/r/z update reads and writes
-// shared memory only; the (z, p) record is still written for the gathers.
-constexpr int kResFloats = 18;
+// Resident row state, per row of the CTA: x (0-2), r (3-5), z (6-8) and, in
+// layout 2, the block-Jacobi inverse (9-17; layout 1 reads it from global
+// memory).  With it, the x/r/z update reads and writes shared memory only; the
+// (z, p) record is still written for the gathers.
+__host__ __device__ __forceinline__ int res_floats(int layout) { return layout == 2 ? 18 : 9; }
 
 // The resident state of row `row` (lane `lane` of slice `sl`).
-__device__ __forceinline__ float* res_slot(const Smem& sm, int sl, int first, int lane) {
-    return sm.res + (size_t)((sl - first) * kSlice + lane) * kResFloats;
+__device__ __forceinline__ float* res_slot(const Smem& sm, int sl, int first, int lane, int layout) {
+    return sm.res + (size_t)((sl - first) * kSlice + lane) * res_floats(layout);
 }
 __device__ __forceinline__ float3 res3(const float* s, int k) { return f3(s[k], s[k + 1], s[k + 2]); }
 __device__ __forceinline__ void res3_store(float* s, int k, float3 v) {
@@ -291,7 +294,7 @@ struct SmemLayout {
     size_t part, st, tot, segb, sseg, slc, rinfo, stage, res, total;
 };
 __host__ __device__ __forceinline__ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
-__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage, bool resident) {
+__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage, int resident) {
     SmemLayout m;
     m.part = 0;
     m.st = m.part + align16((size_t)L * 3 * sizeof(float));
@@ -302,7 +305,7 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool st
     m.rinfo = m.slc + align16((size_t)L * sizeof(int4));
     m.stage = m.rinfo + align16((size_t)L * kSlice * sizeof(unsigned));
     m.res = m.stage + (stage ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
-    m.total = m.res + (resident ? (size_t)L * kSlice * kResFloats * sizeof(float) : 0);
+    m.total = m.res + (resident ? (size_t)L * kSlice * res_floats(resident) * sizeof(float) : 0);
     return m;
 }
 
@@ -416,7 +419,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const int S = a.nscenes;
     const int L = a.slices_per_cta;
     Smem sm;
-    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0, a.resident != 0);
+    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0, a.resident);
     sm.part = reinterpret_cast<float*>(smem_raw + lay.part);
     sm.st = reinterpret_cast<SceneState*>(smem_raw + lay.st);
     sm.tot = reinterpret_cast<float*>(smem_raw + lay.tot);
@@ -428,8 +431,9 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     sm.rinfo = reinterpret_cast<unsigned*>(smem_raw + lay.rinfo);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
-    const int first = blockIdx.x * L;
-    const int last = min(first + L, a.nslices);
+    const int first = a.cta_slice0[blockIdx.x];
+    const int last = a.cta_slice0[blockIdx.x + 1];
+    __shared__ unsigned long long s_t0;  // SpMV-phase start (speed calibration only)
     // Launch-constant reduction tables, staged once (the first grid reduction's
     // CTA barrier orders these writes before their use).
     {
@@ -493,7 +497,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 }
                 store3(a.f_ws, row, rhs);
             }
-            if (a.resident) res3_store(res_slot(sm, sl, first, lane), 3, u);
+            if (a.resident) res3_store(res_slot(sm, sl, first, lane, a.resident), 3, u);
             else a.r[row] = f4(u);
             mx = fmaxf(fabsf(rhs.x), fmaxf(fabsf(rhs.y), fabsf(rhs.z)));
         }
@@ -519,7 +523,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             int row = meta.x + lane;
             float sc = st.scale;
             float3 x = f3(0.f, 0.f, 0.f), r = f3(0.f, 0.f, 0.f);
-            float* rs = a.resident ? res_slot(sm, sl, first, lane) : nullptr;
+            float* rs = a.resident ? res_slot(sm, sl, first, lane, a.resident) : nullptr;
             if (!st.zero) {
                 if (a.solve_rhs == nullptr || a.solve_warm) x = xyz(a.x[row]) * sc;  // else solve mode starts from zero
                 r = (a.resident ? res3(rs, 3) : xyz(a.r[row])) * sc;
@@ -532,8 +536,12 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 b = load3(a.f_ws, row) * sc;
             float3 z;
             if (a.resident) {
-                for (int k = 0; k < 9; ++k) rs[9 + k] = a.minv[9 * (size_t)row + k];
-                z = res_minv_mul(rs, r);
+                if (a.resident == 2) {
+                    for (int k = 0; k < 9; ++k) rs[9 + k] = a.minv[9 * (size_t)row + k];
+                    z = res_minv_mul(rs, r);
+                } else {
+                    z = minv_mul(a.minv, row, r);
+                }
                 res3_store(rs, 0, x);
                 res3_store(rs, 3, r);
                 res3_store(rs, 6, z);
@@ -579,6 +587,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         const float4* rec = (it & 1) ? a.zp1 : a.zp0;  // z and p of this iteration
         float4* rec_next = (it & 1) ? a.zp0 : a.zp1;   // (z, p) for the next, written by phase B
         // phase A: p = z + beta p, y = (PAP + I - P) p, partial p.y
+        if (a.cta_time != nullptr && threadIdx.x == 0) s_t0 = global_ns();
         for (int sl = first + warp; sl < last; sl += W) {
             const int4 sl4 = sm.slc[sl - first];
             const int2 meta = make_int2(sl4.x, sl4.y);
@@ -591,7 +600,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 const float beta = st.beta;
                 float3 pc;
                 if (a.resident) {  // own z resident, previous p in this row's staging slot
-                    const float3 zi = res3(res_slot(sm, sl, first, lane), 6);
+                    const float3 zi = res3(res_slot(sm, sl, first, lane, a.resident), 6);
                     pc = firstit ? zi : next_p(f4(zi), stage_slot(a, sm, sl, first, lane, row)[0], beta);
                 } else {
                     const float4 zi = rec[2 * (size_t)row];
@@ -617,6 +626,13 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             SceneState& st = sm.st[s];
             if (st.active) st.alpha = (float)(st.rz / sm.tot[s * 3]);
         };
+        if (a.cta_time != nullptr) {  // speed calibration: this CTA's SpMV-phase time
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                a.cta_time[2 * blockIdx.x] += global_ns() - s_t0;
+                a.cta_time[2 * blockIdx.x + 1] += 1;
+            }
+        }
         if (!reduce_across_grid(a, sm, buf0, 1, false, first, last, epoch, &s_ok, nullptr, set_alpha)) return;
         // phase B: x += alpha p, r -= alpha y, z = M r, partial r.r and r.z
         for (int sl = first + warp; sl < last; sl += W) {
@@ -629,14 +645,14 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 float alpha = st.alpha;
                 const float4* stg = stage_slot(a, sm, sl, first, lane, row);
                 float3 p = xyz(stg[0]), yv = xyz(stg[1]);
-                float* rs = a.resident ? res_slot(sm, sl, first, lane) : nullptr;
+                float* rs = a.resident ? res_slot(sm, sl, first, lane, a.resident) : nullptr;
                 float3 x = a.resident ? res3(rs, 0) : xyz(a.x[row]);
                 float3 r = a.resident ? res3(rs, 3) : xyz(a.r[row]);
                 x = x + p * alpha;
                 r = r - yv * alpha;
                 float3 z;
                 if (a.resident) {
-                    z = res_minv_mul(rs, r);
+                    z = a.resident == 2 ? res_minv_mul(rs, r) : minv_mul(a.minv, row, r);
                     res3_store(rs, 0, x);
                     res3_store(rs, 3, r);
                     res3_store(rs, 6, z);
@@ -682,7 +698,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         if (lane >= meta.y) continue;
         const SceneState& st = sm.st[sl4.z];
         int row = meta.x + lane;
-        float3 dv = a.resident ? res3(res_slot(sm, sl, first, lane), 0) : xyz(a.x[row]);
+        float3 dv = a.resident ? res3(res_slot(sm, sl, first, lane, a.resident), 0) : xyz(a.x[row]);
         float sc = st.scale;
         dv = f3(dv.x / sc, dv.y / sc, dv.z / sc);
         store3(a.dv, row, dv);
@@ -753,14 +769,15 @@ cudaError_t pcg_configure(Handle& h) {
         int grid, L, stage, resident;
         size_t smem;
     };
-    auto fit = [&](bool want_resident, Config& c) -> cudaError_t {
+    auto fit = [&](int want_resident, int slack_pct, Config& c) -> cudaError_t {
         int grid = (h.nslices + warps_per_cta - 1) / warps_per_cta;
         if (grid < 1) grid = 1;
         if (h.grid_cap > 0 && grid > h.grid_cap) grid = h.grid_cap;
         for (int pass = 0;; ++pass) {
-            const int L = (h.nslices + grid - 1) / grid > 0 ? (h.nslices + grid - 1) / grid : 1;
+            int L = (h.nslices + grid - 1) / grid > 0 ? (h.nslices + grid - 1) / grid : 1;
+            if (slack_pct > 0) L += std::max(1, (L * slack_pct + 99) / 100);
             bool stage = stage_in_smem(L, threads) && pass < 16;  // give up shared staging if it never settles
-            bool res = want_resident && stage;
+            int res = stage ? want_resident : 0;
             int per_sm = 0;
             size_t smem = 0;
             for (int attempt = 0; attempt < 3; ++attempt) {
@@ -780,26 +797,40 @@ cudaError_t pcg_configure(Handle& h) {
                 }
                 smem = lay.total;
                 if (per_sm >= 1) break;
-                if (res) res = false;            // first drop the resident state,
+                if (res) res = 0;                // first drop the resident state,
                 else if (stage) stage = false;  // then the shared staging
                 else break;
             }
             if (per_sm < 1) return cudaErrorInvalidConfiguration;
             const int cap = per_sm * sms;
             if (grid <= cap) {
-                c = Config{grid, L, stage ? 1 : 0, res ? 1 : 0, smem};
+                c = Config{grid, L, stage ? 1 : 0, res, smem};
                 return cudaSuccess;
             }
             grid = cap;
         }
     };
     Config plain{}, resident{};
-    err = fit(false, plain);
+    // automatic: x/r/z resident, inverse blocks from global memory (measured at least as
+    // fast as keeping them resident too, with half the shared memory)
+    const int want = h.resident_pref < 0 ? 1 : h.resident_pref;
+    err = fit(0, 0, plain);
     if (err != cudaSuccess) return err;
-    err = fit(true, resident);
-    if (err != cudaSuccess) return err;
+    resident = plain;
+    if (want > 0) {
+        err = fit(want, 0, resident);
+        if (err != cudaSuccess) return err;
+    }
     // keep the resident state only when it costs no co-resident CTAs
-    const Config& c = (resident.resident && resident.grid == plain.grid) ? resident : plain;
+    Config c = (resident.resident && resident.grid == plain.grid) ? resident : plain;
+    if (h.balance && h.split_headroom > 0) {
+        // room for calibrated splits to give a fast CTA more slices than the even
+        // share, taken when it keeps the grid and the resident state
+        Config wide{};
+        err = fit(c.resident, h.split_headroom, wide);
+        if (err != cudaSuccess) return err;
+        if (wide.grid == c.grid && wide.resident == c.resident && wide.stage == c.stage) c = wide;
+    }
     if (c.smem > 48 * 1024) {
         err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
         if (err != cudaSuccess) return err;
@@ -826,6 +857,8 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.minv = h.minv;
     a.nslices = h.nslices;
     a.slices_per_cta = h.slices_per_cta;
+    a.cta_slice0 = h.cta_slice0;
+    a.cta_time = h.cta_time;
     a.cta_seg_base = h.cta_seg_base;
     a.cta_first_scene = h.cta_first_scene;
     a.scene_slice0 = h.scene_slice0;
