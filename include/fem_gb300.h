@@ -185,6 +185,9 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
                                         only when it costs no co-resident CTAs */
 #define FEM_TUNE_SPLIT_HEADROOM 10   /* percent more slices than the even share a calibrated split may give one CTA
                                         (more shared memory per CTA); default 0 */
+#define FEM_TUNE_TAIL_PREFETCH 11    /* when a CTA's second (last) round of slices keeps at most this percent of its
+                                        warps busy, an idle warp requests that round's matrix bytes into L2 during the
+                                        first round; 0 = off, default 50 */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);

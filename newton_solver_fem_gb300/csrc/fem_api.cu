@@ -926,6 +926,7 @@ int fem_prepare_tet_updates(FemHandle* H, const FemDesc* d, int32_t original_nod
     n.mu_scale = h.mu_scale;
     n.balance = h.balance;
     n.split_headroom = h.split_headroom;
+    n.tail_prefetch = h.tail_prefetch;
     n.resident_pref = h.resident_pref;
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
@@ -1005,6 +1006,7 @@ int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, voi
     n.mu_scale = h.mu_scale;
     n.balance = h.balance;
     n.split_headroom = h.split_headroom;
+    n.tail_prefetch = h.tail_prefetch;
     n.resident_pref = h.resident_pref;
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
@@ -1097,6 +1099,10 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
     } else if (key == FEM_TUNE_RESIDENT_LAYOUT) {
         if (value < -1 || value > 2) return set_error(FEM_ERR_BAD_ARG, "resident layout must be -1, 0, 1 or 2");
         h.resident_pref = (int)value;
+    } else if (key == FEM_TUNE_TAIL_PREFETCH) {
+        if (value < 0 || value > 100) return set_error(FEM_ERR_BAD_ARG, "tail prefetch must be 0..100 percent");
+        h.tail_prefetch = (int)value;
+        return FEM_OK;
     } else if (key == FEM_TUNE_SPLIT_HEADROOM) {
         if (value < 0 || value > 50) return set_error(FEM_ERR_BAD_ARG, "split headroom must be 0..50 percent");
         h.split_headroom = (int)value;
@@ -1131,6 +1137,7 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_BALANCE: *value = h.balance; return FEM_OK;
         case FEM_TUNE_RESIDENT_LAYOUT: *value = h.resident_pref; return FEM_OK;
         case FEM_TUNE_SPLIT_HEADROOM: *value = h.split_headroom; return FEM_OK;
+        case FEM_TUNE_TAIL_PREFETCH: *value = h.tail_prefetch; return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
 }

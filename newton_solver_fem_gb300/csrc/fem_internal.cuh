@@ -60,6 +60,7 @@ struct PcgArgs {
     int slices_per_cta;  // L: the most slices any CTA owns (shared-memory sizing)
     const int* __restrict__ cta_slice0;  // [grid+1] CTA c owns slices [cta_slice0[c], cta_slice0[c+1])
     unsigned long long* cta_time;        // [2*grid] SpMV-phase ns and iterations per CTA, or null
+    int tail_prefetch;                   // prefetch a last round keeping at most this % of the warps busy (0 = off)
     // segment tables for deterministic per-scene reductions
     const int* __restrict__ cta_seg_base;     // [grid]
     const int* __restrict__ cta_first_scene;  // [grid]
@@ -124,6 +125,7 @@ struct Handle {
     int pcg_threads = 0;             // threads per PCG CTA (256, 512, 1024; 0 = chosen from the problem size)
     int balance = 0;                 // 1: slices split by calibrated per-CTA speed (FEM_TUNE_BALANCE)
     int split_headroom = 0;          // % more slices per CTA than the even share a calibrated split may use
+    int tail_prefetch = 50;          // FEM_TUNE_TAIL_PREFETCH (percent of warps busy in the last round)
     int resident_pref = -1;          // resident row-state layout: -1 automatic, 0 none, 1 x/r/z, 2 x/r/z + inverse
     std::vector<double> cta_speed;   // calibrated SpMV speed per CTA index (cost units per ns)
     std::vector<int64_t> host_slice_cost;  // stored blocks + 4 per live row, per slice

@@ -140,6 +140,12 @@ __device__ __forceinline__ unsigned long long policy_evict_first() {
     asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
+// Bulk L2 prefetch (no register or shared-memory destination): the address and
+// the size are multiples of 16 bytes.
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ float4 ld_mat4(const float4* p, unsigned long long pol) {
     float4 v;
     asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
@@ -402,6 +408,32 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
     return *s_ok != 0;
 }
 
+// A CTA's warps take its slices round-robin.  When the last round keeps at most
+// tail_prefetch percent of the warps busy (and its second round is also its
+// last), those few warps cannot keep enough loads in flight to cover DRAM
+// latency; so the last warp, idle in that round, requests the
+// round's slices (one contiguous range per value/column plane) into L2 while
+// the first round streams.  The bytes are the same; the last round then reads
+// from L2.  SELL planes start every slice on a 32-entry boundary, so every range
+// is 16-byte aligned; requests are 32 KB.
+constexpr unsigned kPrefetchChunk = 32 * 1024;
+__device__ __forceinline__ void prefetch_range(const void* base, size_t bytes, int lane) {
+    const char* p = static_cast<const char*>(base);
+    for (size_t off = (size_t)lane * kPrefetchChunk; off < bytes; off += 32 * (size_t)kPrefetchChunk)
+        prefetch_l2(p + off, (unsigned)min((size_t)kPrefetchChunk, bytes - off));
+}
+__device__ __noinline__ void prefetch_last_round(const PcgArgs& a, const Smem& sm, int first, int last, int W,
+                                                 int lane) {
+    const int n = last - first;
+    if (n <= W || 100 * (n - W) > a.tail_prefetch * W) return;
+    const int e0 = sm.slc[W].w * kSlice, e1 = __ldg(a.slice_ptr + last) * kSlice;
+    const size_t m = (size_t)(e1 - e0);
+    prefetch_range(a.valA + e0, m * sizeof(float4), lane);
+    prefetch_range(a.valB + e0, m * sizeof(float4), lane);
+    prefetch_range(a.valC + e0, m * sizeof(float), lane);
+    prefetch_range(a.scol + e0, m * sizeof(int), lane);
+}
+
 __device__ __forceinline__ float rhs_scale(float maximum) {
     // kernels.py:1785-1793
     float scale = 1.0f;
@@ -459,6 +491,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const float h = a.dt;
 
     // ---------------- phase 0: RHS (predictor, springs, projection) and u = rhs - A x0
+    if (a.tail_prefetch && warp == W - 1) prefetch_last_round(a, sm, first, last, W, lane);
     for (int sl = first + warp; sl < last; sl += W) {
         const int4 sl4 = sm.slc[sl - first];
         const int2 meta = make_int2(sl4.x, sl4.y);
@@ -588,6 +621,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         float4* rec_next = (it & 1) ? a.zp0 : a.zp1;   // (z, p) for the next, written by phase B
         // phase A: p = z + beta p, y = (PAP + I - P) p, partial p.y
         if (a.cta_time != nullptr && threadIdx.x == 0) s_t0 = global_ns();
+        if (a.tail_prefetch && warp == W - 1) prefetch_last_round(a, sm, first, last, W, lane);
         for (int sl = first + warp; sl < last; sl += W) {
             const int4 sl4 = sm.slc[sl - first];
             const int2 meta = make_int2(sl4.x, sl4.y);
@@ -859,6 +893,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.slices_per_cta = h.slices_per_cta;
     a.cta_slice0 = h.cta_slice0;
     a.cta_time = h.cta_time;
+    a.tail_prefetch = h.tail_prefetch;
     a.cta_seg_base = h.cta_seg_base;
     a.cta_first_scene = h.cta_first_scene;
     a.scene_slice0 = h.scene_slice0;

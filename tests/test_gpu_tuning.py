@@ -49,6 +49,8 @@ VARIANTS = [
     {_lib.FEM_TUNE_BALANCE: 1},
     {_lib.FEM_TUNE_RESIDENT_LAYOUT: 2, _lib.FEM_TUNE_BALANCE: 1},
     {_lib.FEM_TUNE_SPLIT_HEADROOM: 10, _lib.FEM_TUNE_BALANCE: 1},
+    {_lib.FEM_TUNE_TAIL_PREFETCH: 0},
+    {_lib.FEM_TUNE_TAIL_PREFETCH: 100},
 ]
 
 
@@ -76,7 +78,8 @@ def test_calibrated_split_survives_topology_refresh_and_rejects_bad_values():
     lib = _lib.load()
     _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_BALANCE, 1))
     for key, bad in ((_lib.FEM_TUNE_BALANCE, 2), (_lib.FEM_TUNE_RESIDENT_LAYOUT, 3),
-                     (_lib.FEM_TUNE_SPLIT_HEADROOM, -1), (_lib.FEM_TUNE_SPLIT_HEADROOM, 51)):
+                     (_lib.FEM_TUNE_SPLIT_HEADROOM, -1), (_lib.FEM_TUNE_SPLIT_HEADROOM, 51),
+                     (_lib.FEM_TUNE_TAIL_PREFETCH, 101)):
         assert lib.fem_set_tuning(solver._handle, key, bad) == _lib.FEM_ERR_BAD_ARG
     solver.refresh_topology(model.particle_q)
     assert setting(solver, _lib.FEM_TUNE_BALANCE) == 1
