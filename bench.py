@@ -148,12 +148,13 @@ def build_workload(cells: int, device: str):
     return sc, model, solver, np
 
 
-def spmv_bytes(nnzb: int, n: int) -> int:
-    """Algorithmic bytes of one 3x3-BSR SpMV: 36 B values + 4 B column per block, offsets, x read, y write."""
-    return 40 * nnzb + 4 * (n + 1) + 24 * n
+def spmv_bytes(nnzb: int, n: int, col_bytes: int = 4) -> int:
+    """Algorithmic bytes of one 3x3-BSR SpMV: 36 B values + the column index (4 B, or 2 B as a 16-bit
+    offset from the row) per block, offsets, x read, y write."""
+    return (36 + col_bytes) * nnzb + 4 * (n + 1) + 24 * n
 
 
-def pcg_launch_bytes(nnzb: int, n: int, iterations: float) -> float:
+def pcg_launch_bytes(nnzb: int, n: int, iterations: float, col_bytes: int = 4) -> float:
     """Algorithmic bytes of one persistent PCG launch.
 
     Per CG iteration: one SpMV plus 120 B/node (Minv 36, read x r p Ap 48, write x r p 36).
@@ -161,7 +162,8 @@ def pcg_launch_bytes(nnzb: int, n: int, iterations: float) -> float:
     read v, dv, f and write f, r (60 B/node) plus read x, r, f, Minv and write x, r, z (108 B/node).
     Epilogue: read x, v, q and write dv, q, v (72 B/node).
     """
-    return iterations * (spmv_bytes(nnzb, n) + 120 * n) + spmv_bytes(nnzb, n) + (60 + 108 + 72) * n
+    sp = spmv_bytes(nnzb, n, col_bytes)
+    return iterations * (sp + 120 * n) + sp + (60 + 108 + 72) * n
 
 
 def cpu_port(cells: int):
@@ -613,7 +615,10 @@ def run_gb300(args) -> None:
     launches = n_l.value
     iters = (stats1["total_iterations"] - stats0["total_iterations"]) / max(1, launches)
     launch_ms = t_ms.value / max(1, launches)
-    bytes_launch = pcg_launch_bytes(info["nnzb"], P, iters)
+    cc = ctypes.c_int64()
+    _lib.check(lib.fem_get_tuning(solver._handle, _lib.FEM_TUNE_COMPACT_COLUMNS, ctypes.byref(cc)))
+    col_bytes = 2 if cc.value else 4
+    bytes_launch = pcg_launch_bytes(info["nnzb"], P, iters, col_bytes)
     achieved = bytes_launch / (launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = dram_traffic_per_launch()
@@ -660,6 +665,7 @@ def run_gb300(args) -> None:
                        "cg_maxiter": sc.maxiter, "preconditioner": "block_diag", "parallelism": "replicas",
                        "nnzb": info["nnzb"], "mean_cg_iterations": iters,
                        "pcg_split": "rows split over CTAs by calibrated SpMV speed (FEM_TUNE_BALANCE=1)",
+                       "column_index_bytes": col_bytes,
                        "l2": "inputs larger than L2 (A values 259 MB, element blocks 614 MB at 64^3)"},
             "roofline": {"kernel": "pcg_kernel", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,

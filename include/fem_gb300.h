@@ -188,6 +188,9 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
 #define FEM_TUNE_TAIL_PREFETCH 11    /* when a CTA's second (last) round of slices keeps at most this percent of its
                                         warps busy, an idle warp requests that round's matrix bytes into L2 during the
                                         first round; 0 = off, default 50 */
+#define FEM_TUNE_COMPACT_COLUMNS 12  /* 1 (default): the PCG reads 16-bit column offsets (column - row) instead of 32-bit
+                                        columns when every stored block's offset fits; the getter returns whether they
+                                        are in use */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);

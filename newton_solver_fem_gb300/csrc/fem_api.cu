@@ -736,6 +736,17 @@ int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* ca
     h.valB = b.alloc<float4>(nsell);
     h.valC = b.alloc<float>(nsell);
     h.scol = b.upload(scol);
+    {  // 16-bit column offsets for the PCG when every stored block's offset fits
+        bool fits = true;
+        std::vector<short> dcol(nsell, 0);
+        for (int64_t e = 0; e < nsell && fits; ++e) {
+            if (sell_row[e] < 0) continue;
+            const int d = scol[e] - sell_row[e];
+            if (d < -32768 || d > 32767) fits = false;
+            else dcol[e] = (short)d;
+        }
+        if (fits && nsell > 0) h.dcol = b.upload(dcol);
+    }
     h.slice_ptr = b.upload(slice_ptr);
     h.slice_meta = b.upload(slice_meta);
     h.slice_scene = b.upload(slice_scene);
@@ -927,6 +938,7 @@ int fem_prepare_tet_updates(FemHandle* H, const FemDesc* d, int32_t original_nod
     n.balance = h.balance;
     n.split_headroom = h.split_headroom;
     n.tail_prefetch = h.tail_prefetch;
+    n.compact_cols = h.compact_cols;
     n.resident_pref = h.resident_pref;
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
@@ -1007,6 +1019,7 @@ int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, voi
     n.balance = h.balance;
     n.split_headroom = h.split_headroom;
     n.tail_prefetch = h.tail_prefetch;
+    n.compact_cols = h.compact_cols;
     n.resident_pref = h.resident_pref;
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
@@ -1099,6 +1112,9 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
     } else if (key == FEM_TUNE_RESIDENT_LAYOUT) {
         if (value < -1 || value > 2) return set_error(FEM_ERR_BAD_ARG, "resident layout must be -1, 0, 1 or 2");
         h.resident_pref = (int)value;
+    } else if (key == FEM_TUNE_COMPACT_COLUMNS) {
+        if (value != 0 && value != 1) return set_error(FEM_ERR_BAD_ARG, "compact columns must be 0 or 1");
+        h.compact_cols = (int)value;
     } else if (key == FEM_TUNE_TAIL_PREFETCH) {
         if (value < 0 || value > 100) return set_error(FEM_ERR_BAD_ARG, "tail prefetch must be 0..100 percent");
         h.tail_prefetch = (int)value;
@@ -1138,6 +1154,7 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_RESIDENT_LAYOUT: *value = h.resident_pref; return FEM_OK;
         case FEM_TUNE_SPLIT_HEADROOM: *value = h.split_headroom; return FEM_OK;
         case FEM_TUNE_TAIL_PREFETCH: *value = h.tail_prefetch; return FEM_OK;
+        case FEM_TUNE_COMPACT_COLUMNS: *value = h.compact_cols && h.dcol != nullptr; return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
 }

@@ -51,6 +51,7 @@ struct PcgArgs {
     const float4* __restrict__ valB;  // (a11 a12 a20 a21)
     const float* __restrict__ valC;   // a22
     const int* __restrict__ scol;     // block column
+    const short* __restrict__ dcol;   // block column - row (when every offset fits 16 bits), or null
     const int* __restrict__ slice_ptr;   // [nslices+1]
     const int2* __restrict__ slice_meta; // [nslices] (first row, row count)
     const int* __restrict__ slice_scene; // [nslices]
@@ -232,6 +233,8 @@ struct Handle {
     float4* valB = nullptr;
     float* valC = nullptr;
     int* scol = nullptr;
+    short* dcol = nullptr;  // [nsell] column - row when every offset fits 16 bits (the PCG reads these), else null
+    int compact_cols = 1;   // FEM_TUNE_COMPACT_COLUMNS: the PCG reads dcol when it exists
     int* slice_ptr = nullptr;
     int2* slice_meta = nullptr;
     int* slice_scene = nullptr;

@@ -164,18 +164,27 @@ __device__ __forceinline__ int ld_col(const int* p, unsigned long long pol) {
     return v;
 }
 
+__device__ __forceinline__ int ld_dcol(const short* p, unsigned long long pol) {
+    unsigned short v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+    return (int)(short)v;
+}
+
 struct Entry {
     float4 A, B;
     float C;
     int j;
 };
 
-__device__ __forceinline__ Entry load_entry(const PcgArgs& a, size_t e, unsigned long long pol) {
+// One stored block and its column: the 32-bit column, or (C16) the row plus a
+// 16-bit offset, which saves 2 of the 40 bytes a block costs the SpMV.
+template <bool C16>
+__device__ __forceinline__ Entry load_entry(const PcgArgs& a, size_t e, int row, unsigned long long pol) {
     Entry m;
     m.A = ld_mat4(a.valA + e, pol);
     m.B = ld_mat4(a.valB + e, pol);
     m.C = ld_mat1(a.valC + e, pol);
-    m.j = ld_col(a.scol + e, pol);
+    m.j = C16 ? row + ld_dcol(a.dcol + e, pol) : ld_col(a.scol + e, pol);
     return m;
 }
 
@@ -190,16 +199,16 @@ __device__ __forceinline__ float3 gather_p(const float4* rec, int j, float beta)
 // y_row = sum_k A_k p_{j_k}, with p = z (first iteration) or z + beta p_old.
 // U block columns are loaded before any is used, so U entries (and then U
 // gathers) are in flight per thread; the sum keeps the k order of U = 1.
-template <int U, bool FIRST>
-__device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int len, int lane, const float4* rec,
-                                              float beta, unsigned long long pol) {
+template <int U, bool C16, bool FIRST>
+__device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int len, int lane, int row,
+                                              const float4* rec, float beta, unsigned long long pol) {
     float3 acc = f3(0.f, 0.f, 0.f);
     int k = 0;
     if (U > 1) {
         for (; k + U <= len; k += U) {
             Entry m[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) m[u] = load_entry(a, (size_t)(base + k + u) * kSlice + lane, pol);
+            for (int u = 0; u < U; ++u) m[u] = load_entry<C16>(a, (size_t)(base + k + u) * kSlice + lane, row, pol);
             float3 p[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) p[u] = gather_p<FIRST>(rec, m[u].j, beta);
@@ -208,7 +217,7 @@ __device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int le
         }
     }
     for (; k < len; ++k) {
-        Entry m = load_entry(a, (size_t)(base + k) * kSlice + lane, pol);
+        Entry m = load_entry<C16>(a, (size_t)(base + k) * kSlice + lane, row, pol);
         float3 p = gather_p<FIRST>(rec, m.j, beta);
         acc = acc + bmul(m.A, m.B, m.C, p);
     }
@@ -216,15 +225,15 @@ __device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int le
 }
 
 // Prologue pass: cv = sum_k A_k (v_j - v_i) and ax = sum_k A_k x_j in one read of the row.
-template <int U>
-__device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int len, int lane, float3 vi, float3& cv,
-                                              float3& ax, unsigned long long pol) {
+template <int U, bool C16>
+__device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int len, int lane, int row, float3 vi,
+                                              float3& cv, float3& ax, unsigned long long pol) {
     int k = 0;
     if (U > 1) {
         for (; k + U <= len; k += U) {
             Entry m[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) m[u] = load_entry(a, (size_t)(base + k + u) * kSlice + lane, pol);
+            for (int u = 0; u < U; ++u) m[u] = load_entry<C16>(a, (size_t)(base + k + u) * kSlice + lane, row, pol);
             float3 vj[U], xj[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -239,7 +248,7 @@ __device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int le
         }
     }
     for (; k < len; ++k) {
-        Entry m = load_entry(a, (size_t)(base + k) * kSlice + lane, pol);
+        Entry m = load_entry<C16>(a, (size_t)(base + k) * kSlice + lane, row, pol);
         float3 vj = xyz(a.v4[m.j]), xj = xyz(a.x[m.j]);
         cv = cv + bmul(m.A, m.B, m.C, vj - vi);
         ax = ax + bmul(m.A, m.B, m.C, xj);
@@ -431,7 +440,8 @@ __device__ __noinline__ void prefetch_last_round(const PcgArgs& a, const Smem& s
     prefetch_range(a.valA + e0, m * sizeof(float4), lane);
     prefetch_range(a.valB + e0, m * sizeof(float4), lane);
     prefetch_range(a.valC + e0, m * sizeof(float), lane);
-    prefetch_range(a.scol + e0, m * sizeof(int), lane);
+    if (a.dcol != nullptr) prefetch_range(a.dcol + e0, m * sizeof(short), lane);
+    else prefetch_range(a.scol + e0, m * sizeof(int), lane);
 }
 
 __device__ __forceinline__ float rhs_scale(float maximum) {
@@ -441,7 +451,7 @@ __device__ __forceinline__ float rhs_scale(float maximum) {
     return scale;
 }
 
-template <int U>
+template <int U, bool C16>
 __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const unsigned long long pol_last = policy_evict_last();
     const unsigned long long pol_first = policy_evict_first();
@@ -506,7 +516,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 u = rhs;
                 if (a.solve_warm && !(info & kFixedBit)) {
                     float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
-                    row_predictor<U>(a, sl4.w, (int)(info & ~kFixedBit), lane, xyz(a.v4[row]), cv, ax,
+                    row_predictor<U, C16>(a, sl4.w, (int)(info & ~kFixedBit), lane, row, xyz(a.v4[row]), cv, ax,
                                      sl < a.resident_slices ? pol_last : pol_first);
                     u = rhs - ax;
                 }
@@ -515,7 +525,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                     int len = (int)(info & ~kFixedBit);
                     float3 vi = xyz(a.v4[row]);
                     float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
-                    row_predictor<U>(a, sl4.w, len, lane, vi, cv, ax,
+                    row_predictor<U, C16>(a, sl4.w, len, lane, row, vi, cv, ax,
                                      sl < a.resident_slices ? pol_last : pol_first);
                     rhs = load3(a.f_ws, row) - cv;
                     for (int e = a.spring_ptr[row]; e < a.spring_ptr[row + 1]; ++e) {
@@ -645,8 +655,8 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                     int len = (int)(info & ~kFixedBit);
                     int base = sl4.w;
                     unsigned long long pol = sl < a.resident_slices ? pol_last : pol_first;
-                    acc = firstit ? row_times_p<U, true>(a, base, len, lane, rec, beta, pol)
-                                  : row_times_p<U, false>(a, base, len, lane, rec, beta, pol);
+                    acc = firstit ? row_times_p<U, C16, true>(a, base, len, lane, row, rec, beta, pol)
+                                  : row_times_p<U, C16, false>(a, base, len, lane, row, rec, beta, pol);
                 }
                 float4* stg = stage_slot(a, sm, sl, first, lane, row);
                 stg[0] = f4(pc);
@@ -766,11 +776,11 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
 
 using PcgKernel = void (*)(PcgArgs);
 
-PcgKernel pcg_kernel_for(int unroll) {
+PcgKernel pcg_kernel_for(int unroll, bool c16) {
     switch (unroll) {
-        case 2: return pcg_kernel<2>;
-        case 4: return pcg_kernel<4>;
-        default: return pcg_kernel<1>;
+        case 2: return c16 ? pcg_kernel<2, true> : pcg_kernel<2, false>;
+        case 4: return c16 ? pcg_kernel<4, true> : pcg_kernel<4, false>;
+        default: return c16 ? pcg_kernel<1, true> : pcg_kernel<1, false>;
     }
 }
 
@@ -788,7 +798,7 @@ cudaError_t pcg_configure(Handle& h) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return cudaErrorNotSupported;
-    PcgKernel kern = pcg_kernel_for(h.spmv_unroll);
+    PcgKernel kern = pcg_kernel_for(h.spmv_unroll, h.dcol != nullptr && h.compact_cols);
     // Automatic CTA size: 1024-thread CTAs once there are 8 slices per SM (fewer
     // CTAs make the grid reductions cheaper: on a 3,677-slice Tet4 system 115
     // such CTAs beat 460 of 256 threads by 8% per CG iteration); small systems
@@ -885,6 +895,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.valB = h.valB;
     a.valC = h.valC;
     a.scol = h.scol;
+    a.dcol = h.compact_cols ? h.dcol : nullptr;
     a.slice_ptr = h.slice_ptr;
     a.slice_meta = h.slice_meta;
     a.slice_scene = h.slice_scene;
@@ -944,7 +955,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, pcg_kernel_for(h.spmv_unroll), a);
+    return cudaLaunchKernelEx(&cfg, pcg_kernel_for(h.spmv_unroll, a.dcol != nullptr), a);
 }
 
 }  // namespace fem

@@ -51,6 +51,7 @@ VARIANTS = [
     {_lib.FEM_TUNE_SPLIT_HEADROOM: 10, _lib.FEM_TUNE_BALANCE: 1},
     {_lib.FEM_TUNE_TAIL_PREFETCH: 0},
     {_lib.FEM_TUNE_TAIL_PREFETCH: 100},
+    {_lib.FEM_TUNE_COMPACT_COLUMNS: 0},
 ]
 
 
