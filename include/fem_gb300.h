@@ -19,6 +19,8 @@
  *   fem_get_stats                SolverFEM.last_cg_iters             solver.py:279, 1333-1335
  *   fem_eval_forces              SolverFEM.eval_*_forces             solver.py:1357-1600
  *   fem_set_soft_contacts        Contacts.soft_contact_* into step   solver.py:1540-1566
+ *   fem_set_surface_contacts     SolverFEM.set_soft_surface_contacts solver.py:510-540
+ *   fem_update_surface_contacts  SoftBodySurfaceContacts.update      soft_surface_contacts.py:226-237
  *   fem_prepare_tet_updates      SolverFEM.prepare_tetrahedral_updates solver.py:693-719
  *   fem_update_tet_topology      refresh_topology(element_sources=)   solver.py:872-940, streaming.py:549-700
  *   fem_export_bsr               SolverFEM.A_bsr (Warp BsrMatrix)    solver.py:322-337
@@ -68,7 +70,8 @@ extern "C" {
 #define FEM_TERM_TRI 64           /* triangle membrane, kernels.py:876-960 */
 #define FEM_TERM_PARTICLE 128     /* hash-grid particle-particle contact, kernels.py:1036-1114 */
 #define FEM_TERM_SOFT_CONTACT 256 /* soft-rigid contact list, kernels.py:1198-1261 */
-#define FEM_TERM_ALL 511
+#define FEM_TERM_SURFACE 512      /* soft-body surface contacts, soft_surface_contacts.py */
+#define FEM_TERM_ALL 1023
 
 typedef struct FemHandle FemHandle;
 
@@ -214,6 +217,22 @@ int fem_get_timing(FemHandle* handle, double* pcg_ms_total, int64_t* launches);
  * larger capacity than before allocates scratch, so register before capture. */
 int fem_set_soft_contacts(FemHandle* handle, const int32_t* count, const int32_t* particle, const float* body_pos,
                           const float* body_vel, const float* normal, int32_t capacity);
+
+/* Soft-body surface contacts (SolverFEM.set_soft_surface_contacts, solver.py:510-540;
+ * soft_surface_contacts.py).  body_count bodies, body b owning particles
+ * [body_start[b], body_start[b] + body_size[b]) and the surface triangles
+ * triangles[tri_offsets[b] .. tri_offsets[b+1]) (3 local indices each; HOST
+ * arrays).  Each surface vertex feels the other bodies' surfaces within their
+ * rest bounding-box diagonal: penetration r - signed distance (sign from the
+ * angle-weighted pseudonormal), force n (ke pen - kd min(v.n, 0)).  The
+ * surfaces take the positions q (DEVICE [P,3]) now and at every refit.
+ * body_count 0 clears the registration.  Allocates: call before capture. */
+int fem_set_surface_contacts(FemHandle* handle, int32_t body_count, const int32_t* body_start, const int32_t* body_size,
+                             const int32_t* tri_offsets, const int32_t* triangles, float ke, float kd, const float* q,
+                             void* stream);
+/* Refit the registered surfaces at q (SoftBodySurfaceContacts.update); also
+ * done by the first fem_refresh_tangent and by fem_rebuild_element_blocks. */
+int fem_update_surface_contacts(FemHandle* handle, const float* q, void* stream);
 
 /* Selected force terms (FEM_TERM_* bits), unscaled, summed into out[P,3]. */
 int fem_eval_forces(FemHandle* handle, const float* q, const float* v, const float* activations,

@@ -44,7 +44,8 @@ FEM_TERM_DAMPING = 32
 FEM_TERM_TRI = 64
 FEM_TERM_PARTICLE = 128
 FEM_TERM_SOFT_CONTACT = 256
-FEM_TERM_ALL = 511
+FEM_TERM_SURFACE = 512
+FEM_TERM_ALL = 1023
 
 _f = ctypes.c_float
 _i32 = ctypes.c_int32
@@ -154,6 +155,8 @@ SIGNATURES = [
     ("fem_velocity_increment_ptr", _p, [_p]),
     ("fem_get_stats", _i32, [_p, ctypes.POINTER(FemStats), _p, _p]),
     ("fem_set_soft_contacts", _i32, [_p, _p, _p, _p, _p, _p, _i32]),
+    ("fem_set_surface_contacts", _i32, [_p, _i32, _p, _p, _p, _p, _f, _f, _p, _p]),
+    ("fem_update_surface_contacts", _i32, [_p, _p, _p]),
     ("fem_set_timing", _i32, [_p, _i32]),
     ("fem_get_timing", _i32, [_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]),
     ("fem_eval_forces", _i32, [_p, _p, _p, _p, _p, _i32, _p, _p]),

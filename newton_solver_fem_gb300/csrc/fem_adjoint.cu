@@ -555,9 +555,10 @@ int fem_force_vjp(FemHandle* H, const float* q, const float* v, const float* act
         return fem::report(FEM_ERR_BAD_ARG, "fem_force_vjp: null argument");
     Handle& h = H->h;
     if (h.P == 0) return FEM_OK;
-    if (h.pcontact || h.sc_cap > 0)
+    if (h.pcontact || h.sc_cap > 0 || h.sf_active)
         return fem::report(FEM_ERR_UNSUPPORTED,
-                           "fem_force_vjp: particle and soft contacts are not differentiated (fixed-matrix contract)");
+                           "fem_force_vjp: particle, soft and surface contacts are not differentiated (fixed-matrix "
+                           "contract)");
     AdjDeviceGuard g(H->device);
     cudaStream_t s = (cudaStream_t)stream;
     if (h.elem_grad == nullptr && (h.T > 0 || h.H > 0 || h.Tri > 0)) {  // first call: adjoint scratch

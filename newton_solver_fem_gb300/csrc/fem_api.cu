@@ -132,6 +132,25 @@ T* upload_plain(const std::vector<T>& v, std::vector<void*>& owned, cudaError_t&
     return (T*)p;
 }
 
+// Re-register the surface contacts of a handle being replaced on the new one
+// (topology rebuilds), refitted at q.
+int carry_surfaces(const Handle& from, Handle& to, const float* q) {
+    std::string why;
+    const int nb = (int)from.sf_host_start.size();
+    int code = fem::surface_register(to, nb, from.sf_host_start.data(), from.sf_host_size.data(),
+                                     from.sf_host_toff.data(), from.sf_host_tris.data(), from.sf_ke, from.sf_kd, q,
+                                     nullptr, why);
+    if (code == FEM_ERR_BAD_ARG) return set_error(code, why);
+    if (code == FEM_OK) {
+        to.sf_host_start = from.sf_host_start;
+        to.sf_host_size = from.sf_host_size;
+        to.sf_host_toff = from.sf_host_toff;
+        to.sf_host_tris = from.sf_host_tris;
+        to.tangent_refreshes = from.tangent_refreshes;
+    }
+    return code;
+}
+
 // Register (or clear, capacity 0) the caller's soft-contact list; grows the
 // per-contact scratch and allocates the per-node list heads on first use.
 int register_soft_contacts(Handle& h, const int32_t* count, const int32_t* particle, const float* body_pos,
@@ -868,6 +887,51 @@ int fem_set_soft_contacts(FemHandle* H, const int32_t* count, const int32_t* par
     return register_soft_contacts(H->h, count, particle, body_pos, body_vel, normal, capacity);
 }
 
+int fem_set_surface_contacts(FemHandle* H, int32_t body_count, const int32_t* body_start, const int32_t* body_size,
+                             const int32_t* tri_offsets, const int32_t* triangles, float ke, float kd, const float* q,
+                             void* stream) {
+    if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "fem_set_surface_contacts: null handle");
+    Handle& h = H->h;
+    if (body_count < 0) return set_error(FEM_ERR_BAD_ARG, "fem_set_surface_contacts: negative body count");
+    if (body_count > 0 && (!body_start || !body_size || !tri_offsets || !q || (tri_offsets[body_count] > 0 && !triangles)))
+        return set_error(FEM_ERR_BAD_ARG, "fem_set_surface_contacts: null array");
+    if (body_count > 0 && tri_offsets[0] != 0)
+        return set_error(FEM_ERR_BAD_ARG, "fem_set_surface_contacts: triangle offsets must start at 0");
+    for (int b = 0; b < body_count; ++b) {  // validate before replacing the current registration
+        if (body_start[b] < 0 || body_size[b] < 0 || (int64_t)body_start[b] + body_size[b] > h.P)
+            return set_error(FEM_ERR_BAD_ARG, "fem_set_surface_contacts: body ranges must lie inside the particles");
+        if (tri_offsets[b + 1] < tri_offsets[b])
+            return set_error(FEM_ERR_BAD_ARG, "fem_set_surface_contacts: triangle offsets must not decrease");
+        for (int64_t k = 3 * (int64_t)tri_offsets[b]; k < 3 * (int64_t)tri_offsets[b + 1]; ++k)
+            if (triangles[k] < 0 || triangles[k] >= body_size[b])
+                return set_error(FEM_ERR_BAD_ARG,
+                                 "fem_set_surface_contacts: surface triangle indices must be local to their body");
+    }
+    DeviceGuard g(H->device);
+    h.sf_active = 0;
+    h.sf_host_start.clear();
+    h.sf_host_size.clear();
+    h.sf_host_toff.clear();
+    h.sf_host_tris.clear();
+    if (body_count == 0 || h.P == 0) return FEM_OK;
+    std::string why;
+    const int code = fem::surface_register(h, body_count, body_start, body_size, tri_offsets, triangles, ke, kd, q,
+                                           (cudaStream_t)stream, why);
+    if (code == FEM_ERR_BAD_ARG) return set_error(code, "fem_set_surface_contacts: " + why);
+    if (code != FEM_OK) return code;
+    h.sf_host_start.assign(body_start, body_start + body_count);
+    h.sf_host_size.assign(body_size, body_size + body_count);
+    h.sf_host_toff.assign(tri_offsets, tri_offsets + body_count + 1);
+    h.sf_host_tris.assign(triangles, triangles + 3 * (size_t)tri_offsets[body_count]);
+    return FEM_OK;
+}
+
+int fem_update_surface_contacts(FemHandle* H, const float* q, void* stream) {
+    if (H == nullptr || q == nullptr) return set_error(FEM_ERR_BAD_ARG, "fem_update_surface_contacts: null argument");
+    DeviceGuard g(H->device);
+    return cuda_status(fem::surface_refit(H->h, q, (cudaStream_t)stream), &H->h);
+}
+
 int fem_set_timing(FemHandle* H, int32_t enable) {
     if (H == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle");
     H->h.timing = enable != 0;
@@ -943,6 +1007,7 @@ int fem_prepare_tet_updates(FemHandle* H, const FemDesc* d, int32_t original_nod
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
     if (code == FEM_OK) code = configure_launch(n);
+    if (code == FEM_OK && !h.sf_host_start.empty()) code = carry_surfaces(h, n, h.rest);
     if (code == FEM_OK) {
         std::vector<int> diag(h.P);
         for (int r = 0; r < h.P; ++r) {
@@ -1024,6 +1089,7 @@ int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, voi
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
     if (code == FEM_OK) code = configure_launch(n);
+    if (code == FEM_OK && !h.sf_host_start.empty()) code = carry_surfaces(h, n, q);
     if (code != FEM_OK) {
         fem_destroy(fresh);
         return code;
@@ -1057,7 +1123,12 @@ int fem_refresh_tangent(FemHandle* H, float* q, float dt, void* stream) {
     if (err == cudaSuccess) err = fem::launch_gather(h, s);
     if (err == cudaSuccess && h.streaming)  // the linearisation the next topology update compares against
         err = cudaMemcpyAsync(h.lin_q, q, sizeof(float) * 3 * (size_t)h.P, cudaMemcpyDeviceToDevice, s);
-    if (err == cudaSuccess) h.dt = dt;
+    if (err == cudaSuccess && h.tangent_refreshes == 0)  // the first refresh refits the surfaces (solver.py:824-827, 669-670)
+        err = fem::surface_refit(h, q, s);
+    if (err == cudaSuccess) {
+        h.dt = dt;
+        h.tangent_refreshes += 1;
+    }
     return cuda_status(err, &h);
 }
 
@@ -1073,6 +1144,7 @@ int fem_rebuild_element_blocks(FemHandle* H, float* q, float dt, void* stream) {
     cudaError_t err = fem::launch_node_prepare(h, q, nullptr, true, false, false, s);
     if (err == cudaSuccess) err = fem::launch_element_tangent(h, dt, s);
     if (err == cudaSuccess) err = fem::launch_gather(h, s);
+    if (err == cudaSuccess) err = fem::surface_refit(h, q, s);  // solver.py:669-670
     return cuda_status(err, &h);
 }
 

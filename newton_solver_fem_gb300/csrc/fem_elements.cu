@@ -259,6 +259,7 @@ struct NodeForceArgs {
     const int* sc_head;       // soft-contact list per node, or null
     const int* sc_next;
     const float4* sc_force;
+    const float4* sforce;     // surface-contact force per node, or null
     const float* mass;
     const float* inv_mass;
     const float* radius;
@@ -277,14 +278,16 @@ struct NodeForceArgs {
 
 // Reference solver.py:542-589 (term order), kernels.py:176-218 (springs),
 // 221-291 (bend torque), 1132-1195 (ground), 1198-1261 (soft contacts),
-// 1273-1307 (gravity, damping).  Term order: spring, tet, hex, tri, particle,
-// ground, soft contact, gravity, damping.
+// 1273-1307 (gravity, damping), soft_surface_contacts.py (surface).  Term
+// order: spring, tet, hex, tri, particle, ground, soft contact, gravity,
+// damping, surface.
 __global__ void node_forces_kernel(NodeForceArgs a) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.P) return;
     float3 xi = xyz(a.q4[i]), vi = xyz(a.v4[i]);
     float3 zero = f3(0.f, 0.f, 0.f);
-    float3 fs = zero, ft = zero, fh = zero, ftri = zero, fp = zero, fg = zero, fsc = zero, fgr = zero, fd = zero;
+    float3 fs = zero, ft = zero, fh = zero, ftri = zero, fp = zero, fg = zero, fsc = zero, fgr = zero, fd = zero,
+           fsf = zero;
     // The incident springs and element corners are read kSpringBatch /
     // kCornerBatch at a time (ids, then the data they index) before any is
     // added, so that many independent loads are in flight; the sums keep the
@@ -402,6 +405,7 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
     if ((a.terms & FEM_TERM_DAMPING) && active && a.linear_damping > 0.0f) {
         fd = vi * (-a.linear_damping * a.mass[i]);
     }
+    if ((a.terms & FEM_TERM_SURFACE) && a.sforce != nullptr) fsf = xyz(a.sforce[i]);
     float3 f;
     if (a.scale_by_dt) {
         float h = a.dt;
@@ -414,9 +418,10 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
         f = f + fsc * h;
         f = f + fgr * h;
         f = f + fd * h;
+        f = f + fsf * h;
         if (a.ext != nullptr) f = f + load3(a.ext, i) * h;
     } else {
-        f = fs + ft + fh + ftri + fp + fg + fsc + fgr + fd;
+        f = fs + ft + fh + ftri + fp + fg + fsc + fgr + fd + fsf;
     }
     store3(a.out, i, f);
 }
@@ -728,6 +733,12 @@ cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity
     a.sc_head = nullptr;
     a.sc_next = nullptr;
     a.sc_force = nullptr;
+    a.sforce = nullptr;
+    if ((terms & FEM_TERM_SURFACE) && h.sf_active && h.sf_nsurf > 0 && h.sf_nbody > 1) {
+        cudaError_t err = launch_surface_contacts(h, s);
+        if (err != cudaSuccess) return err;
+        a.sforce = h.sf_force;
+    }
     if ((terms & FEM_TERM_PARTICLE) && h.pcontact) {
         cudaError_t err = launch_particle_contacts(h, s);
         if (err != cudaSuccess) return err;

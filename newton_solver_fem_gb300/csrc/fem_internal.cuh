@@ -137,6 +137,7 @@ struct Handle {
     int grid_cap = 0;                // upper bound on the PCG grid (0: co-residency limit only)
     int resident_slices = 0;
     bool tangent_prepared = false;
+    int tangent_refreshes = 0;       // fem_refresh_tangent calls (the first one refits the surfaces)
     // node data
     float* rest = nullptr;
     float* mass = nullptr;
@@ -214,6 +215,26 @@ struct Handle {
     int* node_count = nullptr;     // [P] zero between updates
     int* diag_entry = nullptr;     // [P] SELL entry of each diagonal block
     int* scan_part = nullptr;
+    // soft-body surface contacts (per-body triangle surfaces with BVHs)
+    int sf_active = 0, sf_nbody = 0, sf_ntri = 0, sf_nsurf = 0, sf_nnode = 0, sf_nleaf = 0, sf_nvert = 0;
+    float sf_ke = 0.f, sf_kd = 0.f;
+    int4* sf_tri = nullptr;        // [ntri] (i, j, k, body), leaf order
+    int4* sf_node = nullptr;       // [nnode] (left, right, first tri, tri count)
+    int* sf_parent = nullptr;      // [nnode]
+    int* sf_root = nullptr;        // [nbody] root node or -1
+    float* sf_max_dist = nullptr;  // [nbody] rest bounding-box diagonal
+    int* sf_surf = nullptr;        // [nsurf] surface particles
+    int* sf_surf_body = nullptr;   // [nsurf]
+    int* sf_adj = nullptr;         // [3 ntri] triangle across each edge or -1
+    int* sf_vslot = nullptr;       // [P] mesh-vertex slot or -1
+    int* sf_verts = nullptr;       // [nvert] mesh vertices
+    int* sf_vt_ptr = nullptr;      // [nvert+1] incident (triangle, corner) lists
+    int* sf_vt = nullptr;
+    int* sf_leaves = nullptr;      // [nleaf]
+    int* sf_arrivals = nullptr;    // [nnode] refit counters
+    float4 *sf_x = nullptr, *sf_force = nullptr;  // [P] refit positions, surface force
+    float4 *sf_fn = nullptr, *sf_en = nullptr, *sf_vn = nullptr, *sf_lo = nullptr, *sf_hi = nullptr;
+    std::vector<int> sf_host_start, sf_host_size, sf_host_toff, sf_host_tris;  // registration (re-applied on rebuild)
     // per-step scratch
     float4* elem_force = nullptr;  // [4T + 8H + 3Tri]
     float4* q4 = nullptr;
@@ -303,6 +324,12 @@ int streaming_candidate(const FemDesc* d, int original_nodes, std::vector<std::v
 cudaError_t streaming_allocate(Handle& h, int original_nodes, const std::vector<int>& diag_entry);
 int streaming_update(Handle& h, const FemDesc* d, const float* q, const int* sources, FemTopologyUpdate* out,
                      cudaStream_t s, std::string& why);
+// --- soft-body surface contacts (fem_surface.cu) ---
+int surface_register(Handle& h, int nbody, const int32_t* body_start, const int32_t* body_size,
+                     const int32_t* tri_offsets, const int32_t* triangles, float ke, float kd, const float* q,
+                     cudaStream_t s, std::string& why);
+cudaError_t surface_refit(Handle& h, const float* q, cudaStream_t s);
+cudaError_t launch_surface_contacts(Handle& h, cudaStream_t s);  // into h.sf_force
 // --- launchers (fem_contacts.cu) ---
 int particle_grid_dim(int P);
 // Exclusive scan of count[0, n) into start[0, n] (start[n] = total); part holds

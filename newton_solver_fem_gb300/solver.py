@@ -16,8 +16,8 @@ Implemented hot-path options: ``solver_type="cg"`` with ``preconditioner_type``
 the optional bend torque, hash-grid particle-particle contact, soft-rigid
 contacts (``contacts.soft_contact_*``), analytic ground, gravity, linear
 damping, tet activations, fixed nodes, batched independent scenes
-(``model.scene_offsets``).  Other Krylov types and the mesh-BVH surface
-contacts are outside this path.
+(``model.scene_offsets``), soft-body surface contacts
+(``set_soft_surface_contacts``).  Other Krylov types are outside this path.
 """
 
 from __future__ import annotations
@@ -62,6 +62,37 @@ class BsrMatrix:
             r, c = rows[k], columns[k]
             out[3 * r:3 * r + 3, 3 * c:3 * c + 3] += values[k]
         return out
+
+
+class SoftBodySurfaceContacts:
+    """Registered surface-contact geometry (reference ``soft_surface_contacts.py``).
+
+    The surfaces and their BVHs live in the library handle; ``update`` refits
+    them at new positions, ``eval_forces`` evaluates the surface term alone."""
+
+    def __init__(self, solver, particle_ranges, surface_triangles_list, ke: float, kd: float):
+        self._solver = solver
+        self.ke, self.kd = float(ke), float(kd)
+        self.n_bodies = len(particle_ranges)
+        self.particle_ranges = [(int(a), int(b)) for a, b in particle_ranges]
+
+    def update(self, particle_q: torch.Tensor) -> None:
+        """Refit every body's surface at particle_q (SoftBodySurfaceContacts.update)."""
+        sv = self._solver
+        _f32(particle_q, (sv.model.particle_count, 3), "particle_q", sv.device)
+        _lib.check(sv._lib.fem_update_surface_contacts(sv._handle, particle_q.data_ptr(), sv._stream()),
+                   "surface contacts")
+
+    def eval_forces(self, particle_q, particle_v, particle_radius=None, particle_flags=None, particle_count=None):
+        """Surface contact force per particle at (particle_q, particle_v), with the model's radii and flags."""
+        sv = self._solver
+
+        class _S:
+            pass
+
+        st = _S()
+        st.particle_q, st.particle_qd = particle_q, particle_v
+        return sv._forces(st, _lib.FEM_TERM_SURFACE)
 
 
 class StreamingTetAssembly:
@@ -174,6 +205,7 @@ class SolverFEM:
         self._prepared_step = None
         self._streaming = None
         self._stepped = False
+        self._soft_surface_contacts = None
         P = model.particle_count
         # persistent velocity increment, owned here so it is visible as a tensor
         self.dv = torch.zeros((P, 3), dtype=torch.float32, device=self.device)
@@ -336,6 +368,46 @@ class SolverFEM:
             _lib.check(self._lib.fem_refresh_topology(self._handle, ctypes.byref(d), particle_q.data_ptr(), dt,
                                                       self._stream()), "refresh_topology")
         del keep
+
+    def set_soft_surface_contacts(self, particle_ranges, surface_triangles_list, ke: float = 1.0e3,
+                                  kd: float = 1.0e2) -> None:
+        """Register per-body surface meshes for soft-soft contacts (reference ``solver.py:510-540``).
+
+        ``particle_ranges`` lists ``(start, count)`` particle slices, one per
+        body; ``surface_triangles_list`` the per-body ``(T_i, 3)`` triangles with
+        body-local indices (``None`` for a body without surface).  Each surface
+        vertex is pushed out of the other bodies' surfaces (penalty ``ke``,
+        damping ``kd``).  The surfaces take the current model positions now and
+        are refitted by the first ``refresh_tangent``, by every
+        ``rebuild_element_blocks`` and by ``soft_surface_contacts.update``.
+        Call before capturing graphs.
+        """
+        if torch.cuda.is_current_stream_capturing():
+            raise RuntimeError("Register surface contacts before CUDA graph capture")
+        if len(particle_ranges) != len(surface_triangles_list):
+            raise ValueError("particle_ranges and surface_triangles_list must have one entry per body")
+        starts, sizes, offsets, tris = [], [], [0], []
+        for (start, count), t in zip(particle_ranges, surface_triangles_list):
+            starts.append(int(start))
+            sizes.append(int(count))
+            t = np.zeros((0, 3), np.int32) if t is None else np.asarray(t, np.int32).reshape(-1, 3)
+            tris.append(t)
+            offsets.append(offsets[-1] + len(t))
+        starts = np.asarray(starts, np.int32)
+        sizes = np.asarray(sizes, np.int32)
+        offsets = np.asarray(offsets, np.int32)
+        tris = np.ascontiguousarray(np.concatenate(tris) if tris else np.zeros((0, 3), np.int32), np.int32)
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.fem_set_surface_contacts(
+                self._handle, len(starts), starts.ctypes.data, sizes.ctypes.data, offsets.ctypes.data,
+                tris.ctypes.data if len(tris) else None, float(ke), float(kd), self.model.particle_q.data_ptr(),
+                self._stream()), "set_soft_surface_contacts")
+        self._soft_surface_contacts = SoftBodySurfaceContacts(self, particle_ranges, surface_triangles_list, ke, kd)
+
+    @property
+    def soft_surface_contacts(self):
+        """Registered surface contact geometry, or None."""
+        return self._soft_surface_contacts
 
     def prepare_tetrahedral_updates(self, original_node_count: int) -> None:
         """Reserve persistent sparse connections for duplicated Tet4 basis nodes (reference ``solver.py:693-719``).

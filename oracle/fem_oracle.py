@@ -377,6 +377,124 @@ def soft_contact_forces(x, v, radius, count, particle, body_pos, body_vel, norma
     return f
 
 
+def closest_on_triangles(p, a, b, c):
+    """Closest points of triangles (a, b, c) [n, 3] to the point p, and their feature codes
+    (0 face, 1..3 edge ab, bc, ca, 4..6 vertex a, b, c): the Voronoi-region method."""
+    ab, ac, ap = b - a, c - a, p - a
+    d1, d2 = np.sum(ab * ap, 1), np.sum(ac * ap, 1)
+    bp = p - b
+    d3, d4 = np.sum(ab * bp, 1), np.sum(ac * bp, 1)
+    cp = p - c
+    d5, d6 = np.sum(ab * cp, 1), np.sum(ac * cp, 1)
+    vc = d1 * d4 - d3 * d2
+    vb = d5 * d2 - d1 * d6
+    va = d3 * d6 - d5 * d4
+    n = len(a)
+    out = np.zeros((n, 3))
+    feat = np.full(n, -1)
+    done = np.zeros(n, bool)
+
+    def take(mask, pts, code):
+        m = mask & ~done
+        out[m] = pts[m]
+        feat[m] = code
+        done[m] = True
+
+    with np.errstate(divide="ignore", invalid="ignore"):
+        take((d1 <= 0) & (d2 <= 0), a, 4)
+        take((d3 >= 0) & (d4 <= d3), b, 5)
+        take((vc <= 0) & (d1 >= 0) & (d3 <= 0), a + ab * (d1 / (d1 - d3))[:, None], 1)
+        take((d6 >= 0) & (d5 <= d6), c, 6)
+        take((vb <= 0) & (d2 >= 0) & (d6 <= 0), a + ac * (d2 / (d2 - d6))[:, None], 3)
+        take((va <= 0) & ((d4 - d3) >= 0) & ((d5 - d6) >= 0),
+             b + (c - b) * ((d4 - d3) / ((d4 - d3) + (d5 - d6)))[:, None], 2)
+        denom = 1.0 / (va + vb + vc)
+        take(np.ones(n, bool), a + ab * (vb * denom)[:, None] + ac * (vc * denom)[:, None], 0)
+    return out, feat
+
+
+def surface_pseudonormals(x, tris):
+    """Unit face normals, angle-weighted vertex pseudonormals (dict node -> normal) and edge
+    pseudonormals (face normal plus the adjacent one) of a triangle surface at positions x."""
+    x = np.asarray(x, np.float64)
+    a, b, c = x[tris[:, 0]], x[tris[:, 1]], x[tris[:, 2]]
+    fn = np.cross(b - a, c - a)
+    fn = fn / np.maximum(np.linalg.norm(fn, axis=1, keepdims=True), 1e-300)
+
+    def angle(p, q, r):
+        u, w = q - p, r - p
+        cosv = np.sum(u * w, 1) / (np.linalg.norm(u, axis=1) * np.linalg.norm(w, axis=1))
+        return np.arccos(np.clip(cosv, -1.0, 1.0))
+
+    vn = {}
+    for k, ang in enumerate((angle(a, b, c), angle(b, c, a), angle(c, a, b))):
+        for t in range(len(tris)):
+            v = int(tris[t, k])
+            vn[v] = vn.get(v, np.zeros(3)) + fn[t] * ang[t]
+    edges = {}
+    for t in range(len(tris)):
+        for k in range(3):
+            e = tuple(sorted((int(tris[t, k]), int(tris[t, (k + 1) % 3]))))
+            edges.setdefault(e, []).append(t)
+    en = np.zeros((len(tris), 3, 3))
+    for t in range(len(tris)):
+        for k in range(3):
+            e = tuple(sorted((int(tris[t, k]), int(tris[t, (k + 1) % 3]))))
+            others = [o for o in edges[e] if o != t]
+            en[t, k] = fn[t] + (fn[others[0]] if others else 0.0)
+    return fn, vn, en
+
+
+def surface_contact_forces(q, v, radius, flags, bodies, x_surface, x_registration, ke, kd):
+    """Soft-body surface contact force (soft_surface_contacts.py:62-135), by brute force over triangles.
+
+    ``bodies`` lists (start, count, local triangles).  Surfaces sit at x_surface (the last
+    refit); the search radius of a body is its bounding-box diagonal at x_registration.
+    """
+    q = np.asarray(q, np.float64)
+    v = np.asarray(v, np.float64)
+    f = np.zeros_like(q)
+    geo = []
+    for start, count, tris in bodies:
+        tris = np.asarray(tris, np.int64).reshape(-1, 3)
+        if len(tris) == 0:
+            geo.append(None)
+            continue
+        g = tris + start
+        pts = np.asarray(x_registration, np.float64)[start:start + count]
+        md = float(np.linalg.norm(pts.max(0) - pts.min(0)))
+        geo.append((g, md, surface_pseudonormals(x_surface, g)))
+    xs = np.asarray(x_surface, np.float64)
+    for b, (start, count, tris) in enumerate(bodies):
+        if geo[b] is None:
+            continue
+        for p in np.unique(geo[b][0]):
+            if (flags[p] & PARTICLE_FLAG_ACTIVE) == 0:
+                continue
+            for o, go in enumerate(geo):
+                if o == b or go is None:
+                    continue
+                g, md, (fn, vn, en) = go
+                pts, feat = closest_on_triangles(q[p], xs[g[:, 0]], xs[g[:, 1]], xs[g[:, 2]])
+                d2 = np.sum((q[p] - pts) ** 2, 1)
+                t = int(np.argmin(d2))
+                if not d2[t] < md * md:
+                    continue
+                diff = q[p] - pts[t]
+                raw = float(np.linalg.norm(diff))
+                if raw < 1.0e-8:
+                    continue
+                ft = int(feat[t])
+                pn = fn[t] if ft == 0 else (en[t, ft - 1] if ft <= 3 else vn[int(g[t, ft - 4])])
+                sign = 1.0 if np.dot(diff, pn) >= 0.0 else -1.0
+                n = diff / raw * sign
+                pen = radius[p] - raw * sign
+                if not pen > 0.0:
+                    continue
+                f[p] += n * (ke * pen - kd * min(float(np.dot(v[p], n)), 0.0))
+    return f
+
+
 def ground_forces(x, v, radius, inv_mass, flags, ke, kd, kf, mu, plane, gravity):
     """Analytic ground penalty + weight-capped Coulomb friction (kernels.py:1132-1195)."""
     x = x.astype(np.float64)
@@ -725,8 +843,10 @@ class OracleFEM:
         torque_damping=0.0,
         particle_contact=None,
         soft_contact=(1.0e3, 10.0, 1.0e3, 0.5),
+        surface=None,
     ):
-        """``particle_contact`` = (ke, kd, kf, mu, cohesion) enables the particle-particle term."""
+        """``particle_contact`` = (ke, kd, kf, mu, cohesion) enables the particle-particle term;
+        ``surface`` = (bodies, ke, kd) registers surface contacts at the construction positions."""
         self.rest = np.asarray(x, np.float64).copy()
         self.n = len(self.rest)
         self.mass = np.asarray(mass, np.float64)
@@ -769,6 +889,8 @@ class OracleFEM:
         self.torque = (float(torque_stiffness), float(torque_damping))
         self.particle_contact = particle_contact
         self.soft_contact = soft_contact
+        self.surface = surface
+        self.surface_x = self.rest.copy()  # surfaces refit at registration
         self.dv = np.zeros((self.n, 3))
         self.last_iterations = []
         self.last_rr_bb = []
@@ -801,11 +923,19 @@ class OracleFEM:
             self.minv = point_jacobi(self.offsets, self.columns, self.values, self.n)
         self._A = bsr_to_scipy(self.offsets, self.columns, self.values, self.n).tocsr()
 
+    def refit_surfaces(self, q):
+        """Surfaces take positions q (SoftBodySurfaceContacts.update, soft_surface_contacts.py:226-237)."""
+        self.surface_x = np.asarray(q, np.float64).copy()
+
     def refresh_tangent(self, q, dt=None):
-        """Refresh the tangent at q; a dt change clears the warm start (solver.py:769-857)."""
+        """Refresh the tangent at q; a dt change clears the warm start (solver.py:769-857).  The first
+        refresh also refits the surfaces (solver.py:824-827 through _rebuild_element_blocks 669-670)."""
         dt = self.dt if dt is None else float(dt)
         q = np.asarray(q, np.float64).copy()
         q[self.fixed] = self.rest[self.fixed]
+        if not getattr(self, "_refreshed", False):
+            self._refreshed = True
+            self.refit_surfaces(q)
         if dt != self.dt:
             self.dv[:] = 0.0
         self._assemble(q, dt)
@@ -816,7 +946,7 @@ class OracleFEM:
         return dense(self.offsets, self.columns, self.values, self.n)
 
     # -- forces --------------------------------------------------------------
-    TERMS = ("spring", "tet", "hex", "tri", "particle", "ground", "soft_contact", "gravity", "damping")
+    TERMS = ("spring", "tet", "hex", "tri", "particle", "ground", "soft_contact", "gravity", "damping", "surface")
 
     def forces(self, q, v, *, activation=None, terms=TERMS, contacts=None):
         """Per-term forces in the reference's accumulation order (solver.py:571-582).
@@ -853,6 +983,9 @@ class OracleFEM:
         if "damping" in terms:
             out["damping"] = damping_forces(v, self.mass, self.flags, self.linear_damping) if self.linear_damping > 0 \
                 else np.zeros((self.n, 3))
+        if "surface" in terms:
+            out["surface"] = np.zeros((self.n, 3)) if self.surface is None else surface_contact_forces(
+                q, v, self.radius, self.flags, self.surface[0], self.surface_x, self.rest, *self.surface[1:])
         return out
 
     # -- step ----------------------------------------------------------------

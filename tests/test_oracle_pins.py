@@ -332,3 +332,63 @@ def test_soft_contact_known_answer():
     none = O.soft_contact_forces(x + (0, 0, 0.01), v, np.array([0.01]), 1, np.array([0]), np.zeros((1, 3)),
                                  np.zeros((1, 3)), np.array([[0.0, 0.0, 1.0]]), 1e3, 10.0, 1e3, 0.5)
     assert not none.any()
+
+
+# ---------------------------------------------------------------- surface contacts
+
+
+def _tet_block_surface(x, tets):
+    """Boundary faces of a tet mesh, oriented outward."""
+    faces = {}
+    for t in tets:
+        for k in range(4):
+            f = [int(t[j]) for j in range(4) if j != k]
+            faces.setdefault(tuple(sorted(f)), []).append((f, int(t[k])))
+    out = []
+    for lst in faces.values():
+        if len(lst) != 1:
+            continue
+        (i, j, k), opp = lst[0]
+        if np.dot(np.cross(x[j] - x[i], x[k] - x[i]), x[opp] - x[i]) > 0:
+            j, k = k, j
+        out.append((i, j, k))
+    return np.asarray(out, np.int64)
+
+
+def test_closest_point_on_triangle_regions():
+    a, b, c = np.array([[0.0, 0, 0]]), np.array([[1.0, 0, 0]]), np.array([[0.0, 1, 0]])
+    for p, want, feat in (((0.2, 0.2, 0.5), (0.2, 0.2, 0.0), 0), ((-1.0, -1.0, 0.3), (0, 0, 0), 4),
+                          ((2.0, -0.5, 0.0), (1, 0, 0), 5), ((0.5, -1.0, 0.0), (0.5, 0, 0), 1),
+                          ((1.0, 1.0, 0.0), (0.5, 0.5, 0), 2), ((-1.0, 0.5, 0.0), (0, 0.5, 0), 3)):
+        pts, f = O.closest_on_triangles(np.asarray(p, float), a, b, c)
+        np.testing.assert_allclose(pts[0], want, atol=1e-12)
+        assert f[0] == feat
+
+
+def test_pseudonormal_sign_separates_inside_from_outside_a_closed_surface():
+    """Angle-weighted pseudonormals give the exact inside/outside sign of a closed mesh (Baerentzen-Aanaes)."""
+    x, tets, _, _ = scenes.tet_block(2, 2, 2, 0.5, (0.0, 0.0, 0.0), 1e5, 0.4, 1000.0)
+    tris = _tet_block_surface(x, tets)
+    fn, vn, en = O.surface_pseudonormals(x, tris)
+    rng = np.random.default_rng(0)
+    for p in rng.uniform(-0.5, 1.5, (200, 3)):
+        pts, feat = O.closest_on_triangles(p, x[tris[:, 0]], x[tris[:, 1]], x[tris[:, 2]])
+        t = int(np.argmin(np.sum((p - pts) ** 2, 1)))
+        ft = int(feat[t])
+        pn = fn[t] if ft == 0 else (en[t, ft - 1] if ft <= 3 else vn[int(tris[t, ft - 4])])
+        inside = bool(np.all((p > 0) & (p < 1)))
+        assert (np.dot(p - pts[t], pn) < 0) == inside
+
+
+def test_surface_force_pushes_a_penetrating_vertex_out_of_the_other_body():
+    xa, ta, _, _ = scenes.tet_block(1, 1, 1, 0.1, (0.0, 0.0, 0.0), 1e5, 0.4, 1000.0)
+    xb, tb, _, _ = scenes.tet_block(1, 1, 1, 0.1, (0.09, 0.02, 0.03), 1e5, 0.4, 1000.0)
+    x = np.concatenate([xa, xb])
+    bodies = [(0, len(xa), _tet_block_surface(xa, ta)), (len(xa), len(xb), _tet_block_surface(xb, tb))]
+    radius = np.full(len(x), 0.004)
+    f = O.surface_contact_forces(x, np.zeros_like(x), radius, np.ones(len(x), np.int32), bodies, x, x, 1e3, 1e2)
+    # corner (0.1, 0.1, 0.1) of A lies 1 cm inside B along x: pushed toward -x with ke (0.01 + r)
+    k = int(np.argmin(np.linalg.norm(xa - (0.1, 0.1, 0.1), axis=1)))
+    np.testing.assert_allclose(f[k], (-1e3 * (0.01 + 0.004), 0.0, 0.0), atol=1e-9)
+    far = int(np.argmin(np.linalg.norm(xa - (0.0, 0.0, 0.0), axis=1)))
+    assert not f[far].any()
