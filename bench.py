@@ -148,13 +148,14 @@ def build_workload(cells: int, device: str):
     return sc, model, solver, np
 
 
-def spmv_bytes(nnzb: int, n: int, col_bytes: int = 4) -> int:
-    """Algorithmic bytes of one 3x3-BSR SpMV: 36 B values + the column index (4 B, or 2 B as a 16-bit
-    offset from the row) per block, offsets, x read, y write."""
+def spmv_bytes(nnzb: int, n: int, col_bytes: float = 4) -> float:
+    """Algorithmic bytes of one 3x3-BSR SpMV: 36 B values + the column index per block (4 B, 2 B as a
+    16-bit offset from the row, or on average less where a slice's rows share one offset), offsets,
+    x read, y write."""
     return (36 + col_bytes) * nnzb + 4 * (n + 1) + 24 * n
 
 
-def pcg_launch_bytes(nnzb: int, n: int, iterations: float, col_bytes: int = 4) -> float:
+def pcg_launch_bytes(nnzb: int, n: int, iterations: float, col_bytes: float = 4) -> float:
     """Algorithmic bytes of one persistent PCG launch.
 
     Per CG iteration: one SpMV plus 120 B/node (Minv 36, read x r p Ap 48, write x r p 36).
@@ -617,7 +618,11 @@ def run_gb300(args) -> None:
     launch_ms = t_ms.value / max(1, launches)
     cc = ctypes.c_int64()
     _lib.check(lib.fem_get_tuning(solver._handle, _lib.FEM_TUNE_COMPACT_COLUMNS, ctypes.byref(cc)))
-    col_bytes = 2 if cc.value else 4
+    ub = ctypes.c_int64()
+    _lib.check(lib.fem_get_tuning(solver._handle, _lib.FEM_TUNE_UNIFORM_COLUMN_BLOCKS, ctypes.byref(ub)))
+    # column bytes read per stored block: 32-bit columns, 16-bit offsets, or 16-bit offsets only outside
+    # the slots whose offset is shared by the slice (read once per slice: 8 B mask + 2 B per slot)
+    col_bytes = 4.0 if cc.value == 0 else 2.0 * (info["nnzb"] - ub.value) / info["nnzb"]
     bytes_launch = pcg_launch_bytes(info["nnzb"], P, iters, col_bytes)
     achieved = bytes_launch / (launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
@@ -665,7 +670,7 @@ def run_gb300(args) -> None:
                        "cg_maxiter": sc.maxiter, "preconditioner": "block_diag", "parallelism": "replicas",
                        "nnzb": info["nnzb"], "mean_cg_iterations": iters,
                        "pcg_split": "rows split over CTAs by calibrated SpMV speed (FEM_TUNE_BALANCE=1)",
-                       "column_index_bytes": col_bytes,
+                       "column_mode": int(cc.value), "column_index_bytes": round(col_bytes, 4),
                        "l2": "inputs larger than L2 (A values 259 MB, element blocks 614 MB at 64^3)"},
             "roofline": {"kernel": "pcg_kernel", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,

@@ -191,9 +191,12 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
 #define FEM_TUNE_TAIL_PREFETCH 11    /* when a CTA's second (last) round of slices keeps at most this percent of its
                                         warps busy, an idle warp requests that round's matrix bytes into L2 during the
                                         first round; 0 = off, default 50 */
-#define FEM_TUNE_COMPACT_COLUMNS 12  /* 1 (default): the PCG reads 16-bit column offsets (column - row) instead of 32-bit
-                                        columns when every stored block's offset fits; the getter returns whether they
-                                        are in use */
+#define FEM_TUNE_COMPACT_COLUMNS 12  /* column storage the PCG reads when every stored block's column - row offset fits
+                                        16 bits: 0 32-bit columns; 1 16-bit offsets; 2 (default) 16-bit offsets, except
+                                        at the slots where all 32 rows of a slice have the same offset, which are read
+                                        once per slice from shared memory.  The getter returns the mode in use (0 when
+                                        the offsets do not fit) */
+#define FEM_TUNE_UNIFORM_COLUMN_BLOCKS 13  /* read-only: stored blocks whose column offset mode 2 reads once per slice */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);

@@ -34,6 +34,7 @@ FEM_TUNE_RESIDENT_LAYOUT = 9
 FEM_TUNE_SPLIT_HEADROOM = 10
 FEM_TUNE_TAIL_PREFETCH = 11
 FEM_TUNE_COMPACT_COLUMNS = 12
+FEM_TUNE_UNIFORM_COLUMN_BLOCKS = 13
 
 FEM_TERM_SPRING = 1
 FEM_TERM_TET = 2

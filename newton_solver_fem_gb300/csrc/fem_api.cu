@@ -764,7 +764,35 @@ int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* ca
             if (d < -32768 || d > 32767) fits = false;
             else dcol[e] = (short)d;
         }
-        if (fits && nsell > 0) h.dcol = b.upload(dcol);
+        if (fits && nsell > 0) {
+            h.dcol = b.upload(dcol);
+            // slots k < 64 at which every live row of a slice has the same offset
+            std::vector<unsigned long long> kmask(h.nslices, 0ull);
+            std::vector<short> kval((size_t)h.nslices * 64, 0);
+            for (int sl = 0; sl < h.nslices; ++sl) {
+                const int w = std::min(64, slice_ptr[sl + 1] - slice_ptr[sl]);
+                for (int k = 0; k < w; ++k) {
+                    bool any = false, same = true;
+                    short v = 0;
+                    int rows = 0;
+                    for (int l = 0; l < slice_meta[sl].y && same; ++l) {
+                        if (k >= row_nnz[slice_meta[sl].x + l]) continue;
+                        const short d = dcol[((int64_t)slice_ptr[sl] + k) * fem::kSlice + l];
+                        if (!any) v = d;
+                        same = !any || d == v;
+                        any = true;
+                        ++rows;
+                    }
+                    if (any && same) {
+                        kmask[sl] |= 1ull << k;
+                        kval[(size_t)sl * 64 + k] = v;
+                        h.uniform_blocks += rows;
+                    }
+                }
+            }
+            h.slice_kmask = b.upload(kmask);
+            h.slice_kval = b.upload(kval);
+        }
     }
     h.slice_ptr = b.upload(slice_ptr);
     h.slice_meta = b.upload(slice_meta);
@@ -1185,7 +1213,7 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
         if (value < -1 || value > 2) return set_error(FEM_ERR_BAD_ARG, "resident layout must be -1, 0, 1 or 2");
         h.resident_pref = (int)value;
     } else if (key == FEM_TUNE_COMPACT_COLUMNS) {
-        if (value != 0 && value != 1) return set_error(FEM_ERR_BAD_ARG, "compact columns must be 0 or 1");
+        if (value < 0 || value > 2) return set_error(FEM_ERR_BAD_ARG, "compact columns must be 0, 1 or 2");
         h.compact_cols = (int)value;
     } else if (key == FEM_TUNE_TAIL_PREFETCH) {
         if (value < 0 || value > 100) return set_error(FEM_ERR_BAD_ARG, "tail prefetch must be 0..100 percent");
@@ -1226,7 +1254,10 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_RESIDENT_LAYOUT: *value = h.resident_pref; return FEM_OK;
         case FEM_TUNE_SPLIT_HEADROOM: *value = h.split_headroom; return FEM_OK;
         case FEM_TUNE_TAIL_PREFETCH: *value = h.tail_prefetch; return FEM_OK;
-        case FEM_TUNE_COMPACT_COLUMNS: *value = h.compact_cols && h.dcol != nullptr; return FEM_OK;
+        case FEM_TUNE_COMPACT_COLUMNS: *value = h.dcol != nullptr ? h.compact_cols : 0; return FEM_OK;
+        case FEM_TUNE_UNIFORM_COLUMN_BLOCKS:
+            *value = (h.dcol != nullptr && h.compact_cols == 2) ? h.uniform_blocks : 0;
+            return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
 }

@@ -52,6 +52,8 @@ struct PcgArgs {
     const float* __restrict__ valC;   // a22
     const int* __restrict__ scol;     // block column
     const short* __restrict__ dcol;   // block column - row (when every offset fits 16 bits), or null
+    const unsigned long long* __restrict__ slice_kmask;  // [nslices] slots k < 64 with one offset for the slice
+    const short* __restrict__ slice_kval;                // [nslices * 64] that offset
     const int* __restrict__ slice_ptr;   // [nslices+1]
     const int2* __restrict__ slice_meta; // [nslices] (first row, row count)
     const int* __restrict__ slice_scene; // [nslices]
@@ -255,7 +257,10 @@ struct Handle {
     float* valC = nullptr;
     int* scol = nullptr;
     short* dcol = nullptr;  // [nsell] column - row when every offset fits 16 bits (the PCG reads these), else null
-    int compact_cols = 1;   // FEM_TUNE_COMPACT_COLUMNS: the PCG reads dcol when it exists
+    int compact_cols = 2;   // FEM_TUNE_COMPACT_COLUMNS: 0 scol, 1 dcol, 2 dcol + uniform slots (when dcol exists)
+    int64_t uniform_blocks = 0;  // stored blocks in uniform slots (FEM_TUNE_UNIFORM_COLUMN_BLOCKS)
+    unsigned long long* slice_kmask = nullptr;  // [nslices] bit k: every row of the slice has the same dcol at k
+    short* slice_kval = nullptr;                // [nslices * 64] that dcol
     int* slice_ptr = nullptr;
     int2* slice_meta = nullptr;
     int* slice_scene = nullptr;

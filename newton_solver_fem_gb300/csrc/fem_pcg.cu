@@ -176,15 +176,42 @@ struct Entry {
     int j;
 };
 
-// One stored block and its column: the 32-bit column, or (C16) the row plus a
-// 16-bit offset, which saves 2 of the 40 bytes a block costs the SpMV.
-template <bool C16>
-__device__ __forceinline__ Entry load_entry(const PcgArgs& a, size_t e, int row, unsigned long long pol) {
+// The 16-bit column offset of entry e, loaded only when `load` (warp-uniform);
+// otherwise `shared`, the offset every row of the slice has at this k.
+__device__ __forceinline__ int ld_dcol_unless(const short* p, unsigned long long pol, bool load, short shared) {
+    unsigned short v = (unsigned short)shared;
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t"
+        "@q ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %3;\n\t}"
+        : "+h"(v)
+        : "l"(p), "r"((unsigned)load), "l"(pol));
+    return (int)(short)v;
+}
+
+// Column storage of the SpMV (the kernel's CM template parameter): 0 the 32-bit
+// column; 1 the row plus a 16-bit offset, which saves 2 of the 40 bytes a block
+// costs; 2 the same, except that at the slots k < 64 where every row of the
+// slice has the same offset (bit k of the slice's mask) it is read once from
+// shared memory instead of per row.
+struct SliceCols {
+    unsigned long long mask;  // CM 2: uniform slots
+    const short* val;         // CM 2: [64] their offsets (shared memory)
+};
+
+// One stored block and its column.
+template <int CM>
+__device__ __forceinline__ Entry load_entry(const PcgArgs& a, size_t e, int k, int row, const SliceCols& sc,
+                                            unsigned long long pol) {
     Entry m;
     m.A = ld_mat4(a.valA + e, pol);
     m.B = ld_mat4(a.valB + e, pol);
     m.C = ld_mat1(a.valC + e, pol);
-    m.j = C16 ? row + ld_dcol(a.dcol + e, pol) : ld_col(a.scol + e, pol);
+    if (CM == 2) {
+        const bool uni = k < 64 && ((sc.mask >> k) & 1ull);
+        m.j = row + ld_dcol_unless(a.dcol + e, pol, !uni, uni ? sc.val[k] : (short)0);
+    } else {
+        m.j = CM == 1 ? row + ld_dcol(a.dcol + e, pol) : ld_col(a.scol + e, pol);
+    }
     return m;
 }
 
@@ -199,16 +226,18 @@ __device__ __forceinline__ float3 gather_p(const float4* rec, int j, float beta)
 // y_row = sum_k A_k p_{j_k}, with p = z (first iteration) or z + beta p_old.
 // U block columns are loaded before any is used, so U entries (and then U
 // gathers) are in flight per thread; the sum keeps the k order of U = 1.
-template <int U, bool C16, bool FIRST>
+template <int U, int CM, bool FIRST>
 __device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int len, int lane, int row,
-                                              const float4* rec, float beta, unsigned long long pol) {
+                                              const SliceCols& sc, const float4* rec, float beta,
+                                              unsigned long long pol) {
     float3 acc = f3(0.f, 0.f, 0.f);
     int k = 0;
     if (U > 1) {
         for (; k + U <= len; k += U) {
             Entry m[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) m[u] = load_entry<C16>(a, (size_t)(base + k + u) * kSlice + lane, row, pol);
+            for (int u = 0; u < U; ++u)
+                m[u] = load_entry<CM>(a, (size_t)(base + k + u) * kSlice + lane, k + u, row, sc, pol);
             float3 p[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) p[u] = gather_p<FIRST>(rec, m[u].j, beta);
@@ -217,7 +246,7 @@ __device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int le
         }
     }
     for (; k < len; ++k) {
-        Entry m = load_entry<C16>(a, (size_t)(base + k) * kSlice + lane, row, pol);
+        Entry m = load_entry<CM>(a, (size_t)(base + k) * kSlice + lane, k, row, sc, pol);
         float3 p = gather_p<FIRST>(rec, m.j, beta);
         acc = acc + bmul(m.A, m.B, m.C, p);
     }
@@ -225,15 +254,17 @@ __device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int le
 }
 
 // Prologue pass: cv = sum_k A_k (v_j - v_i) and ax = sum_k A_k x_j in one read of the row.
-template <int U, bool C16>
-__device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int len, int lane, int row, float3 vi,
-                                              float3& cv, float3& ax, unsigned long long pol) {
+template <int U, int CM>
+__device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int len, int lane, int row,
+                                              const SliceCols& sc, float3 vi, float3& cv, float3& ax,
+                                              unsigned long long pol) {
     int k = 0;
     if (U > 1) {
         for (; k + U <= len; k += U) {
             Entry m[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) m[u] = load_entry<C16>(a, (size_t)(base + k + u) * kSlice + lane, row, pol);
+            for (int u = 0; u < U; ++u)
+                m[u] = load_entry<CM>(a, (size_t)(base + k + u) * kSlice + lane, k + u, row, sc, pol);
             float3 vj[U], xj[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -248,7 +279,7 @@ __device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int le
         }
     }
     for (; k < len; ++k) {
-        Entry m = load_entry<C16>(a, (size_t)(base + k) * kSlice + lane, row, pol);
+        Entry m = load_entry<CM>(a, (size_t)(base + k) * kSlice + lane, k, row, sc, pol);
         float3 vj = xyz(a.v4[m.j]), xj = xyz(a.x[m.j]);
         cv = cv + bmul(m.A, m.B, m.C, vj - vi);
         ax = ax + bmul(m.A, m.B, m.C, xj);
@@ -264,6 +295,8 @@ struct Smem {
     int* sseg;        // [S + 1] first segment of every scene (copy of scene_seg0)
     float* res;       // [L * 32 * res_floats] resident row state (x, r, z[, inverse diagonal block])
     int4* slc;        // [L] this CTA's slices: (first row, row count, scene, SELL base)
+    unsigned long long* kmask;  // [L] column mode 2: uniform-offset slots of each slice
+    short* kval;                // [L * 64] column mode 2: their offsets
     unsigned* rinfo;  // [L * 32] row length | fixed bit of this CTA's rows
     int nsc;          // scenes (segments) this CTA covers
     int segbase;      // this CTA's first segment
@@ -306,10 +339,10 @@ __host__ __device__ __forceinline__ bool stage_in_smem(int L, int threads) {
 // a 16-byte boundary (the staging area holds float4).  One definition serves
 // the kernel and the host-side size.
 struct SmemLayout {
-    size_t part, st, tot, segb, sseg, slc, rinfo, stage, res, total;
+    size_t part, st, tot, segb, sseg, slc, kmask, kval, rinfo, stage, res, total;
 };
 __host__ __device__ __forceinline__ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
-__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage, int resident) {
+__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage, int resident, bool uni) {
     SmemLayout m;
     m.part = 0;
     m.st = m.part + align16((size_t)L * 3 * sizeof(float));
@@ -317,7 +350,9 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool st
     m.segb = m.tot + align16((size_t)S * 3 * sizeof(float));
     m.sseg = m.segb + align16((size_t)(L + 1) * sizeof(int));
     m.slc = m.sseg + align16((size_t)(S + 1) * sizeof(int));
-    m.rinfo = m.slc + align16((size_t)L * sizeof(int4));
+    m.kmask = m.slc + align16((size_t)L * sizeof(int4));
+    m.kval = m.kmask + (uni ? align16((size_t)L * sizeof(unsigned long long)) : 0);
+    m.rinfo = m.kval + (uni ? align16((size_t)L * 64 * sizeof(short)) : 0);
     m.stage = m.rinfo + align16((size_t)L * kSlice * sizeof(unsigned));
     m.res = m.stage + (stage ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
     m.total = m.res + (resident ? (size_t)L * kSlice * res_floats(resident) * sizeof(float) : 0);
@@ -451,7 +486,7 @@ __device__ __forceinline__ float rhs_scale(float maximum) {
     return scale;
 }
 
-template <int U, bool C16>
+template <int U, int CM>
 __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const unsigned long long pol_last = policy_evict_last();
     const unsigned long long pol_first = policy_evict_first();
@@ -461,7 +496,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const int S = a.nscenes;
     const int L = a.slices_per_cta;
     Smem sm;
-    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0, a.resident);
+    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0, a.resident, CM == 2);
     sm.part = reinterpret_cast<float*>(smem_raw + lay.part);
     sm.st = reinterpret_cast<SceneState*>(smem_raw + lay.st);
     sm.tot = reinterpret_cast<float*>(smem_raw + lay.tot);
@@ -471,6 +506,8 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     sm.res = reinterpret_cast<float*>(smem_raw + lay.res);
     sm.slc = reinterpret_cast<int4*>(smem_raw + lay.slc);
     sm.rinfo = reinterpret_cast<unsigned*>(smem_raw + lay.rinfo);
+    sm.kmask = reinterpret_cast<unsigned long long*>(smem_raw + lay.kmask);
+    sm.kval = reinterpret_cast<short*>(smem_raw + lay.kval);
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int first = a.cta_slice0[blockIdx.x];
@@ -488,7 +525,10 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         for (int t = threadIdx.x; t < last - first; t += blockDim.x) {
             const int2 m = a.slice_meta[first + t];
             sm.slc[t] = make_int4(m.x, m.y, a.slice_scene[first + t], a.slice_ptr[first + t]);
+            if (CM == 2) sm.kmask[t] = a.slice_kmask[first + t];
         }
+        if (CM == 2)
+            for (int t = threadIdx.x; t < (last - first) * 64; t += blockDim.x) sm.kval[t] = a.slice_kval[(size_t)first * 64 + t];
     }
     __syncthreads();  // the slice table is complete before the row table reads it
     for (int t = threadIdx.x; t < (last - first) * kSlice; t += blockDim.x) {
@@ -499,6 +539,9 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     __syncthreads();
     unsigned epoch = 0;
     const float h = a.dt;
+    auto slice_cols = [&](int sl) {
+        return CM == 2 ? SliceCols{sm.kmask[sl - first], sm.kval + 64 * (sl - first)} : SliceCols{0ull, nullptr};
+    };
 
     // ---------------- phase 0: RHS (predictor, springs, projection) and u = rhs - A x0
     if (a.tail_prefetch && warp == W - 1) prefetch_last_round(a, sm, first, last, W, lane);
@@ -516,8 +559,8 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 u = rhs;
                 if (a.solve_warm && !(info & kFixedBit)) {
                     float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
-                    row_predictor<U, C16>(a, sl4.w, (int)(info & ~kFixedBit), lane, row, xyz(a.v4[row]), cv, ax,
-                                     sl < a.resident_slices ? pol_last : pol_first);
+                    row_predictor<U, CM>(a, sl4.w, (int)(info & ~kFixedBit), lane, row, slice_cols(sl), xyz(a.v4[row]),
+                                         cv, ax, sl < a.resident_slices ? pol_last : pol_first);
                     u = rhs - ax;
                 }
             } else {
@@ -525,8 +568,8 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                     int len = (int)(info & ~kFixedBit);
                     float3 vi = xyz(a.v4[row]);
                     float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
-                    row_predictor<U, C16>(a, sl4.w, len, lane, row, vi, cv, ax,
-                                     sl < a.resident_slices ? pol_last : pol_first);
+                    row_predictor<U, CM>(a, sl4.w, len, lane, row, slice_cols(sl), vi, cv, ax,
+                                         sl < a.resident_slices ? pol_last : pol_first);
                     rhs = load3(a.f_ws, row) - cv;
                     for (int e = a.spring_ptr[row]; e < a.spring_ptr[row + 1]; ++e) {
                         int ent = a.spring_ent[e];
@@ -655,8 +698,9 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                     int len = (int)(info & ~kFixedBit);
                     int base = sl4.w;
                     unsigned long long pol = sl < a.resident_slices ? pol_last : pol_first;
-                    acc = firstit ? row_times_p<U, C16, true>(a, base, len, lane, row, rec, beta, pol)
-                                  : row_times_p<U, C16, false>(a, base, len, lane, row, rec, beta, pol);
+                    const SliceCols sc = slice_cols(sl);
+                    acc = firstit ? row_times_p<U, CM, true>(a, base, len, lane, row, sc, rec, beta, pol)
+                                  : row_times_p<U, CM, false>(a, base, len, lane, row, sc, rec, beta, pol);
                 }
                 float4* stg = stage_slot(a, sm, sl, first, lane, row);
                 stg[0] = f4(pc);
@@ -776,12 +820,22 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
 
 using PcgKernel = void (*)(PcgArgs);
 
-PcgKernel pcg_kernel_for(int unroll, bool c16) {
+template <int CM>
+PcgKernel pcg_kernel_cm(int unroll) {
     switch (unroll) {
-        case 2: return c16 ? pcg_kernel<2, true> : pcg_kernel<2, false>;
-        case 4: return c16 ? pcg_kernel<4, true> : pcg_kernel<4, false>;
-        default: return c16 ? pcg_kernel<1, true> : pcg_kernel<1, false>;
+        case 2: return pcg_kernel<2, CM>;
+        case 4: return pcg_kernel<4, CM>;
+        default: return pcg_kernel<1, CM>;
     }
+}
+PcgKernel pcg_kernel_for(int unroll, int cm) {
+    return cm == 2 ? pcg_kernel_cm<2>(unroll) : (cm == 1 ? pcg_kernel_cm<1>(unroll) : pcg_kernel_cm<0>(unroll));
+}
+
+// The column mode a handle's launches use.
+static int column_mode(const Handle& h) {
+    if (h.dcol == nullptr || h.compact_cols == 0) return 0;
+    return (h.compact_cols == 2 && h.slice_kmask != nullptr) ? 2 : 1;
 }
 
 // Grid size, slices per CTA and staging place for the handle's kernel variant
@@ -798,7 +852,8 @@ cudaError_t pcg_configure(Handle& h) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return cudaErrorNotSupported;
-    PcgKernel kern = pcg_kernel_for(h.spmv_unroll, h.dcol != nullptr && h.compact_cols);
+    const int cm = column_mode(h);
+    PcgKernel kern = pcg_kernel_for(h.spmv_unroll, cm);
     // Automatic CTA size: 1024-thread CTAs once there are 8 slices per SM (fewer
     // CTAs make the grid reductions cheaper: on a 3,677-slice Tet4 system 115
     // such CTAs beat 460 of 256 threads by 8% per CG iteration); small systems
@@ -826,8 +881,9 @@ cudaError_t pcg_configure(Handle& h) {
             int per_sm = 0;
             size_t smem = 0;
             for (int attempt = 0; attempt < 3; ++attempt) {
-                const SmemLayout lay = smem_layout(L, h.nscenes, stage, res);
-                if ((lay.st | lay.tot | lay.segb | lay.sseg | lay.slc | lay.rinfo | lay.stage | lay.res) & 15)
+                const SmemLayout lay = smem_layout(L, h.nscenes, stage, res, cm == 2);
+                if ((lay.st | lay.tot | lay.segb | lay.sseg | lay.slc | lay.kmask | lay.kval | lay.rinfo | lay.stage |
+                     lay.res) & 15)
                     return cudaErrorMisalignedAddress;
                 if (lay.total > 227 * 1024) {
                     per_sm = 0;
@@ -895,7 +951,10 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.valB = h.valB;
     a.valC = h.valC;
     a.scol = h.scol;
-    a.dcol = h.compact_cols ? h.dcol : nullptr;
+    const int cm = column_mode(h);
+    a.dcol = cm > 0 ? h.dcol : nullptr;
+    a.slice_kmask = h.slice_kmask;
+    a.slice_kval = h.slice_kval;
     a.slice_ptr = h.slice_ptr;
     a.slice_meta = h.slice_meta;
     a.slice_scene = h.slice_scene;
@@ -955,7 +1014,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, pcg_kernel_for(h.spmv_unroll, a.dcol != nullptr), a);
+    return cudaLaunchKernelEx(&cfg, pcg_kernel_for(h.spmv_unroll, cm), a);
 }
 
 }  // namespace fem

@@ -52,6 +52,8 @@ VARIANTS = [
     {_lib.FEM_TUNE_TAIL_PREFETCH: 0},
     {_lib.FEM_TUNE_TAIL_PREFETCH: 100},
     {_lib.FEM_TUNE_COMPACT_COLUMNS: 0},
+    {_lib.FEM_TUNE_COMPACT_COLUMNS: 1},
+    {_lib.FEM_TUNE_COMPACT_COLUMNS: 1, _lib.FEM_TUNE_SPMV_UNROLL: 1},
 ]
 
 
@@ -87,3 +89,21 @@ def test_calibrated_split_survives_topology_refresh_and_rejects_bad_values():
     s0, s1 = model.state(), model.state()
     solver.step(s0, s1, None, None, sc.dt)
     assert torch.isfinite(s1.particle_q).all()
+
+
+def test_column_modes_are_bit_identical_and_report_shared_slots():
+    """Column modes only change where a block's column comes from, so substeps agree bit for bit."""
+    sc = scenes.hex_block_64(n=12)
+    model, solver, _ = scene_pair(sc, with_oracle=False)
+    lib = _lib.load()
+    assert setting(solver, _lib.FEM_TUNE_COMPACT_COLUMNS) == 2
+    shared = setting(solver, _lib.FEM_TUNE_UNIFORM_COLUMN_BLOCKS)
+    assert 0 < shared < solver.matrix_info()["nnzb"]
+    ref = substep(model, solver, sc)
+    for mode in (1, 0):
+        _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_COMPACT_COLUMNS, mode))
+        assert setting(solver, _lib.FEM_TUNE_UNIFORM_COLUMN_BLOCKS) == 0
+        got = substep(model, solver, sc)
+        np.testing.assert_array_equal(got[0], ref[0])
+        np.testing.assert_array_equal(got[1], ref[1])
+    assert lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_COMPACT_COLUMNS, 3) == _lib.FEM_ERR_BAD_ARG
