@@ -173,7 +173,8 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
 /* Launch tuning of the persistent PCG kernel (chosen by an autotuner).  Not
  * capturable: a change rebuilds the launch tables. */
 #define FEM_TUNE_SPMV_UNROLL 1       /* block columns in flight per thread: 1, 2 or 4 (default 4) */
-#define FEM_TUNE_L2_RESIDENT_BYTES 2 /* matrix bytes loaded evict_last (kept in L2 across iterations); -1 = 60% of L2; default 0 */
+#define FEM_TUNE_L2_RESIDENT_BYTES 2 /* matrix bytes loaded evict_last (kept in L2 across iterations); -1 = 60% of L2;
+                                        -2 (default) = the whole matrix when it fits in 60% of L2, else none */
 #define FEM_TUNE_RESIDENT_SLICES 3   /* read-only: resulting number of L2-resident 32-row slices */
 #define FEM_TUNE_GRID 4              /* read-only: cooperative grid size */
 #define FEM_TUNE_CTA_THREADS 5       /* threads per PCG CTA: 256, 512, 1024, or 0 = automatic (default): 1024 when there are
@@ -192,10 +193,11 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
                                         warps busy, an idle warp requests that round's matrix bytes into L2 during the
                                         first round; 0 = off, default 50 */
 #define FEM_TUNE_COMPACT_COLUMNS 12  /* column storage the PCG reads when every stored block's column - row offset fits
-                                        16 bits: 0 32-bit columns; 1 16-bit offsets; 2 (default) 16-bit offsets, except
-                                        at the slots where all 32 rows of a slice have the same offset, which are read
-                                        once per slice from shared memory.  The getter returns the mode in use (0 when
-                                        the offsets do not fit) */
+                                        16 bits: 0 32-bit columns; 1 16-bit offsets; 2 16-bit offsets, except at the
+                                        slots where all 32 rows of a slice have the same offset, which are read once
+                                        per slice from shared memory; -1 (default) automatic: 2 when the matrix
+                                        streams from DRAM, 1 when all of it is kept in L2.  The getter returns the mode
+                                        in use (0 when the offsets do not fit) */
 #define FEM_TUNE_UNIFORM_COLUMN_BLOCKS 13  /* read-only: stored blocks whose column offset mode 2 reads once per slice */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);

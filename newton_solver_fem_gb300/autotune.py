@@ -3,8 +3,9 @@
 Tunables (``fem_set_tuning``): the SpMV unroll (block columns in flight per
 thread: 1, 2, 4), the threads per persistent CTA (256, 512, 1024: the grid is
 as many CTAs as stay co-resident) and the matrix bytes loaded with the L2
-evict_last policy.  L2 residency lost on every matrix larger than L2, so the
-default candidates leave it at 0.
+evict_last policy.  Pinning part of a matrix larger than L2 lost every time,
+and pinning a whole matrix that fits won, so the default candidates use the
+automatic rule (-2: the whole matrix when it fits in 60% of L2, else none).
 For a solver and a frame function the tuner restores the same initial state
 for every candidate, runs one warm-up frame, then times the PCG launches of
 ``frames`` eager frames with per-launch CUDA events.  It scores each candidate
@@ -30,7 +31,7 @@ import torch
 from . import _lib
 
 # (unroll, CTA threads, L2-resident bytes)
-DEFAULT_CANDIDATES = [(u, t, 0) for t in (1024, 512, 256) for u in (4, 2)] + [(1, 1024, 0)]
+DEFAULT_CANDIDATES = [(u, t, -2) for t in (1024, 512, 256) for u in (4, 2)] + [(1, 1024, -2)]
 CACHE = Path(os.environ.get("FEM_GB300_TUNE_CACHE", Path.home() / ".cache" / "fem_gb300_tune.json"))
 
 

@@ -228,6 +228,29 @@ int configure_launch(Handle& h) {
     if (h.P == 0) return FEM_OK;
     for (void* p : h.launch_allocations) cudaFree(p);
     h.launch_allocations.clear();
+    // L2-resident prefix of the matrix stream (40 bytes per stored block):
+    // automatic (-2) keeps the whole matrix when it fits in 60% of L2 and none
+    // otherwise, since pinning part of a larger matrix only evicts the vectors
+    int64_t budget = h.l2_resident_bytes;
+    if (budget < 0) {
+        int dev = 0, l2 = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+        budget = (int64_t)(0.6 * (double)l2);
+        if (h.l2_resident_bytes == -2) {
+            const int64_t total = (int64_t)h.host_slice_ptr[h.nslices] * fem::kSlice * 40;
+            budget = total <= budget ? total : 0;
+        }
+    }
+    int64_t acc = 0;
+    int rs = 0;
+    for (int sl = 0; sl < h.nslices; ++sl) {
+        int64_t bytes = (int64_t)(h.host_slice_ptr[sl + 1] - h.host_slice_ptr[sl]) * fem::kSlice * 40;
+        if (acc + bytes > budget) break;
+        acc += bytes;
+        ++rs;
+    }
+    h.resident_slices = rs;
     cudaError_t err = fem::pcg_configure(h);
     if (err != cudaSuccess) return cuda_status(err, &h);
     const std::vector<int>& slice_scene = h.host_slice_scene;
@@ -266,23 +289,6 @@ int configure_launch(Handle& h) {
     std::vector<float> zeros(2 * 3 * (size_t)std::max(1, nseg), 0.0f);
     h.seg_part = upload_plain(zeros, h.launch_allocations, err);
     if (err != cudaSuccess) return cuda_status(err, &h);
-    // L2-resident prefix of the matrix stream (40 bytes per stored block)
-    int64_t budget = h.l2_resident_bytes;
-    if (budget < 0) {
-        int dev = 0, l2 = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
-        budget = (int64_t)(0.6 * (double)l2);
-    }
-    int64_t acc = 0;
-    int rs = 0;
-    for (int sl = 0; sl < h.nslices; ++sl) {
-        int64_t bytes = (int64_t)(h.host_slice_ptr[sl + 1] - h.host_slice_ptr[sl]) * fem::kSlice * 40;
-        if (acc + bytes > budget) break;
-        acc += bytes;
-        ++rs;
-    }
-    h.resident_slices = rs;
     return FEM_OK;
 }
 
@@ -1200,7 +1206,7 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
         if (value != 1 && value != 2 && value != 4) return set_error(FEM_ERR_BAD_ARG, "unroll must be 1, 2 or 4");
         h.spmv_unroll = (int)value;
     } else if (key == FEM_TUNE_L2_RESIDENT_BYTES) {
-        if (value < -1) return set_error(FEM_ERR_BAD_ARG, "resident bytes must be >= -1");
+        if (value < -2) return set_error(FEM_ERR_BAD_ARG, "resident bytes must be >= -2");
         h.l2_resident_bytes = value;
     } else if (key == FEM_TUNE_CTA_THREADS) {
         if (value != 0 && value != 256 && value != 512 && value != 1024)
@@ -1213,7 +1219,7 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
         if (value < -1 || value > 2) return set_error(FEM_ERR_BAD_ARG, "resident layout must be -1, 0, 1 or 2");
         h.resident_pref = (int)value;
     } else if (key == FEM_TUNE_COMPACT_COLUMNS) {
-        if (value < 0 || value > 2) return set_error(FEM_ERR_BAD_ARG, "compact columns must be 0, 1 or 2");
+        if (value < -1 || value > 2) return set_error(FEM_ERR_BAD_ARG, "compact columns must be -1, 0, 1 or 2");
         h.compact_cols = (int)value;
     } else if (key == FEM_TUNE_TAIL_PREFETCH) {
         if (value < 0 || value > 100) return set_error(FEM_ERR_BAD_ARG, "tail prefetch must be 0..100 percent");
@@ -1254,10 +1260,8 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_RESIDENT_LAYOUT: *value = h.resident_pref; return FEM_OK;
         case FEM_TUNE_SPLIT_HEADROOM: *value = h.split_headroom; return FEM_OK;
         case FEM_TUNE_TAIL_PREFETCH: *value = h.tail_prefetch; return FEM_OK;
-        case FEM_TUNE_COMPACT_COLUMNS: *value = h.dcol != nullptr ? h.compact_cols : 0; return FEM_OK;
-        case FEM_TUNE_UNIFORM_COLUMN_BLOCKS:
-            *value = (h.dcol != nullptr && h.compact_cols == 2) ? h.uniform_blocks : 0;
-            return FEM_OK;
+        case FEM_TUNE_COMPACT_COLUMNS: *value = column_mode(h); return FEM_OK;
+        case FEM_TUNE_UNIFORM_COLUMN_BLOCKS: *value = column_mode(h) == 2 ? h.uniform_blocks : 0; return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
 }

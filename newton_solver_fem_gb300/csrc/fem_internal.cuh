@@ -124,7 +124,7 @@ struct Handle {
     float tol = 1e-2f;
     long long wait_limit_ns = 2000000000LL;
     int spmv_unroll = 4;          // block columns in flight per thread in the PCG SpMV (1, 2 or 4)
-    int64_t l2_resident_bytes = 0;   // matrix bytes loaded evict_last (-1: 60% of L2); measured slower, so off
+    int64_t l2_resident_bytes = -2;  // matrix bytes loaded evict_last (-1: 60% of L2; -2: all if it fits there, else 0)
     int pcg_threads = 0;             // threads per PCG CTA (256, 512, 1024; 0 = chosen from the problem size)
     int balance = 0;                 // 1: slices split by calibrated per-CTA speed (FEM_TUNE_BALANCE)
     int split_headroom = 0;          // % more slices per CTA than the even share a calibrated split may use
@@ -257,7 +257,7 @@ struct Handle {
     float* valC = nullptr;
     int* scol = nullptr;
     short* dcol = nullptr;  // [nsell] column - row when every offset fits 16 bits (the PCG reads these), else null
-    int compact_cols = 2;   // FEM_TUNE_COMPACT_COLUMNS: 0 scol, 1 dcol, 2 dcol + uniform slots (when dcol exists)
+    int compact_cols = -1;  // FEM_TUNE_COMPACT_COLUMNS: 0 scol, 1 dcol, 2 dcol + uniform slots, -1 automatic
     int64_t uniform_blocks = 0;  // stored blocks in uniform slots (FEM_TUNE_UNIFORM_COLUMN_BLOCKS)
     unsigned long long* slice_kmask = nullptr;  // [nslices] bit k: every row of the slice has the same dcol at k
     short* slice_kval = nullptr;                // [nslices * 64] that dcol
@@ -319,6 +319,17 @@ cudaError_t launch_element_forces(Handle& h, const float* activations, cudaStrea
 cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity, float dt, int terms, bool scale_by_dt,
                                float* out, cudaStream_t s);
 cudaError_t launch_constant_blocks(Handle& h, float dt, cudaStream_t s);
+// The column storage a handle's PCG launches read (FEM_TUNE_COMPACT_COLUMNS):
+// 0 without 16-bit offsets; automatic (-1) reads shared slot offsets once per
+// slice (2) when the matrix streams from DRAM, and per row (1) when all of it is
+// kept in L2, where the saved bytes no longer pay for the extra instructions.
+inline int column_mode(const Handle& h) {
+    if (h.dcol == nullptr || h.compact_cols == 0) return 0;
+    if (h.compact_cols == 1 || h.slice_kmask == nullptr) return 1;
+    if (h.compact_cols == 2) return 2;
+    return h.resident_slices < h.nslices ? 2 : 1;
+}
+
 inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
 // first triplet of the Tet4 region: [P | 2S | 3Tri | 16T | 64H]
 inline int64_t tet_triplet_offset(const Handle& h) {

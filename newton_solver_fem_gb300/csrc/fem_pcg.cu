@@ -832,11 +832,6 @@ PcgKernel pcg_kernel_for(int unroll, int cm) {
     return cm == 2 ? pcg_kernel_cm<2>(unroll) : (cm == 1 ? pcg_kernel_cm<1>(unroll) : pcg_kernel_cm<0>(unroll));
 }
 
-// The column mode a handle's launches use.
-static int column_mode(const Handle& h) {
-    if (h.dcol == nullptr || h.compact_cols == 0) return 0;
-    return (h.compact_cols == 2 && h.slice_kmask != nullptr) ? 2 : 1;
-}
 
 // Grid size, slices per CTA and staging place for the handle's kernel variant
 // and CTA size: as many CTAs as stay co-resident (the cooperative limit, and

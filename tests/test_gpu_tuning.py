@@ -53,7 +53,10 @@ VARIANTS = [
     {_lib.FEM_TUNE_TAIL_PREFETCH: 100},
     {_lib.FEM_TUNE_COMPACT_COLUMNS: 0},
     {_lib.FEM_TUNE_COMPACT_COLUMNS: 1},
-    {_lib.FEM_TUNE_COMPACT_COLUMNS: 1, _lib.FEM_TUNE_SPMV_UNROLL: 1},
+    {_lib.FEM_TUNE_COMPACT_COLUMNS: 2},
+    {_lib.FEM_TUNE_COMPACT_COLUMNS: 2, _lib.FEM_TUNE_SPMV_UNROLL: 1},
+    {_lib.FEM_TUNE_L2_RESIDENT_BYTES: 0},
+    {_lib.FEM_TUNE_L2_RESIDENT_BYTES: 1 << 20, _lib.FEM_TUNE_COMPACT_COLUMNS: 2},
 ]
 
 
@@ -91,11 +94,30 @@ def test_calibrated_split_survives_topology_refresh_and_rejects_bad_values():
     assert torch.isfinite(s1.particle_q).all()
 
 
+def test_automatic_residency_and_column_mode():
+    """A matrix that fits in 60% of L2 is kept there whole and read with per-row offsets; one that
+    streams (no resident bytes) reads the offsets its slices share once per slice."""
+    sc = scenes.hex_block_64(n=12)
+    model, solver, _ = scene_pair(sc, with_oracle=False)
+    lib = _lib.load()
+    nslices = -(-model.particle_count // 32)
+    assert setting(solver, _lib.FEM_TUNE_L2_RESIDENT_BYTES) == -2
+    assert setting(solver, _lib.FEM_TUNE_RESIDENT_SLICES) == nslices
+    assert setting(solver, _lib.FEM_TUNE_COMPACT_COLUMNS) == 1
+    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_L2_RESIDENT_BYTES, 0))
+    assert setting(solver, _lib.FEM_TUNE_RESIDENT_SLICES) == 0
+    assert setting(solver, _lib.FEM_TUNE_COMPACT_COLUMNS) == 2
+    assert setting(solver, _lib.FEM_TUNE_UNIFORM_COLUMN_BLOCKS) > 0
+    for key, bad in ((_lib.FEM_TUNE_L2_RESIDENT_BYTES, -3), (_lib.FEM_TUNE_COMPACT_COLUMNS, -2)):
+        assert lib.fem_set_tuning(solver._handle, key, bad) == _lib.FEM_ERR_BAD_ARG
+
+
 def test_column_modes_are_bit_identical_and_report_shared_slots():
     """Column modes only change where a block's column comes from, so substeps agree bit for bit."""
     sc = scenes.hex_block_64(n=12)
     model, solver, _ = scene_pair(sc, with_oracle=False)
     lib = _lib.load()
+    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_COMPACT_COLUMNS, 2))
     assert setting(solver, _lib.FEM_TUNE_COMPACT_COLUMNS) == 2
     shared = setting(solver, _lib.FEM_TUNE_UNIFORM_COLUMN_BLOCKS)
     assert 0 < shared < solver.matrix_info()["nnzb"]
