@@ -182,6 +182,11 @@ int register_soft_contacts(Handle& h, const int32_t* count, const int32_t* parti
     return FEM_OK;
 }
 
+// Up to this many scenes keep each CTA's slices a contiguous run; more scenes
+// (a batch) are dealt to the CTAs in up to kSceneChunks runs per scene.
+constexpr int kContiguousScenes = 4;
+constexpr int kSceneChunks = 16;
+
 // Contiguous split of the slices over the CTAs that minimises the largest
 // cost / speed, with at most Lmax slices per CTA: bisection on the makespan,
 // each CTA taking (in order) every slice that still fits.
@@ -255,36 +260,69 @@ int configure_launch(Handle& h) {
     if (err != cudaSuccess) return cuda_status(err, &h);
     const std::vector<int>& slice_scene = h.host_slice_scene;
     const int nscenes = h.nscenes;
-    // slices per CTA: by calibrated speed (FEM_TUNE_BALANCE), else by slice cost
-    // alone; at most slices_per_cta each
+    // Slices per CTA, at most slices_per_cta each, balanced by slice cost (or by
+    // calibrated speed, FEM_TUNE_BALANCE).  One scene, or a few: contiguous runs.
+    // Many scenes (a batch): each scene is cut into up to kSceneChunks runs, the
+    // runs are interleaved (run 0 of every scene, then run 1, ...) and that
+    // sequence is split into contiguous pieces; so once most scenes have
+    // converged, the rows still iterating are spread over many CTAs instead of
+    // the two or three that would own a scene's contiguous slices.
     {
         std::vector<double> speed(h.grid, 1.0);
         if (h.balance && (int)h.cta_speed.size() == h.grid) speed = h.cta_speed;
-        h.host_cta_slice0 = split_slices(h.host_slice_cost, speed, h.slices_per_cta);
+        std::vector<int> order(h.nslices);
+        for (int sl = 0; sl < h.nslices; ++sl) order[sl] = sl;
+        h.cta_contiguous = nscenes <= kContiguousScenes ? 1 : 0;
+        if (!h.cta_contiguous) {
+            std::vector<int> s0(nscenes + 1, 0);
+            for (int sl = 0; sl < h.nslices; ++sl) s0[slice_scene[sl] + 1]++;
+            for (int sc = 0; sc < nscenes; ++sc) s0[sc + 1] += s0[sc];
+            order.clear();
+            for (int j = 0; j < kSceneChunks; ++j)
+                for (int sc = 0; sc < nscenes; ++sc) {
+                    const int n = s0[sc + 1] - s0[sc], k = std::min(kSceneChunks, n);
+                    if (j >= k) continue;
+                    for (int sl = s0[sc] + (int)((int64_t)n * j / k); sl < s0[sc] + (int)((int64_t)n * (j + 1) / k); ++sl)
+                        order.push_back(sl);
+                }
+        }
+        std::vector<int64_t> cost(h.nslices);
+        for (int i = 0; i < h.nslices; ++i) cost[i] = h.host_slice_cost[order[i]];
+        h.host_cta_slice0 = split_slices(cost, speed, h.slices_per_cta);
         int widest = 0;
-        for (int c = 0; c < h.grid; ++c)
+        for (int c = 0; c < h.grid; ++c) {
             widest = std::max(widest, h.host_cta_slice0[c + 1] - h.host_cta_slice0[c]);
+            std::sort(order.begin() + h.host_cta_slice0[c], order.begin() + h.host_cta_slice0[c + 1]);
+        }
         if (widest > h.slices_per_cta) return set_error(FEM_ERR_CUDA, "slice split exceeds the per-CTA capacity");
+        h.host_cta_list = order;
         h.cta_slice0 = upload_plain(h.host_cta_slice0, h.launch_allocations, err);
+        h.cta_list = upload_plain(h.host_cta_list, h.launch_allocations, err);
     }
-    std::vector<int> cta_seg_base(h.grid, 0), cta_first_scene(h.grid, nscenes), scene_seg0(nscenes + 1, 0);
-    int nseg = 0;
-    std::vector<int> count(nscenes, 0);
+    // Segments: the runs of one scene in a CTA's (ascending) slice list.  Their
+    // partials go to the segment buffer scene-major, ordered by CTA within a
+    // scene, so every per-scene total sums the same values in the same order.
+    std::vector<int> cta_seg_base(h.grid + 1, 0), seg_start, seg_scene, scene_seg0(nscenes + 1, 0);
     for (int c = 0; c < h.grid; ++c) {
-        int first = h.host_cta_slice0[c], last = h.host_cta_slice0[c + 1];
-        cta_seg_base[c] = nseg;
-        if (first >= last) continue;
-        cta_first_scene[c] = slice_scene[first];
-        for (int s = slice_scene[first]; s <= slice_scene[last - 1]; ++s) {
-            count[s]++;
-            ++nseg;
+        cta_seg_base[c] = (int)seg_start.size();
+        for (int i = h.host_cta_slice0[c]; i < h.host_cta_slice0[c + 1]; ++i) {
+            const int sc = slice_scene[h.host_cta_list[i]];
+            if (i == h.host_cta_slice0[c] || sc != seg_scene.back()) {
+                seg_start.push_back(i);
+                seg_scene.push_back(sc);
+                scene_seg0[sc + 1]++;
+            }
         }
     }
-    // segments are ordered by (cta, scene), which is also scene-major
-    for (int s = 0; s < nscenes; ++s) scene_seg0[s + 1] = scene_seg0[s] + count[s];
+    const int nseg = (int)seg_start.size();
+    cta_seg_base[h.grid] = nseg;
+    for (int sc = 0; sc < nscenes; ++sc) scene_seg0[sc + 1] += scene_seg0[sc];
+    std::vector<int> seg_pos(nseg), fill(scene_seg0.begin(), scene_seg0.end() - 1);
+    for (int t = 0; t < nseg; ++t) seg_pos[t] = fill[seg_scene[t]]++;
     h.nseg = nseg;
     h.cta_seg_base = upload_plain(cta_seg_base, h.launch_allocations, err);
-    h.cta_first_scene = upload_plain(cta_first_scene, h.launch_allocations, err);
+    h.seg_start = upload_plain(seg_start, h.launch_allocations, err);
+    h.seg_pos = upload_plain(seg_pos, h.launch_allocations, err);
     h.scene_seg0 = upload_plain(scene_seg0, h.launch_allocations, err);
     std::vector<float> zeros(2 * 3 * (size_t)std::max(1, nseg), 0.0f);
     h.seg_part = upload_plain(zeros, h.launch_allocations, err);
@@ -327,7 +365,8 @@ int calibrate_balance(Handle& h) {
         std::vector<double> next = speed;
         for (int c = 0; c < h.grid; ++c) {
             int64_t cost = 0;
-            for (int sl = h.host_cta_slice0[c]; sl < h.host_cta_slice0[c + 1]; ++sl) cost += h.host_slice_cost[sl];
+            for (int i = h.host_cta_slice0[c]; i < h.host_cta_slice0[c + 1]; ++i)
+                cost += h.host_slice_cost[h.host_cta_list[i]];
             if (cost == 0 || t[2 * c + 1] == 0) continue;
             const double per_iter = (double)t[2 * c] / (double)t[2 * c + 1];
             worst = std::max(worst, per_iter);

@@ -61,13 +61,15 @@ struct PcgArgs {
     const float* __restrict__ minv;  // [P*9]
     int nslices;
     int slices_per_cta;  // L: the most slices any CTA owns (shared-memory sizing)
-    const int* __restrict__ cta_slice0;  // [grid+1] CTA c owns slices [cta_slice0[c], cta_slice0[c+1])
+    const int* __restrict__ cta_slice0;  // [grid+1] CTA c's positions in cta_list: [cta_slice0[c], cta_slice0[c+1])
     unsigned long long* cta_time;        // [2*grid] SpMV-phase ns and iterations per CTA, or null
     int tail_prefetch;                   // prefetch a last round keeping at most this % of the warps busy (0 = off)
     // segment tables for deterministic per-scene reductions
-    const int* __restrict__ cta_seg_base;     // [grid]
-    const int* __restrict__ cta_first_scene;  // [grid]
-    const int* __restrict__ scene_slice0;     // [S+1]
+    const int* __restrict__ cta_seg_base;     // [grid+1] CTA c's segments are [cta_seg_base[c], cta_seg_base[c+1])
+    const int* __restrict__ seg_start;        // [nseg] a segment's first position in its CTA's slice list
+    const int* __restrict__ seg_pos;          // [nseg] its slot in the segment buffer (scene-major)
+    const int* __restrict__ cta_list;         // [nslices] CTA c owns slices cta_list[cta_slice0[c] .. cta_slice0[c+1])
+    int contiguous;                           // every CTA's list is a contiguous run of slices
     const int* __restrict__ scene_seg0;       // [S+1]
     int nscenes;
     float* seg_part;  // [2][nseg * 3], alternating between consecutive reductions
@@ -132,8 +134,11 @@ struct Handle {
     int resident_pref = -1;          // resident row-state layout: -1 automatic, 0 none, 1 x/r/z, 2 x/r/z + inverse
     std::vector<double> cta_speed;   // calibrated SpMV speed per CTA index (cost units per ns)
     std::vector<int64_t> host_slice_cost;  // stored blocks + 4 per live row, per slice
-    std::vector<int> host_cta_slice0;      // the partition in use
+    std::vector<int> host_cta_slice0;      // the partition in use: CTA c owns host_cta_list[cta_slice0[c] ..)
+    std::vector<int> host_cta_list;        // slice indices, ascending within each CTA
     int* cta_slice0 = nullptr;
+    int* cta_list = nullptr;
+    int cta_contiguous = 1;                // every CTA owns a contiguous run of slices
     unsigned long long* cta_time = nullptr;  // set only while calibrating
     int pcg_threads_used = 0;        // the CTA size of the current configuration
     int grid_cap = 0;                // upper bound on the PCG grid (0: co-residency limit only)
@@ -279,8 +284,9 @@ struct Handle {
     int grid = 0;
     size_t pcg_smem = 0;
     int slices_per_cta = 0;
-    int* cta_seg_base = nullptr;
-    int* cta_first_scene = nullptr;
+    int* cta_seg_base = nullptr;  // [grid+1]
+    int* seg_start = nullptr;     // [nseg]
+    int* seg_pos = nullptr;       // [nseg]
     int* scene_slice0 = nullptr;
     int* scene_seg0 = nullptr;
     int nseg = 0;

@@ -291,15 +291,15 @@ struct Smem {
     SceneState* st;   // [S]
     float* tot;       // [S * 3] per-scene totals of the last reduction
     float4* stage;    // [L * 32 * 2] (p, y) per row, when staged in shared memory
-    int* segb;        // [nsc + 1] slice bounds of this CTA's per-scene segments
+    int* segb;        // [L + 1] bounds (positions in the CTA's slice list) of its per-scene segments,
+                      // then [L] where each segment's partials go in the segment buffer
     int* sseg;        // [S + 1] first segment of every scene (copy of scene_seg0)
     float* res;       // [L * 32 * res_floats] resident row state (x, r, z[, inverse diagonal block])
-    int4* slc;        // [L] this CTA's slices: (first row, row count, scene, SELL base)
+    int4* slc;        // [L] this CTA's slices: (first row, row count, scene | kResidentSlice, SELL base)
     unsigned long long* kmask;  // [L] column mode 2: uniform-offset slots of each slice
     short* kval;                // [L * 64] column mode 2: their offsets
     unsigned* rinfo;  // [L * 32] row length | fixed bit of this CTA's rows
     int nsc;          // scenes (segments) this CTA covers
-    int segbase;      // this CTA's first segment
 };
 
 // Resident row state, per row of the CTA: x (0-2), r (3-5), z (6-8) and, in
@@ -348,7 +348,7 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool st
     m.st = m.part + align16((size_t)L * 3 * sizeof(float));
     m.tot = m.st + align16((size_t)S * sizeof(SceneState));
     m.segb = m.tot + align16((size_t)S * 3 * sizeof(float));
-    m.sseg = m.segb + align16((size_t)(L + 1) * sizeof(int));
+    m.sseg = m.segb + align16((size_t)(2 * L + 1) * sizeof(int));
     m.slc = m.sseg + align16((size_t)(S + 1) * sizeof(int));
     m.kmask = m.slc + align16((size_t)L * sizeof(int4));
     m.kval = m.kmask + (uni ? align16((size_t)L * sizeof(unsigned long long)) : 0);
@@ -381,6 +381,24 @@ __device__ __forceinline__ float4* stage_slot(const PcgArgs& a, const Smem& sm, 
 // results are deterministic.  When s_any is given it is cleared on entry (for
 // the updates to set).  Returns false after a timed-out wait.
 constexpr int kSegLoadBatch = 8;  // segment partials a lane loads before adding them
+constexpr int kSegmentsPerWarp0 = 2;  // segments warp 0 writes alone
+constexpr int kResidentSlice = 1 << 30;  // slice table scene field: the slice's blocks are loaded evict_last
+
+// Segment t's partials (sum or max over its slices: lane-strided, then a fixed
+// xor butterfly) to its slot of the segment buffer; entered by a whole warp.
+__device__ __forceinline__ void write_segment(const PcgArgs& a, const Smem& sm, float* buf, int nv, bool is_max,
+                                              int first, int t, int lane) {
+    const int lo = sm.segb[t], hi = sm.segb[t + 1];
+    for (int k = 0; k < nv; ++k) {
+        float acc = 0.f;
+        for (int sl = lo + lane; sl < hi; sl += 32) {
+            const float v = sm.part[(sl - first) * 3 + k];
+            acc = is_max ? fmaxf(acc, v) : acc + v;
+        }
+        acc = is_max ? warp_max(acc) : warp_sum(acc);
+        if (lane == 0) buf[(size_t)sm.segb[a.slices_per_cta + 1 + t] * 3 + k] = acc;
+    }
+}
 
 template <class Update>
 __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf, int nv, bool is_max, int first,
@@ -389,19 +407,16 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
     const int S = a.nscenes;
     if (threadIdx.x == 0 && s_any != nullptr) *s_any = 0;
     __syncthreads();  // slice partials complete, activity flag cleared
+    // many segments: all warps write them, and a CTA barrier orders the writes
+    // before the arrival
+    const bool spread = sm.nsc > kSegmentsPerWarp0;
+    if (spread) {
+        for (int t = warp; t < sm.nsc; t += (int)(blockDim.x >> 5)) write_segment(a, sm, buf, nv, is_max, first, t, lane);
+        __syncthreads();
+    }
     if (warp == 0) {
-        for (int t = 0; t < sm.nsc; ++t) {
-            const int lo = sm.segb[t], hi = sm.segb[t + 1];
-            for (int k = 0; k < nv; ++k) {
-                float acc = 0.f;
-                for (int sl = lo + lane; sl < hi; sl += 32) {
-                    const float v = sm.part[(sl - first) * 3 + k];
-                    acc = is_max ? fmaxf(acc, v) : acc + v;
-                }
-                acc = is_max ? warp_max(acc) : warp_sum(acc);
-                if (lane == 0) buf[(size_t)(sm.segbase + t) * 3 + k] = acc;
-            }
-        }
+        if (!spread)
+            for (int t = 0; t < sm.nsc; ++t) write_segment(a, sm, buf, nv, is_max, first, t, lane);
         __syncwarp();
         int ok = 1;
         if (lane == 0) ok = arrive_and_wait(a.barrier, gridDim.x, epoch, a.status, a.limit_ns);
@@ -516,19 +531,23 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     // Launch-constant reduction tables, staged once (the first grid reduction's
     // CTA barrier orders these writes before their use).
     {
-        const int s0 = a.cta_first_scene[blockIdx.x];
-        sm.nsc = first < last ? a.slice_scene[last - 1] - s0 + 1 : 0;
-        sm.segbase = a.cta_seg_base[blockIdx.x];
-        for (int t = threadIdx.x; t <= sm.nsc; t += blockDim.x)
-            sm.segb[t] = t == 0 ? first : (t == sm.nsc ? last : a.scene_slice0[s0 + t]);
+        const int segbase = a.cta_seg_base[blockIdx.x];
+        sm.nsc = a.cta_seg_base[blockIdx.x + 1] - segbase;
+        for (int t = threadIdx.x; t <= sm.nsc; t += blockDim.x) {
+            sm.segb[t] = t == sm.nsc ? last : a.seg_start[segbase + t];
+            if (t < sm.nsc) sm.segb[L + 1 + t] = a.seg_pos[segbase + t];
+        }
         for (int t = threadIdx.x; t <= S; t += blockDim.x) sm.sseg[t] = a.scene_seg0[t];
         for (int t = threadIdx.x; t < last - first; t += blockDim.x) {
-            const int2 m = a.slice_meta[first + t];
-            sm.slc[t] = make_int4(m.x, m.y, a.slice_scene[first + t], a.slice_ptr[first + t]);
-            if (CM == 2) sm.kmask[t] = a.slice_kmask[first + t];
+            const int g = a.cta_list[first + t];
+            const int2 m = a.slice_meta[g];
+            sm.slc[t] = make_int4(m.x, m.y, a.slice_scene[g] | (g < a.resident_slices ? kResidentSlice : 0),
+                                  a.slice_ptr[g]);
+            if (CM == 2) sm.kmask[t] = a.slice_kmask[g];
         }
         if (CM == 2)
-            for (int t = threadIdx.x; t < (last - first) * 64; t += blockDim.x) sm.kval[t] = a.slice_kval[(size_t)first * 64 + t];
+            for (int t = threadIdx.x; t < (last - first) * 64; t += blockDim.x)
+                sm.kval[t] = a.slice_kval[(size_t)a.cta_list[first + t / 64] * 64 + t % 64];
     }
     __syncthreads();  // the slice table is complete before the row table reads it
     for (int t = threadIdx.x; t < (last - first) * kSlice; t += blockDim.x) {
@@ -544,7 +563,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     };
 
     // ---------------- phase 0: RHS (predictor, springs, projection) and u = rhs - A x0
-    if (a.tail_prefetch && warp == W - 1) prefetch_last_round(a, sm, first, last, W, lane);
+    if (a.tail_prefetch && a.contiguous && warp == W - 1) prefetch_last_round(a, sm, first, last, W, lane);
     for (int sl = first + warp; sl < last; sl += W) {
         const int4 sl4 = sm.slc[sl - first];
         const int2 meta = make_int2(sl4.x, sl4.y);
@@ -560,7 +579,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 if (a.solve_warm && !(info & kFixedBit)) {
                     float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
                     row_predictor<U, CM>(a, sl4.w, (int)(info & ~kFixedBit), lane, row, slice_cols(sl), xyz(a.v4[row]),
-                                         cv, ax, sl < a.resident_slices ? pol_last : pol_first);
+                                         cv, ax, (sl4.z & kResidentSlice) ? pol_last : pol_first);
                     u = rhs - ax;
                 }
             } else {
@@ -569,7 +588,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                     float3 vi = xyz(a.v4[row]);
                     float3 cv = f3(0.f, 0.f, 0.f), ax = f3(0.f, 0.f, 0.f);
                     row_predictor<U, CM>(a, sl4.w, len, lane, row, slice_cols(sl), vi, cv, ax,
-                                         sl < a.resident_slices ? pol_last : pol_first);
+                                         (sl4.z & kResidentSlice) ? pol_last : pol_first);
                     rhs = load3(a.f_ws, row) - cv;
                     for (int e = a.spring_ptr[row]; e < a.spring_ptr[row + 1]; ++e) {
                         int ent = a.spring_ent[e];
@@ -603,7 +622,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     for (int sl = first + warp; sl < last; sl += W) {
         const int4 sl4 = sm.slc[sl - first];
         const int2 meta = make_int2(sl4.x, sl4.y);
-        const SceneState& st = sm.st[sl4.z];
+        const SceneState& st = sm.st[sl4.z & ~kResidentSlice];
         float rr = 0.f, rz = 0.f, bb = 0.f;
         if (lane < meta.y) {
             int row = meta.x + lane;
@@ -674,11 +693,11 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         float4* rec_next = (it & 1) ? a.zp0 : a.zp1;   // (z, p) for the next, written by phase B
         // phase A: p = z + beta p, y = (PAP + I - P) p, partial p.y
         if (a.cta_time != nullptr && threadIdx.x == 0) s_t0 = global_ns();
-        if (a.tail_prefetch && warp == W - 1) prefetch_last_round(a, sm, first, last, W, lane);
+        if (a.tail_prefetch && a.contiguous && warp == W - 1) prefetch_last_round(a, sm, first, last, W, lane);
         for (int sl = first + warp; sl < last; sl += W) {
             const int4 sl4 = sm.slc[sl - first];
             const int2 meta = make_int2(sl4.x, sl4.y);
-            const SceneState& st = sm.st[sl4.z];
+            const SceneState& st = sm.st[sl4.z & ~kResidentSlice];
             float pap = 0.f;
             if (st.active && lane < meta.y) {
                 int row = meta.x + lane;
@@ -697,7 +716,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 if (!(info & kFixedBit)) {
                     int len = (int)(info & ~kFixedBit);
                     int base = sl4.w;
-                    unsigned long long pol = sl < a.resident_slices ? pol_last : pol_first;
+                    unsigned long long pol = (sl4.z & kResidentSlice) ? pol_last : pol_first;
                     const SliceCols sc = slice_cols(sl);
                     acc = firstit ? row_times_p<U, CM, true>(a, base, len, lane, row, sc, rec, beta, pol)
                                   : row_times_p<U, CM, false>(a, base, len, lane, row, sc, rec, beta, pol);
@@ -726,7 +745,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         for (int sl = first + warp; sl < last; sl += W) {
             const int4 sl4 = sm.slc[sl - first];
             const int2 meta = make_int2(sl4.x, sl4.y);
-            const SceneState& st = sm.st[sl4.z];
+            const SceneState& st = sm.st[sl4.z & ~kResidentSlice];
             float rr = 0.f, rz = 0.f;
             if (st.active && lane < meta.y) {
                 int row = meta.x + lane;
@@ -784,7 +803,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         const int4 sl4 = sm.slc[sl - first];
         const int2 meta = make_int2(sl4.x, sl4.y);
         if (lane >= meta.y) continue;
-        const SceneState& st = sm.st[sl4.z];
+        const SceneState& st = sm.st[sl4.z & ~kResidentSlice];
         int row = meta.x + lane;
         float3 dv = a.resident ? res3(res_slot(sm, sl, first, lane, a.resident), 0) : xyz(a.x[row]);
         float sc = st.scale;
@@ -961,8 +980,10 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.cta_time = h.cta_time;
     a.tail_prefetch = h.tail_prefetch;
     a.cta_seg_base = h.cta_seg_base;
-    a.cta_first_scene = h.cta_first_scene;
-    a.scene_slice0 = h.scene_slice0;
+    a.cta_list = h.cta_list;
+    a.contiguous = h.cta_contiguous;
+    a.seg_start = h.seg_start;
+    a.seg_pos = h.seg_pos;
     a.scene_seg0 = h.scene_seg0;
     a.nscenes = h.nscenes;
     a.seg_part = h.seg_part;
