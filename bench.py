@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched vs plain measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-beam gradient measurement")
     p.add_argument("--no-tet", action="store_true", help="skip the jittered Tet4 48^3 measurement")
+    p.add_argument("--profile-workload", choices=("batched", "tet"), default=None,
+                   help="run only --steps eager frames of the 256-scene batch or the jittered Tet4 48^3 block, "
+                        "print their time, and exit (a target for ncu launch lists; no JSON line)")
     p.add_argument("--trace-iterations", action="store_true",
                    help="print the CG iterations of every PCG launch of the eager warm-up frame to stderr "
                         "(maps an ncu launch index to its iteration count)")
@@ -690,8 +693,47 @@ def run_gb300(args) -> None:
         torch.distributed.destroy_process_group()
 
 
+def profile_workload(name: str, steps: int) -> None:
+    """Eager frames (tangent refresh + substeps) of one secondary workload, for profiling."""
+    import torch
+
+    from newton_solver_fem_gb300 import scenes
+
+    if name == "batched":
+        sc = scenes.batched_scenes()
+        model, solver = scene_solver(sc, "cuda:0", sc.scene_offsets)
+    else:
+        from newton_solver_fem_gb300 import SolverFEM, model_from_arrays
+
+        sc = scenes.tet_jittered_48()
+        model = model_from_arrays(sc.x, sc.mass, tets=sc.tets, tet_materials=sc.tet_materials, springs=sc.springs,
+                                  spring_ke=sc.spring_ke, spring_kd=sc.spring_kd, velocity=sc.velocity,
+                                  radius=sc.radius, gravity=sc.gravity, device="cuda:0")
+        ke, kd, kf, mu = sc.ground
+        solver = SolverFEM(model, dt=sc.dt, solver_type="cg", preconditioner_type="block_diag",
+                           linear_solver_maxiter=sc.maxiter, linear_solver_tolerance=sc.tolerance,
+                           self_contact_ke=0.0, ground_plane=sc.ground_plane, ground_ke=ke, ground_kd=kd,
+                           ground_kf=kf, ground_mu=mu)
+    a, b = model.state(), model.state()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        solver.refresh_tangent(a.particle_q)
+        for _ in range(sc.substeps):
+            solver.step(a, b, None, None, sc.dt)
+            a, b = b, a
+    e1.record()
+    torch.cuda.synchronize()
+    print(f"{name}: {steps} eager frames, {e0.elapsed_time(e1) / max(1, steps):.3f} ms per frame, "
+          f"{model.particle_count} nodes, last substep max CG iterations {solver.stats()['max_iterations']}",
+          file=sys.stderr)
+
+
 def main():
     args = parse()
+    if args.profile_workload is not None:
+        profile_workload(args.profile_workload, args.steps)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -389,7 +389,16 @@ def test_captured_graph_matches_eager_with_live_inputs():
 
 def test_batched_scenes_match_individual_solves():
     """Scenes packed in one handle (per-scene CG scalars and convergence) equal each scene solved alone."""
-    sc = small_batch()
+    check_batch_against_solo_solves(small_batch())
+
+
+def test_spread_batch_matches_individual_solves():
+    """24 scenes of up to 10^3 cells: each scene's slices are dealt to several CTAs in interleaved
+    runs, and its reductions sum segments from many CTAs; the result still equals each scene alone."""
+    check_batch_against_solo_solves(scenes.batched_scenes(count=24, seed=5, dims=(3, 10)))
+
+
+def check_batch_against_solo_solves(sc):
     model, solver, _ = scene_pair(sc)
     s0, s1 = model.state(), model.state()
     solver.step(s0, s1, None, None, sc.dt)
