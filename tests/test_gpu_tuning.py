@@ -129,3 +129,17 @@ def test_column_modes_are_bit_identical_and_report_shared_slots():
         np.testing.assert_array_equal(got[0], ref[0])
         np.testing.assert_array_equal(got[1], ref[1])
     assert lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_COMPACT_COLUMNS, 3) == _lib.FEM_ERR_BAD_ARG
+
+
+def test_calibrated_split_of_a_spread_batch():
+    """A 24-scene batch (slices dealt to CTAs in interleaved runs) re-split by calibrated CTA speed
+    solves the same system, deterministically."""
+    sc = scenes.batched_scenes(count=24, seed=5, dims=(3, 10))
+    model, solver, _ = scene_pair(sc, linear_solver_tolerance=1e-6, linear_solver_maxiter=200, with_oracle=False)
+    dv_ref, _ = substep(model, solver, sc)
+    lib = _lib.load()
+    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_BALANCE, 1))
+    dv, _ = substep(model, solver, sc)
+    dv2, _ = substep(model, solver, sc)
+    np.testing.assert_array_equal(dv, dv2)
+    assert rel_l2(dv, dv_ref) < 1e-5
