@@ -647,10 +647,9 @@ int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* ca
     });
 
     // ---- SELL-32 layout, sliced per scene
-    std::vector<int> slice_ptr(1, 0), slice_scene, scene_slice0(nscenes + 1, 0);
+    std::vector<int> slice_ptr(1, 0), slice_scene;
     std::vector<int2> slice_meta;
     for (int s = 0; s < nscenes; ++s) {
-        scene_slice0[s] = (int)slice_meta.size();
         for (int64_t r0 = scenes[s]; r0 < scenes[s + 1]; r0 += fem::kSlice) {
             int n = (int)std::min<int64_t>(fem::kSlice, scenes[s + 1] - r0);
             int w = 0;
@@ -660,7 +659,6 @@ int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* ca
             slice_ptr.push_back(slice_ptr.back() + w);
         }
     }
-    scene_slice0[nscenes] = (int)slice_meta.size();
     h.nslices = (int)slice_meta.size();
     const int64_t nsell = (int64_t)slice_ptr.back() * fem::kSlice;
     h.nsell = nsell;
@@ -842,7 +840,6 @@ int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* ca
     h.slice_ptr = b.upload(slice_ptr);
     h.slice_meta = b.upload(slice_meta);
     h.slice_scene = b.upload(slice_scene);
-    h.scene_slice0 = b.upload(scene_slice0);
     h.row_info = b.upload(row_info);
     h.minv = b.alloc<float>(9 * (size_t)P);
     h.x = b.alloc<float4>(P);

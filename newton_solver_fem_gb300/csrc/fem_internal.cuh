@@ -287,7 +287,6 @@ struct Handle {
     int* cta_seg_base = nullptr;  // [grid+1]
     int* seg_start = nullptr;     // [nseg]
     int* seg_pos = nullptr;       // [nseg]
-    int* scene_slice0 = nullptr;
     int* scene_seg0 = nullptr;
     int nseg = 0;
     float* seg_part = nullptr;
