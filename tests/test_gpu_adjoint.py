@@ -353,3 +353,81 @@ def test_per_segment_refresh_matches_frozen_matrix_segments():
         qb, vb = torch.autograd.grad((q, v), (qs, vs), grad_outputs=(qb, vb))
     np.testing.assert_allclose(to_np(dq_c), to_np(qb), rtol=1e-6, atol=1e-9)
     np.testing.assert_allclose(to_np(dv_c), to_np(vb), rtol=1e-6, atol=1e-9)
+
+
+def test_load_optimization_recovers_the_tip_load():
+    """Fit a tip load from a cantilever's final shape by gradient descent through the
+    differentiable step (tests/test_solver.py:424-429, tests/diffsim_optimize.py): the bundled
+    12-node Tet4 cantilever, x = 0 nodes massless and restored after every substep, 12 substeps
+    of 0.01 s, loss 1e4 * mean |q - target|^2; secant step sizes with a backtracking check."""
+    from fixtures import mesh
+
+    points, tets = mesh("tet_cantilever")
+    b = FEMBuilder(gravity=(0.0, 0.0, 0.0))
+    b.add_soft_mesh(pos=(0.0, 0.0, 0.0), rot=(0.0, 0.0, 0.0, 1.0), scale=1.0, vel=(0.0, 0.0, 0.0),
+                    vertices=points, indices=tets.reshape(-1), density=100.0, k_mu=500.0, k_lambda=1000.0,
+                    k_damp=0.1)
+    for i, p in enumerate(b.particle_q):
+        if abs(p[0]) < 1.0e-8:
+            b.particle_mass[i] = 0.0
+    model = b.finalize(DEVICE)
+    dt = 0.01
+    solver = SolverFEM(model, dt=dt, linear_solver_maxiter=64, solver_type="cg", preconditioner_type="block_diag",
+                       min_stretch=-1.0, self_contact_ke=0.0)
+    diff = DifferentiableSolver(solver)
+    rest = model.particle_q.clone()
+    support = (model.particle_inv_mass == 0.0)[:, None]
+    x0 = rest[:, 0].cpu().numpy()
+    weights = torch.as_tensor((x0 > 0.199) / (x0 > 0.199).sum(), dtype=torch.float32, device=DEVICE)
+
+    def final_q(amplitude):
+        q, v = rest.clone(), torch.zeros_like(rest)
+        for _ in range(12):
+            force = torch.stack([torch.zeros_like(weights), torch.zeros_like(weights), amplitude * weights], 1)
+            raw_q, raw_v = diff.step(q, v, dt, external_forces=force)
+            q = torch.where(support, rest, raw_q)
+            v = torch.where(support, torch.zeros_like(raw_v), raw_v)
+        return q
+
+    def loss_of(q):
+        return 1.0e4 * ((q - target) ** 2).sum() / q.shape[0]
+
+    with torch.no_grad():
+        target = final_q(torch.tensor(-0.2, device=DEVICE))
+    amplitude = torch.tensor(-0.06, device=DEVICE, requires_grad=True)
+    history, previous, accepted_updates = [], None, 0
+    for iteration in range(16):
+        loss = loss_of(final_q(amplitude))
+        value = float(loss.detach())
+        history.append(value)
+        if iteration == 15 or value < 1.0e-11:
+            break
+        (gradient,) = torch.autograd.grad(loss, amplitude)
+        gradient, current = float(gradient), float(amplitude.detach())
+        assert np.isfinite(gradient)
+        rate = 0.08 / max(abs(gradient), 1.0e-12)
+        if previous is not None:
+            change = current - previous[0]
+            curvature = (gradient - previous[1]) / change if abs(change) > 1.0e-10 else 0.0
+            if curvature > 0.0:
+                rate = 1.0 / curvature
+        accepted = False
+        for _ in range(12):
+            candidate = current - rate * gradient
+            with torch.no_grad():
+                trial = float(loss_of(final_q(torch.tensor(candidate, device=DEVICE))))
+            if trial < value:
+                previous = current, gradient
+                with torch.no_grad():
+                    amplitude.fill_(candidate)
+                accepted_updates += 1
+                accepted = True
+                break
+            rate *= 0.5
+        if not accepted:
+            break
+    assert accepted_updates > 0
+    assert history[-1] < 0.01 * history[0]
+    assert abs(float(amplitude.detach()) - (-0.2)) < 0.01
+    tip = torch.as_tensor(x0 > 0.199, device=DEVICE)
+    assert abs(float((target - rest)[tip, 2].mean())) > 1.0e-5
