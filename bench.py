@@ -631,6 +631,8 @@ def run_gb300(args) -> None:
     peak, peak_kind = peaks()
     traffic = dram_traffic_per_launch()
 
+    spmv = standalone_spmv(solver, lib, P, info["nnzb"], peak)
+
     # ---- end to end through the public API with host buffers
     host_q = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
     host_v = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
@@ -678,6 +680,7 @@ def run_gb300(args) -> None:
             "roofline": {"kernel": "pcg_kernel", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "bytes_per_launch": bytes_launch, "launch_ms": launch_ms, "launches": launches},
+            "spmv": spmv,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 12 * P,
                     "d2h_bytes_per_step": 2 * 12 * P},
             "gpu_launches": args.steps * (3 + 4 * substeps),
@@ -691,6 +694,38 @@ def run_gb300(args) -> None:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def standalone_spmv(solver, lib, P: int, nnzb: int, peak: float) -> dict:
+    """One (PAP + I - P) x through the public fem_apply_operator, timed alone (CUDA events on the
+    launching stream, a 512 MB L2 flush before each of 30 launches, median)."""
+    import ctypes
+
+    import torch
+
+    from newton_solver_fem_gb300 import _lib
+
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn((P, 3), device="cuda", generator=g)
+    y = torch.empty_like(x)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    cc = ctypes.c_int64()
+    _lib.check(lib.fem_get_tuning(solver._handle, _lib.FEM_TUNE_COMPACT_COLUMNS, ctypes.byref(cc)))
+    times = []
+    for _ in range(31):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(lib.fem_apply_operator(solver._handle, x.data_ptr(), y.data_ptr(), stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    us = 1e3 * statistics.median(times[1:])
+    col = 4 if cc.value == 0 else 2  # the operator reads 16-bit offsets whenever the handle has them
+    gbs = spmv_bytes(nnzb, P, col) / (us / 1e6) / 1e9
+    return {"kernel": "apply_operator_kernel (fem_apply_operator)", "us": us, "achieved": gbs, "peak": peak,
+            "unit": "GB/s", "frac": gbs / peak, "column_index_bytes": col}
 
 
 def profile_workload(name: str, steps: int) -> None:

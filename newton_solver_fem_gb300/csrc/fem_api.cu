@@ -837,6 +837,21 @@ int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* ca
             h.slice_kval = b.upload(kval);
         }
     }
+    {  // per (slice, k): the lanes whose column at k is a fixed node (fem_apply_operator's mask)
+        std::vector<unsigned> fixcol(nsell / fem::kSlice, 0u);
+        bool any = false;
+        for (int sl = 0; sl < h.nslices; ++sl)
+            for (int k = 0; k < slice_ptr[sl + 1] - slice_ptr[sl]; ++k)
+                for (int l = 0; l < slice_meta[sl].y; ++l) {
+                    const int r = slice_meta[sl].x + l;
+                    if (k >= row_nnz[r]) continue;
+                    if (fixed_mask[scol[((int64_t)slice_ptr[sl] + k) * fem::kSlice + l]]) {
+                        fixcol[(size_t)slice_ptr[sl] + k] |= 1u << l;
+                        any = true;
+                    }
+                }
+        if (any) h.fixcol = b.upload(fixcol);
+    }
     h.slice_ptr = b.upload(slice_ptr);
     h.slice_meta = b.upload(slice_meta);
     h.slice_scene = b.upload(slice_scene);

@@ -265,6 +265,7 @@ struct Handle {
     int compact_cols = -1;  // FEM_TUNE_COMPACT_COLUMNS: 0 scol, 1 dcol, 2 dcol + uniform slots, -1 automatic
     int64_t uniform_blocks = 0;  // stored blocks in uniform slots (FEM_TUNE_UNIFORM_COLUMN_BLOCKS)
     unsigned long long* slice_kmask = nullptr;  // [nslices] bit k: every row of the slice has the same dcol at k
+    unsigned* fixcol = nullptr;  // [nsell / 32] per (slice, k): lanes whose column at k is a fixed node (null: none)
     short* slice_kval = nullptr;                // [nslices * 64] that dcol
     int* slice_ptr = nullptr;
     int2* slice_meta = nullptr;

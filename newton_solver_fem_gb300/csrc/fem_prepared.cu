@@ -109,12 +109,29 @@ __global__ void prepared_rhs_kernel(int P, const float* __restrict__ impulse, co
     st3(out, i, r);
 }
 
-// y = (PAP + I - P) x: fixed rows return x_i; free rows skip fixed columns.
-__global__ void apply_operator_kernel(int nslices, const int* __restrict__ slice_ptr, const int2* __restrict__ meta,
-                                      const unsigned* __restrict__ row_info, const float4* __restrict__ valA,
-                                      const float4* __restrict__ valB, const float* __restrict__ valC,
-                                      const int* __restrict__ scol, const float* __restrict__ x,
-                                      float* __restrict__ y) {
+// y = (PAP + I - P) x (fixed_particles.py:56-73): fixed rows return x_i, free
+// rows skip fixed columns and sum in k order.  One warp per SELL slice and lane
+// per row, streamed like the PCG's SpMV: kOperatorBatch block columns loaded
+// before any is used, the column as a 16-bit offset when the handle has them,
+// the blocks through the non-coherent path without L1 allocation, and the
+// fixed columns read from a per-(slice, k) lane mask rather than from each
+// column's row info.
+constexpr int kOperatorBatch = 4;
+__device__ __forceinline__ float4 ld_stream4(const float4* p) {
+    float4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ float ld_stream1(const float* p) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__global__ void __launch_bounds__(256) apply_operator_kernel(
+    int nslices, const int* __restrict__ slice_ptr, const int2* __restrict__ meta,
+    const unsigned* __restrict__ row_info, const float4* __restrict__ valA, const float4* __restrict__ valB,
+    const float* __restrict__ valC, const int* __restrict__ scol, const short* __restrict__ dcol,
+    const unsigned* __restrict__ fixcol, const float* __restrict__ x, float* __restrict__ y) {
     const int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (sl >= nslices) return;
     const int2 m = meta[sl];
@@ -125,13 +142,29 @@ __global__ void apply_operator_kernel(int nslices, const int* __restrict__ slice
         st3(y, row, ld3(x, row));
         return;
     }
-    const int len = (int)(info & ~kFixedBit);
+    const int len = (int)(info & ~kFixedBit), base = slice_ptr[sl];
     float3 acc = f3(0.f, 0.f, 0.f);
-    for (int k = 0; k < len; ++k) {
-        const size_t e = (size_t)(slice_ptr[sl] + k) * kSlice + lane;
-        const int j = scol[e];
-        if (row_info[j] & kFixedBit) continue;
-        acc = acc + block_mul(valA[e], valB[e], valC[e], ld3(x, j));
+    for (int k0 = 0; k0 < len; k0 += kOperatorBatch) {
+        float4 A[kOperatorBatch], B[kOperatorBatch];
+        float C[kOperatorBatch];
+        int j[kOperatorBatch];
+        bool use[kOperatorBatch];
+#pragma unroll
+        for (int u = 0; u < kOperatorBatch; ++u) {
+            const int k = k0 + u < len ? k0 + u : len - 1;  // a repeated last column is loaded, not added
+            const size_t e = (size_t)(base + k) * kSlice + lane;
+            A[u] = ld_stream4(valA + e);
+            B[u] = ld_stream4(valB + e);
+            C[u] = ld_stream1(valC + e);
+            j[u] = dcol != nullptr ? row + (int)__ldg(dcol + e) : __ldg(scol + e);
+            use[u] = k0 + u < len && (fixcol == nullptr || ((__ldg(fixcol + base + k) >> lane) & 1u) == 0u);
+        }
+        float3 xj[kOperatorBatch];
+#pragma unroll
+        for (int u = 0; u < kOperatorBatch; ++u) xj[u] = ld3(x, j[u]);
+#pragma unroll
+        for (int u = 0; u < kOperatorBatch; ++u)
+            if (use[u]) acc = acc + block_mul(A[u], B[u], C[u], xj[u]);
     }
     st3(y, row, acc);
 }
@@ -250,7 +283,7 @@ int fem_apply_operator(FemHandle* H, const float* x, float* y, void* stream) {
     if (h.P == 0 || h.nslices == 0) return FEM_OK;
     fem::Guard g(H->device);
     fem::apply_operator_kernel<<<fem::blocks((int64_t)h.nslices * 32, 256), 256, 0, (cudaStream_t)stream>>>(
-        h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.scol, x, y);
+        h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.scol, h.dcol, h.fixcol, x, y);
     return fem::report_cuda(cudaGetLastError());
 }
 
