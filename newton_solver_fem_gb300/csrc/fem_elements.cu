@@ -293,7 +293,7 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
     // added, so that many independent loads are in flight; the sums keep the
     // ascending incidence order.
     if (a.terms & FEM_TERM_SPRING) {
-        constexpr int kSpringBatch = 4;
+        constexpr int kSpringBatch = 2;
         const int e1 = a.spring_ptr[i + 1];
         for (int e0 = a.spring_ptr[i]; e0 < e1; e0 += kSpringBatch) {
             int ent[kSpringBatch], ia[kSpringBatch], ib[kSpringBatch];
