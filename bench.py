@@ -13,10 +13,11 @@ time with inputs resident in HBM.  ``e2e`` = the same metric through the
 public ``SolverFEM`` API with the frame's positions/velocities copied from
 pinned host memory and the result read back every frame.  ``roofline`` = the
 persistent PCG kernel's algorithmic bytes per launch over its CUDA-event launch
-time.  ``cpu_baseline`` = the CPU oracle (NumPy/SciPy restatement of the
-reference algorithm) on a bounded sample of the same workload.
+time.  ``cpu_baseline`` = the float32 C/OpenMP port of the reference algorithm
+(``oracle/fem_port.c``, checked against the float64 NumPy oracle by the tests)
+on all host cores, on a bounded sample of the same workload.
 
-``--impl reference`` times that CPU restatement alone on the same metric and
+``--impl reference`` times that C/OpenMP port alone on the same metric and
 config (the reference itself needs Warp and Newton, which cannot be installed
 in this image).  Multi-GPU: the single mesh does not shard, so N GPUs run N
 independent replicas ("replicas only"); value = all replicas' DOF-substeps / max

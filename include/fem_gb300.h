@@ -366,14 +366,23 @@ int fem_prepared_reconstruct(FemHandle* h, const FemPreparedWs* ws, const float*
  * an allocation's implicit synchronisation), which rules out fem_create.
  * offsets [rows+1], columns [nnzb], values [nnzb,3,3], rhs [rows,3] and
  * x_inout [rows,3] (warm start in, solution out) are device pointers; info is
- * an optional device int[2] receiving (iterations, status).  Solves
- * A x = rhs to ||r|| <= tolerance ||rhs|| with the reference's RHS
- * normalisation and at most maxiter iterations.  Working vectors live in a
- * static device array sized for at most 65,536 block rows (about 6.5 MB per
- * GPU that loads the library, held until exit); larger systems return
- * FEM_ERR_BAD_ARG.  The first call on a device resolves that array's address
- * and must come before any stream capture.  All calls share the array, so
- * calls that overlap on the GPU race; serialise them. */
+ * an optional device int[2] receiving (iterations, status bits: 1 a bounded
+ * grid-barrier wait timed out, 2 a non-finite value).  Solves A x = rhs to
+ * ||r|| <= tolerance ||rhs|| with the reference's RHS normalisation and at
+ * most maxiter iterations.  There is no fixed-node projection: the caller's
+ * matrix and rhs must already hold it (identity rows and zero columns at
+ * fixed nodes, zero rhs there), as SolverFEM's exported operator does.
+ * Failures are reported only on the device: the return code covers argument
+ * and launch errors, so with info == NULL a timeout or a non-finite solve goes
+ * unnoticed.  After a non-finite solve x_inout keeps the warm start; after a
+ * timeout its contents are unspecified.  Each wait gives up after 2 s, or after
+ * the nanoseconds in the environment variable FEM_NOALLOC_WAIT_LIMIT_NS (read
+ * at every call).  Working vectors live in a static device array sized for at
+ * most 65,536 block rows (about 6.5 MB per GPU that loads the library, held
+ * until exit); larger systems return FEM_ERR_BAD_ARG.  The first call on a
+ * device resolves that array's address and must come before any stream
+ * capture; calls after cudaDeviceReset are not supported.  All calls share the
+ * array, so calls that overlap on the GPU race; serialise them. */
 int fem_pcg_solve_noalloc(const int32_t* offsets, const int32_t* columns, const float* values, const float* rhs,
                           float* x_inout, int32_t rows, float tolerance, int32_t maxiter, int32_t* info,
                           void* stream);

@@ -21,7 +21,23 @@
 // Host code cannot use the array's name as a device address, so the first
 // call on each device looks the address up with cudaGetSymbolAddress (with
 // that device current) and caches it, together with the launch configuration.
-// Make that first call before any stream capture.
+// Make that first call before any stream capture.  The cache is not refreshed:
+// calls after cudaDeviceReset (or any teardown of the device's primary
+// context) are not supported.
+//
+// Failures.  Every grid barrier wait is bounded (2 s, or the nanoseconds in the
+// environment variable FEM_NOALLOC_WAIT_LIMIT_NS read at each call).  A CTA
+// whose wait runs out, and every CTA that then sees the shared failure flag,
+// skips to a common exit instead of returning, so the optional info word is
+// always written: info[0] = iterations done, info[1] = status bits (1: a wait
+// timed out, 2: a non-finite value in the solve).  The host zeroes info on the
+// caller's stream before the launch and the kernel only ORs bits into
+// info[1], so no failure report is lost.  After a non-finite value every CTA
+// leaves x_inout untouched (the warm start survives); after a timeout the CTAs
+// that saw it leave their rows untouched and the others may already have
+// written theirs, so x_inout is unspecified.  With info == NULL neither failure
+// is visible to the caller.
+#include <cstdlib>
 #include <mutex>
 
 #include "fem_gb300.h"
@@ -105,17 +121,21 @@ __device__ __forceinline__ unsigned load_acquire(const unsigned* p) {
 }
 
 // Bounded grid barrier (counter zeroed before the launch); false on timeout.
+// The counter and the target are compared as a wrap-safe difference: the
+// counter only grows, and no CTA runs more than one barrier ahead, so the
+// difference stays far inside the signed 32-bit range however many barriers
+// a solve takes.
 __device__ bool barrier(const Scratch& s, unsigned& epoch, long long limit_ns, int* flag) {
     __syncthreads();
     if (threadIdx.x == 0) {
         epoch += 1;
-        unsigned target = epoch * gridDim.x;
+        const unsigned target = epoch * gridDim.x;  // modulo 2^32, like the counter
         __threadfence();
         atomicAdd(s.barrier, 1u);
         int ok = 1;
         unsigned long long t0 = now_ns();
         unsigned spins = 0;
-        while (load_acquire(s.barrier) < target) {
+        while ((int)(load_acquire(s.barrier) - target) < 0) {
             if ((++spins & 63u) == 1u) {
                 if (atomicAdd(s.status, 0) != 0 || (long long)(now_ns() - t0) >= limit_ns) {
                     ok = 0;
@@ -196,17 +216,21 @@ __device__ __forceinline__ void row_mul(const Args& a, const float* vec, int i, 
     out[2] = s2;
 }
 
-__global__ void __launch_bounds__(kThreads) noalloc_pcg_kernel(Args a) {
-    __shared__ double red[3 * 32];
-    __shared__ double tot[3];
-    __shared__ int flag;
-    Scratch s = carve(a.scratch);
+// The solve proper.  Returns the CG iterations done and sets *fail: bit 1 when
+// a barrier wait ran out (this CTA's or, seen through the shared status word,
+// another CTA's), bit 2 when a grid total is non-finite (every CTA forms the
+// same totals, so every CTA sets it at the same point).  Either way the CTA
+// goes straight to the common exit.
+__device__ int noalloc_solve(const Args& a, const Scratch& s, double* red, double* tot, int* flag, float* scale_out,
+                             int* fail) {
     const int n = a.n;
     const int rows_per_cta = (n + gridDim.x - 1) / gridDim.x;
     const int r0 = blockIdx.x * rows_per_cta;
     const int r1 = min(n, r0 + rows_per_cta);
     unsigned epoch = 0;
     int ph = 0;  // reduction counter (selects the partial-array half)
+    *fail = 0;
+    *scale_out = 1.0f;
 
     // preconditioner from the diagonal blocks (identity where a row has none), max |b|
     double mx = 0.0;
@@ -231,7 +255,10 @@ __global__ void __launch_bounds__(kThreads) noalloc_pcg_kernel(Args a) {
             half(s, ph)[4 * blockIdx.x + 3] = m;
         }
     }
-    if (!barrier(s, epoch, a.limit_ns, &flag)) return;
+    if (!barrier(s, epoch, a.limit_ns, flag)) {
+        *fail = 1;
+        return 0;
+    }
     if (threadIdx.x == 0) {
         double m = 0.0;
         for (int k = 0; k < (int)gridDim.x; ++k) m = fmax(m, half(s, ph)[4 * k + 3]);
@@ -241,13 +268,17 @@ __global__ void __launch_bounds__(kThreads) noalloc_pcg_kernel(Args a) {
     ++ph;
     const float maximum = (float)tot[0];
     const float scale = (maximum > 0.0f && maximum < 1.0e-12f) ? fminf(1.0f / maximum, 1.0e30f) : 1.0f;
+    *scale_out = scale;
     __syncthreads();
 
     // x0 = scaled warm start (zero when b == 0)
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
         for (int c = 0; c < 3; ++c)
             s.x[3 * (size_t)i + c] = maximum == 0.0f ? 0.0f : scale * a.x_inout[3 * (size_t)i + c];
-    if (!barrier(s, epoch, a.limit_ns, &flag)) return;
+    if (!barrier(s, epoch, a.limit_ns, flag)) {
+        *fail = 1;
+        return 0;
+    }
     double rr = 0, rz = 0, bb = 0;
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
         float ax[3];
@@ -269,13 +300,20 @@ __global__ void __launch_bounds__(kThreads) noalloc_pcg_kernel(Args a) {
         }
     }
     cta_partials(s, ph, rr, rz, bb, red);
-    if (!barrier(s, epoch, a.limit_ns, &flag)) return;
+    if (!barrier(s, epoch, a.limit_ns, flag)) {
+        *fail = 1;
+        return 0;
+    }
     grid_totals(s, ph++, tot);
     rr = tot[0];
     rz = tot[1];
     bb = tot[2];
     const double atol_sq = (double)a.tol * a.tol * bb;
     int it = 0;
+    if (!isfinite(rr)) {  // every CTA sees the same totals, so all of them stop here
+        *fail = 2;
+        return it;
+    }
     while (it < a.maxiter && rr > atol_sq) {
         double pap = 0;
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
@@ -287,10 +325,17 @@ __global__ void __launch_bounds__(kThreads) noalloc_pcg_kernel(Args a) {
             }
         }
         cta_partials(s, ph, pap, 0.0, 0.0, red);
-        if (!barrier(s, epoch, a.limit_ns, &flag)) return;
+        if (!barrier(s, epoch, a.limit_ns, flag)) {
+            *fail = 1;
+            return it;
+        }
         grid_totals(s, ph++, tot);
         const float alpha = (float)(rz / tot[0]);
         __syncthreads();
+        if (!isfinite(alpha)) {  // same value in every CTA: all stop before touching x
+            *fail = 2;
+            return it;
+        }
         double rr_l = 0, rz_l = 0;
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
             float r[3];
@@ -309,29 +354,54 @@ __global__ void __launch_bounds__(kThreads) noalloc_pcg_kernel(Args a) {
             }
         }
         cta_partials(s, ph, rr_l, rz_l, 0.0, red);
-        if (!barrier(s, epoch, a.limit_ns, &flag)) return;
+        if (!barrier(s, epoch, a.limit_ns, flag)) {
+            *fail = 1;
+            return it;
+        }
         grid_totals(s, ph++, tot);
         const float beta = (float)(tot[1] / rz);
         rr = tot[0];
         rz = tot[1];
         __syncthreads();
+        ++it;
+        if (!isfinite(rr)) {
+            *fail = 2;
+            return it;
+        }
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
             for (int c = 0; c < 3; ++c) {
                 size_t k = 3 * (size_t)i + c;
                 s.p[k] = s.z[k] + beta * s.p[k];
             }
-        ++it;
-        if (!isfinite(rr)) {
-            if (threadIdx.x == 0) atomicOr(s.status, 2);
-            break;
+        if (!barrier(s, epoch, a.limit_ns, flag)) {
+            *fail = 1;
+            return it;
         }
-        if (!barrier(s, epoch, a.limit_ns, &flag)) return;
     }
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
-        for (int c = 0; c < 3; ++c) a.x_inout[3 * (size_t)i + c] = s.x[3 * (size_t)i + c] / scale;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && a.info != nullptr) {
-        a.info[0] = it;
-        a.info[1] = atomicAdd(s.status, 0);
+    return it;
+}
+
+__global__ void __launch_bounds__(kThreads) noalloc_pcg_kernel(Args a) {
+    __shared__ double red[3 * 32];
+    __shared__ double tot[3];
+    __shared__ int flag;
+    const Scratch s = carve(a.scratch);
+    float scale = 1.0f;
+    int fail = 0;
+    const int it = noalloc_solve(a, s, red, tot, &flag, &scale, &fail);
+    // Common exit.  A CTA that saw a failure keeps the caller's warm start in
+    // its rows of x_inout and ORs the failure into info[1] (zeroed by the host).
+    if (fail == 0) {
+        const int n = a.n;
+        const int rows_per_cta = (n + gridDim.x - 1) / gridDim.x;
+        const int r0 = blockIdx.x * rows_per_cta;
+        const int r1 = min(n, r0 + rows_per_cta);
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+            for (int c = 0; c < 3; ++c) a.x_inout[3 * (size_t)i + c] = s.x[3 * (size_t)i + c] / scale;
+    }
+    if (threadIdx.x == 0 && a.info != nullptr) {
+        if (fail != 0) atomicOr(a.info + 1, fail);
+        if (blockIdx.x == 0) a.info[0] = it;
     }
 }
 
@@ -391,6 +461,18 @@ extern "C" int fem_pcg_solve_noalloc(const int32_t* offsets, const int32_t* colu
     Scratch sc = carve(d->scratch);
     if (cudaError_t e = cudaMemsetAsync(sc.barrier, 0, 128, s); e != cudaSuccess)  // barrier + status
         return fem::report_cuda(e);
+    if (info != nullptr)  // the kernel ORs failure bits into info[1]
+        if (cudaError_t e = cudaMemsetAsync(info, 0, 2 * sizeof(int32_t), s); e != cudaSuccess)
+            return fem::report_cuda(e);
+    long long limit_ns = 2000000000LL;
+    if (const char* env = std::getenv("FEM_NOALLOC_WAIT_LIMIT_NS")) {
+        char* end = nullptr;
+        const long long v = std::strtoll(env, &end, 10);
+        if (end == env || *end != '\0' || v < 0)
+            return fem::report(FEM_ERR_BAD_ARG, "fem_pcg_solve_noalloc: FEM_NOALLOC_WAIT_LIMIT_NS must be a "
+                                                "non-negative integer");
+        limit_ns = v;
+    }
     int rows_per_cta_min = 64;  // keep CTAs busy
     int grid = (rows + rows_per_cta_min - 1) / rows_per_cta_min;
     if (grid > d->max_grid) grid = d->max_grid;
@@ -406,7 +488,7 @@ extern "C" int fem_pcg_solve_noalloc(const int32_t* offsets, const int32_t* colu
     a.maxiter = maxiter;
     a.info = info;
     a.scratch = d->scratch;
-    a.limit_ns = 2000000000LL;
+    a.limit_ns = limit_ns;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kThreads);

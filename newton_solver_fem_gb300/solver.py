@@ -155,7 +155,9 @@ class SolverFEM:
         if solver_type not in ("cg", "bicgstab", "gmres", "cr"):
             raise ValueError(f"Invalid solver type: {solver_type}")
         if solver_type != "cg":
-            raise NotImplementedError(f"solver_type={solver_type!r}: the GB300 hot path implements 'cg'")
+            raise NotImplementedError(
+                f"solver_type={solver_type!r} is not implemented on GB300; pass solver_type='cg' (the reference's "
+                f"default is 'bicgstab', but its hot path and every shipped configuration use 'cg')")
         if preconditioner_type not in ("block_diag", "diag"):
             raise NotImplementedError(f"preconditioner_type={preconditioner_type!r} is not implemented")
         self.torque_stiffness = float(torque_stiffness)

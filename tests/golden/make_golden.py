@@ -6,9 +6,9 @@ VTK order) and ``tet_cantilever.usda`` (12 nodes, 10 tets).  OpenUSD (``pxr``)
 is not installed, so this script reads the three plain-text attributes it needs
 (``points``, ``tetVertexIndices`` and ``customData.hex_mesh.hex_vertex_indices``)
 with regular expressions and stores them as arrays.  Run it where the reference
-checkout is available::
+checkout is available, passing the checkout's root directory::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 """
 
 import re
@@ -53,4 +53,6 @@ def main(reference_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout root>")
+    main(sys.argv[1])

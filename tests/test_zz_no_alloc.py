@@ -64,3 +64,50 @@ def test_noalloc_rejects_sizes_beyond_its_static_capacity(cuda_device):
     lib = _lib.load()
     code = lib.fem_pcg_solve_noalloc(None, None, None, None, None, 65537, 1e-2, 10, None, None)
     assert code == _lib.FEM_ERR_BAD_ARG
+
+
+def _chain_system(rows, device):
+    """A block tridiagonal SPD system (4I on the diagonal, -I to each neighbour) in BSR form."""
+    import numpy as np
+
+    offsets, columns, values = [0], [], []
+    for i in range(rows):
+        for j in (i - 1, i, i + 1):
+            if 0 <= j < rows:
+                columns.append(j)
+                values.append(4.0 * np.eye(3) if j == i else -np.eye(3))
+        offsets.append(len(columns))
+
+    class A:
+        pass
+
+    a = A()
+    a.offsets = torch.tensor(offsets, dtype=torch.int32, device=device)
+    a.columns = torch.tensor(columns, dtype=torch.int32, device=device)
+    a.values = torch.tensor(np.asarray(values), dtype=torch.float32, device=device)
+    return a
+
+
+def test_noalloc_bounded_wait_reports_timeout_in_info_and_recovers(cuda_device, monkeypatch):
+    """A grid-barrier wait that runs out (zero wait limit) still writes info: status bit 1 is set and the
+    kernel returns.  With the default limit the next call on the same context solves the system."""
+    lib = _lib.load()
+    rows = 60_000  # hundreds of co-resident CTAs, so some CTA reaches the first barrier before the others
+    A = _chain_system(rows, cuda_device)
+    g = torch.Generator(device=cuda_device).manual_seed(7)
+    rhs = torch.randn((rows, 3), device=cuda_device, generator=g)
+    info = torch.full((2,), -1, dtype=torch.int32, device=cuda_device)
+    x = torch.zeros((rows, 3), dtype=torch.float32, device=cuda_device)
+    monkeypatch.setenv("FEM_NOALLOC_WAIT_LIMIT_NS", "0")
+    _solve_noalloc(lib, A, rhs, x, rows, 1e-6, 100, info)
+    assert int(info[1]) & 1
+    monkeypatch.delenv("FEM_NOALLOC_WAIT_LIMIT_NS")
+    for _ in range(2):  # the context stays usable: two solves in a row at the default limit
+        x = torch.zeros((rows, 3), dtype=torch.float32, device=cuda_device)
+        _solve_noalloc(lib, A, rhs, x, rows, 1e-6, 100, info)
+        assert int(info[1]) == 0
+        xs, bs = x.double().cpu(), rhs.double().cpu()
+        ax = 4.0 * xs
+        ax[1:] -= xs[:-1]
+        ax[:-1] -= xs[1:]
+        assert float((ax - bs).norm() / bs.norm()) < 1e-5
