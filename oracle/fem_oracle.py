@@ -98,12 +98,25 @@ def signed_svd(F: np.ndarray):
 
 
 def clamp_stretch(F: np.ndarray, lo: float, hi: float) -> np.ndarray:
-    """``U diag(clamp(S, lo, hi)) V^T``; identity map when a bound is negative (kernels.py:421-444)."""
+    """``U diag(clamp(S, lo, hi)) V^T``; identity map when a bound is negative (kernels.py:421-444).
+
+    Matrices whose signed stretches provably lie in [lo, hi] are returned
+    unchanged, which is what the clamp does to them; only the others are
+    decomposed.  The test is sufficient: J > 0, ||F||_F^2 <= hi^2 bounds the
+    largest stretch, and the smallest is J / (s_a s_b) >= 2 J / ||F||_F^2 >= lo.
+    """
     if lo < 0.0 or hi < 0.0 or len(F) == 0:
         return F
-    U, S, V = signed_svd(F)
+    ic = np.sum(F * F, axis=(-2, -1))
+    J = np.linalg.det(F)
+    need = ~((J > 0.0) & (ic <= hi * hi) & (2.0 * J >= lo * ic))
+    if not need.any():
+        return F
+    out = np.array(F, copy=True)
+    U, S, V = signed_svd(F[need])
     S = np.maximum(np.minimum(S, hi), lo)
-    return np.einsum("eij,ej,ekj->eik", U, S, V)
+    out[need] = np.einsum("eij,ej,ekj->eik", U, S, V)
+    return out
 
 
 def clamp_active(F: np.ndarray, lo: float, hi: float) -> np.ndarray:
@@ -601,11 +614,15 @@ def hex_tangent(x, hexes, inv_J0, det_J0_w, mats, lo, hi, dt):
     dJ = np.einsum("hgij,hgaj->hgai", cof, dN)
     dots = np.einsum("hgai,hgbi->hgab", dN, dN)
     w = det_J0_w.astype(np.float64)
-    K = (
-        np.einsum("hg,hgab,ij->habij", w * mu[:, None] * s, dots, np.eye(3))
-        + np.einsum("hg,hgai,hgbj->habij", w * coef, Fd, Fd)
-        + np.einsum("hg,hgai,hgbj->habij", w * lam[:, None], dJ, dJ)
-    ) * (dt * dt)
+    # Gauss sums as batched products over g: [H, 24, g] @ [H, g, 24] -> [H, (a i), (b j)]
+    def outer_sum(weight, G):
+        G2 = G.reshape(Hn, 8, 24)
+        return np.matmul(np.swapaxes(weight[:, :, None] * G2, 1, 2), G2).reshape(Hn, 8, 3, 8, 3).transpose(0, 1, 3, 2, 4)
+
+    iso = np.einsum("hg,hgab->hab", w * mu[:, None] * s, dots)
+    K = outer_sum(w * coef, Fd) + outer_sum(w * lam[:, None], dJ)
+    K += iso[:, :, :, None, None] * np.eye(3)
+    K *= dt * dt
     return rows.reshape(-1), cols.reshape(-1), K.reshape(-1, 3, 3)
 
 

@@ -7,6 +7,7 @@
  * Reference algorithm followed (src/newton_solver_fem/_src/solvers/fem/):
  *   tet force          kernels.py:511-632     tet tangent   kernels.py:635-850
  *   hex force          kernels.py:1481-1601   hex tangent   kernels.py:1609-1747
+ *   springs            kernels.py:176-218, 294-366   spring damping restore  implicit_predictor.py:26-41
  *   ground, gravity    kernels.py:1132-1195, 1273-1307
  *   block inverse      kernels.py:1817-1849   predictor     implicit_predictor.py:9-41
  *   RHS normalisation  kernels.py:1779-1814   solve         solver.py:1254-1351 (Warp cg semantics)
@@ -339,6 +340,33 @@ void port_hex_tangent(int64_t H, const int32_t* idx, const float* invJ, const fl
         }
         float scale = dt * dt;
         for (int k = 0; k < 64 * 9; ++k) vals[576 * h + k] = ((float*)K)[k] * scale;
+    }
+}
+
+/* Linear spring + damping forces (kernels.py:176-218) into out[2S][3]: entry 2s
+ * is the force on the first endpoint, 2s+1 on the second (zero for springs with
+ * a negative index or a length below 1e-6). */
+void port_spring_forces(int64_t S, const int32_t* idx, const float* rest, const float* ke, const float* kd,
+                        const float* q, const float* v, float* out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t s = 0; s < S; ++s) {
+        float* o = out + 6 * s;
+        memset(o, 0, 6 * sizeof(float));
+        int32_t i = idx[2 * s], j = idx[2 * s + 1];
+        if (i < 0 || j < 0) continue;
+        float xij[3], vij[3];
+        for (int c = 0; c < 3; ++c) {
+            xij[c] = q[3 * (int64_t)i + c] - q[3 * (int64_t)j + c];
+            vij[c] = v[3 * (int64_t)i + c] - v[3 * (int64_t)j + c];
+        }
+        float L = sqrtf(dot3(xij, xij));
+        if (L < 1.0e-6f) continue;
+        float d[3] = {xij[0] / L, xij[1] / L, xij[2] / L};
+        float m = ke[s] * (L - rest[s]) + kd[s] * dot3(d, vij);
+        for (int c = 0; c < 3; ++c) {
+            o[c] = -d[c] * m;
+            o[3 + c] = d[c] * m;
+        }
     }
 }
 

@@ -43,6 +43,7 @@ def load():
         lib.port_threads.restype = ctypes.c_int
         lib.port_tet_forces.argtypes = [i64, p, p, p, p, p, f, f, p]
         lib.port_hex_forces.argtypes = [i64, p, p, p, p, p, p, f, f, p]
+        lib.port_spring_forces.argtypes = [i64, p, p, p, p, p, p, p]
         lib.port_tet_tangent.argtypes = [i64, p, p, p, p, f, f, f, p]
         lib.port_hex_tangent.argtypes = [i64, p, p, p, p, p, f, f, f, p]
         lib.port_gather.argtypes = [i64, p, p, p, p]
@@ -67,10 +68,11 @@ def _csr(keys: np.ndarray, n: int):
 
 
 class PortFEM:
-    """Float32 CPU port of the hot path for one scene (Tet4 and/or Hex8, ground, gravity, fixed nodes)."""
+    """Float32 CPU port of the hot path for one scene (Tet4 and/or Hex8, springs, ground, gravity, fixed nodes)."""
 
     def __init__(self, x, mass, *, tets=None, tet_poses=None, tet_materials=None, hexes=None, hex_inv_J0=None,
-                 hex_det_J0_w=None, hex_materials=None, gravity=(0.0, 0.0, -9.81), dt=1.0 / 600.0, min_stretch=0.05,
+                 hex_det_J0_w=None, hex_materials=None, springs=None, spring_rest=None, spring_ke=None, spring_kd=None,
+                 gravity=(0.0, 0.0, -9.81), dt=1.0 / 600.0, min_stretch=0.05,
                  max_stretch=20.0, ground_plane=None, ground=(1.0e5, 1.0e2, 1.0e3, 0.5), radius=0.0, fixed=None,
                  maxiter=50, tolerance=1.0e-2):
         self.lib = load()
@@ -95,12 +97,26 @@ class PortFEM:
         self.fixed_mask = np.zeros(n, np.uint8)
         self.fixed_mask[self.fixed] = 1
         self.maxiter, self.tol = int(maxiter), float(tolerance)
+        self.springs = np.ascontiguousarray(np.zeros((0, 2)) if springs is None else springs, np.int32)
+        S = len(self.springs)
+        rest_len = np.linalg.norm(self.rest[self.springs[:, 0]] - self.rest[self.springs[:, 1]], axis=1) \
+            if spring_rest is None else spring_rest
+        self.spring_rest = np.ascontiguousarray(rest_len, f32)
+        self.spring_ke = np.ascontiguousarray(np.zeros(S) if spring_ke is None else spring_ke, f32)
+        self.spring_kd = np.ascontiguousarray(np.zeros(S) if spring_kd is None else spring_kd, f32)
         T, H = len(self.tets), len(self.hexes)
-        # triplet layout [P | 16T | 64H] (no springs in the port)
-        rows = np.concatenate([np.arange(n), np.repeat(self.tets, 4, axis=1).ravel(), np.repeat(self.hexes, 8, axis=1).ravel()])
-        cols = np.concatenate([np.arange(n), np.tile(self.tets, (1, 4)).ravel(), np.tile(self.hexes, (1, 8)).ravel()])
-        key = rows.astype(np.int64) * n + cols
+        # triplet layout [P | 2S | 16T | 64H] (solver.py:312-321; springs as (a, b), (b, a) pairs)
+        sp_rows = self.springs.reshape(-1)
+        sp_cols = self.springs[:, ::-1].reshape(-1)
+        rows = np.concatenate([np.arange(n), sp_rows, np.repeat(self.tets, 4, axis=1).ravel(),
+                               np.repeat(self.hexes, 8, axis=1).ravel()])
+        cols = np.concatenate([np.arange(n), sp_cols, np.tile(self.tets, (1, 4)).ravel(),
+                               np.tile(self.hexes, (1, 8)).ravel()])
+        valid = (rows >= 0) & (cols >= 0)  # springs with a negative index add no block
+        rows, cols = np.where(valid, rows, 0), np.where(valid, cols, 0)
+        key = np.where(valid, rows.astype(np.int64) * n + cols, -1)
         order = np.argsort(key, kind="stable")
+        order = order[key[order] >= 0]
         ks = key[order]
         uniq, start = np.unique(ks, return_index=True)
         self.contrib = order.astype(np.int32)
@@ -116,6 +132,9 @@ class PortFEM:
         self.minv = np.zeros((n, 9), f32)
         self.elem_tet = np.zeros((4 * T, 3), f32)
         self.elem_hex = np.zeros((8 * H, 3), f32)
+        self.elem_spring = np.zeros((2 * S, 3), f32)
+        ends = self.springs.reshape(-1).astype(np.int64)
+        self.spring_ptr, self.spring_ent = _csr(np.where(ends >= 0, ends, n), n + 1)
         self.tet_ptr, self.tet_ent = _csr(self.tets.ravel().astype(np.int64), n)
         self.hex_ptr, self.hex_ent = _csr(self.hexes.ravel().astype(np.int64), n)
         self.dv = np.zeros((n, 3), f32)
@@ -124,20 +143,35 @@ class PortFEM:
         self.refresh_tangent(self.rest)
 
     def _set_constant(self, dt):
-        d = np.zeros((self.n, 9), np.float32)
-        d[:, 0] = d[:, 4] = d[:, 8] = self.mass
-        self.trip[: self.n] = d
+        """Mass + spring (h d + h^2 k) diagonal and -(h d + h^2 k) I off-diagonal blocks (solver.py:1015-1060)."""
+        n, S = self.n, len(self.springs)
+        h = np.float32(dt)
+        c = (h * self.spring_kd + h * h * self.spring_ke).astype(np.float32)
+        diag = self.mass.astype(np.float32).copy()
+        for col in (0, 1):
+            idx = self.springs[:, col]
+            ok = idx >= 0
+            np.add.at(diag, idx[ok], c[ok])
+        d = np.zeros((n, 9), np.float32)
+        d[:, 0] = d[:, 4] = d[:, 8] = diag
+        self.trip[:n] = d
+        if S:
+            off = np.zeros((2 * S, 9), np.float32)
+            cc = np.repeat(-c, 2)
+            off[:, 0] = off[:, 4] = off[:, 8] = cc
+            self.trip[n:n + 2 * S] = off
 
     def refresh_tangent(self, q):
         q = np.ascontiguousarray(q, np.float32).copy()
         q[self.fixed] = self.rest[self.fixed]
         n, T, H, L = self.n, len(self.tets), len(self.hexes), self.lib
+        base = n + 2 * len(self.springs)
         if T:
             L.port_tet_tangent(T, _p(self.tets), _p(self.tet_poses), _p(self.tet_mat), _p(q), self.lo, self.hi, self.dt,
-                               _p(self.trip[n:]))
+                               _p(self.trip[base:]))
         if H:
             L.port_hex_tangent(H, _p(self.hexes), _p(self.hex_invJ), _p(self.hex_detw), _p(self.hex_mat), _p(q),
-                               self.lo, self.hi, self.dt, _p(self.trip[n + 16 * T:]))
+                               self.lo, self.hi, self.dt, _p(self.trip[base + 16 * T:]))
         L.port_gather(self.nnzb, _p(self.cptr), _p(self.contrib), _p(self.trip), _p(self.values))
         L.port_block_jacobi(n, _p(self.offsets), _p(self.columns), _p(self.values), _p(self.minv))
         return q
@@ -150,6 +184,12 @@ class PortFEM:
         n, T, H, L = self.n, len(self.tets), len(self.hexes), self.lib
         ft = np.zeros((n, 3), np.float32)
         fh = np.zeros((n, 3), np.float32)
+        fs = np.zeros((n + 1, 3), np.float32)
+        S = len(self.springs)
+        if S:
+            L.port_spring_forces(S, _p(self.springs), _p(self.spring_rest), _p(self.spring_ke), _p(self.spring_kd),
+                                 _p(q), _p(v), _p(self.elem_spring))
+            L.port_node_gather(n, _p(self.spring_ptr), _p(self.spring_ent), _p(self.elem_spring), _p(fs))
         if T:
             L.port_tet_forces(T, _p(self.tets), _p(self.tet_poses), _p(self.tet_mat), _p(q), _p(v), self.lo, self.hi,
                               _p(self.elem_tet))
@@ -159,13 +199,19 @@ class PortFEM:
                               self.lo, self.hi, _p(self.elem_hex))
             L.port_node_gather(n, _p(self.hex_ptr), _p(self.hex_ent), _p(self.elem_hex), _p(fh))
         h = np.float32(dt)
-        f = ft * h + fh * h
+        f = fs[:n] * h + ft * h + fh * h  # term order: spring, tet, hex (solver.py:571-582)
         if self.ground_plane is not None:
             ke, kd, kf, mu = self.ground
             fg = O.ground_forces(q, v, self.radius, self.inv_mass, np.ones(n, np.int32), ke, kd, kf, mu,
                                  self.ground_plane, self.gravity)
             f = f + fg.astype(np.float32) * h
         f = f + (np.outer(self.mass, self.gravity).astype(np.float32)) * h
+        if S:  # spring damping restored after the elastic predictor (implicit_predictor.py:26-41); rhs = f - cv
+            a, b = self.springs[:, 0], self.springs[:, 1]
+            ok = (a >= 0) & (b >= 0)
+            corr = (h * self.spring_kd[ok, None]) * (v[a[ok]] - v[b[ok]])
+            np.add.at(f, a[ok], corr)
+            np.subtract.at(f, b[ok], corr)
         f = np.ascontiguousarray(f, np.float32)
         q_out = np.empty_like(q)
         v_out = np.empty_like(v)

@@ -1,0 +1,179 @@
+"""Parity at the benchmark sizes (``-m gpu``): the Hex8 64^3 block, the jittered Tet4 48^3 block and
+the 256-scene batch, checked through ``SolverFEM`` (ctypes -> libfemgb300.so).
+
+* One substep with a fixed CG iteration count (tolerance 1e-30, the reference semantics for
+  iterate-level parity) against the float64 oracle: velocity increment within 1e-4 relative L2,
+  and the assembled matrix (pattern exact, values within 1e-5 of the largest entry).
+* Trajectories at the workloads' own settings (CG tolerance 1e-2, at most 50 iterations, warm
+  start) against the float32 C/OpenMP port of the same algorithm, which ``tests/test_port.py``
+  checks against the oracle: every frame's positions within 1e-3 of the bounding-box diagonal.
+* The 256-scene batch: every scene's increment against its own oracle at a fixed iteration count.
+
+The oracles run on the host cores; the batch's 256 oracles run in a ``spawn`` process pool (a
+process forked after CUDA initialisation can hang).
+"""
+
+import multiprocessing as mp
+import os
+
+import numpy as np
+import pytest
+from gpu_helpers import rel_l2, rounded, scene_pair, tensor, to_np
+
+from newton_solver_fem_gb300 import scenes
+from oracle import fem_oracle as O
+from oracle import fem_port
+
+pytestmark = pytest.mark.gpu
+
+FIXED_ITERATIONS = 12  # near the workloads' mean CG count at tolerance 1e-2 (13-14)
+
+
+@pytest.fixture(autouse=True)
+def _cuda(cuda_device):
+    yield
+
+
+def _matrix_matches(solver, oracle):
+    A = solver.A_bsr
+    np.testing.assert_array_equal(A.offsets.cpu().numpy(), oracle.offsets)
+    np.testing.assert_array_equal(A.columns.cpu().numpy(), oracle.columns)
+    values = A.values.cpu().numpy().astype(np.float64)
+    err = np.abs(values - oracle.values).max() / np.abs(oracle.values).max()
+    assert err < 1e-5, err
+
+
+def _fixed_iteration_substep(sc, q, v):
+    """Refresh the tangent at q, take one substep from (q, v) with FIXED_ITERATIONS CG updates on the
+    GPU and in the oracle; return (gpu dv, oracle dv, solver, oracle)."""
+    model, solver, oracle = scene_pair(sc, linear_solver_maxiter=FIXED_ITERATIONS, linear_solver_tolerance=1e-30)
+    s0, s1 = model.state(), model.state()
+    s0.particle_q.copy_(tensor(q))
+    s0.particle_qd.copy_(tensor(v))
+    solver.refresh_tangent(s0.particle_q)
+    solver.step(s0, s1, None, None, sc.dt)
+    stats = solver.stats()
+    assert stats["max_iterations"] == FIXED_ITERATIONS and stats["status"] == 0
+    oracle.refresh_tangent(q)
+    oracle.step(q, v, sc.dt, fixed_iterations=FIXED_ITERATIONS)
+    return to_np(solver.velocity_increment), oracle.dv, solver, oracle
+
+
+def test_hex8_64_fixed_iteration_substep_matches_oracle():
+    """Hex8 64^3 (274,625 nodes): deformed start with the workload's seeded velocities and ground contact."""
+    sc = scenes.hex_block_64()
+    rng = np.random.default_rng(21)
+    q = rounded(sc.x + rng.normal(0.0, 2.0e-4, sc.x.shape))  # ~2% strain noise; bottom nodes dip below z = 0
+    v = rounded(sc.velocity)
+    dv, dv_ref, solver, oracle = _fixed_iteration_substep(sc, q, v)
+    _matrix_matches(solver, oracle)
+    assert rel_l2(dv, dv_ref) < 1e-4, rel_l2(dv, dv_ref)
+
+
+def test_tet4_48_fixed_iteration_substep_matches_oracle():
+    """Jittered Tet4 48^3 with 795,024 edge springs, lowered so its bottom layer presses into the ground."""
+    sc = scenes.tet_jittered_48()
+    rng = np.random.default_rng(22)
+    q = rounded(sc.x - (0.0, 0.0, 0.2015) + rng.normal(0.0, 2.0e-4, sc.x.shape))
+    v = rounded(rng.normal(0.0, 0.05, sc.x.shape))
+    dv, dv_ref, solver, oracle = _fixed_iteration_substep(sc, q, v)
+    _matrix_matches(solver, oracle)
+    assert rel_l2(dv, dv_ref) < 1e-4, rel_l2(dv, dv_ref)
+
+
+def _port_for(sc, model):
+    """The C/OpenMP port on exactly the GPU model's float32 inputs."""
+    x = rounded(model.particle_q.cpu().numpy())
+    args = dict(gravity=sc.gravity, dt=sc.dt, ground_plane=sc.ground_plane, ground=sc.ground,
+                fixed=sc.fixed if len(sc.fixed) else None, maxiter=sc.maxiter, tolerance=sc.tolerance)
+    if len(sc.tets):
+        args.update(tets=sc.tets, tet_poses=model.tet_poses.cpu().numpy(), tet_materials=sc.tet_materials)
+    if len(sc.hexes):
+        args.update(hexes=sc.hexes, hex_inv_J0=model.fem.hex_inv_J0.cpu().numpy(),
+                    hex_det_J0_w=model.fem.hex_det_J0_w.cpu().numpy(), hex_materials=sc.hex_materials)
+    if len(sc.springs):
+        args.update(springs=sc.springs, spring_rest=model.spring_rest_length.cpu().numpy(), spring_ke=sc.spring_ke,
+                    spring_kd=sc.spring_kd)
+    return fem_port.PortFEM(x, model.particle_mass.cpu().numpy(), **args)
+
+
+def _trajectory_error(sc, frames):
+    """Largest per-frame node distance between the GPU and the port over `frames` frames, over the
+    bounding-box diagonal; also returns the GPU's CG iteration counts and convergence record."""
+    model, solver, _ = scene_pair(sc, with_oracle=False)
+    port = _port_for(sc, model)
+    a, b = model.state(), model.state()
+    q = to_np(a.particle_q).astype(np.float32)
+    v = to_np(a.particle_qd).astype(np.float32)
+    diag = np.linalg.norm(np.ptp(sc.x, axis=0))
+    worst, iterations, unconverged = 0.0, [], 0
+    for _ in range(frames):
+        solver.refresh_tangent(a.particle_q)
+        q = port.refresh_tangent(q)
+        for _ in range(sc.substeps):
+            solver.step(a, b, None, None, sc.dt)
+            st = solver.stats()
+            iterations.append(st["max_iterations"])
+            unconverged += st["unconverged_scenes"]
+            a, b = b, a
+            q, v, _ = port.step(q, v, sc.dt)
+        worst = max(worst, float(np.abs(to_np(a.particle_q) - q).max() / diag))
+    assert np.isfinite(to_np(a.particle_q)).all()
+    return worst, iterations, unconverged
+
+
+def test_hex8_64_trajectory_30_frames_matches_port():
+    """30 frames x 10 substeps of the Hex8 64^3 block at tolerance 1e-2 within 1e-3 bbox diagonal of the port."""
+    sc = scenes.hex_block_64()
+    worst, iterations, unconverged = _trajectory_error(sc, 30)
+    assert worst < 1e-3, worst
+    assert max(iterations) <= sc.maxiter and unconverged == 0
+
+
+def test_tet4_48_trajectory_20_frames_matches_port():
+    """20 frames x 10 substeps of the falling Tet4 48^3 block (ground contact from frame 12 on) within
+    1e-3 bbox diagonal of the port."""
+    sc = scenes.tet_jittered_48()
+    worst, iterations, unconverged = _trajectory_error(sc, 20)
+    assert worst < 1e-3, worst
+    assert max(iterations) <= sc.maxiter and unconverged == 0
+
+
+def _scene_job(part, iterations):
+    x = rounded(part.x)
+    job = dict(x=x, mass=rounded(part.mass), q=x, v=np.zeros_like(x), iterations=iterations, dt=part.dt,
+               gravity=part.gravity, fixed=part.fixed, maxiter=iterations, tolerance=1e-30)
+    if len(part.tets):
+        job.update(tets=part.tets, tet_poses=scenes.tet_poses(x, part.tets), tet_materials=part.tet_materials)
+    if len(part.hexes):
+        inv, det = O.hex_builder_data(x, part.hexes)
+        job.update(hexes=part.hexes, hex_inv_J0=inv.astype(np.float32), hex_det_J0_w=det.astype(np.float32),
+                   hex_materials=part.hex_materials)
+    return job
+
+
+def test_batched_256_scenes_fixed_iterations_match_oracle_per_scene():
+    """The benchmark's 256-scene batch (128 Tet4 + 128 Hex8, dims U{4..32}^3, 1.56M nodes) in one handle:
+    each scene's increment after FIXED_ITERATIONS CG updates equals that scene's own oracle."""
+    import oracle_workers
+
+    sc = scenes.batched_scenes()
+    parts = scenes.split_batched(sc)
+    jobs = [_scene_job(p, FIXED_ITERATIONS) for p in parts]
+    workers = max(1, min(16, (os.cpu_count() or 2) - 1))
+    with mp.get_context("spawn").Pool(workers) as pool:
+        pending = pool.map_async(oracle_workers.fixed_iteration_dv, jobs, chunksize=1)
+        model, solver, _ = scene_pair(sc, with_oracle=False, linear_solver_maxiter=FIXED_ITERATIONS,
+                                      linear_solver_tolerance=1e-30)
+        s0, s1 = model.state(), model.state()
+        solver.refresh_tangent(s0.particle_q)
+        solver.step(s0, s1, None, None, sc.dt)
+        stats = solver.stats()
+        dv = to_np(solver.velocity_increment)
+        results = pending.get()
+    assert stats["status"] == 0
+    assert stats["scene_iterations"] == [FIXED_ITERATIONS] * len(parts)
+    offs = sc.scene_offsets
+    errors = [rel_l2(dv[offs[s]:offs[s + 1]], results[s][0]) for s in range(len(parts))]
+    assert max(errors) < 1e-4, (int(np.argmax(errors)), max(errors))
+    assert all(r[1] == [FIXED_ITERATIONS] for r in results)

@@ -471,16 +471,15 @@ def test_large_hex_block_true_residual_property():
                        A.offsets.cpu().numpy()), shape=(3 * P, 3 * P))
     rhs = to_np(s0.particle_f).ravel()
     res = np.linalg.norm(M @ to_np(solver.velocity_increment).ravel() - rhs) / np.linalg.norm(rhs)
-    assert st["max_iterations"] <= 50
-    if st["unconverged_scenes"] == 0:
-        assert res < 1e-2 * 1.01
+    assert st["unconverged_scenes"] == 0 and st["max_iterations"] <= 50, st
+    assert res < 1e-2 * 1.01, res
     assert np.isfinite(to_np(s1.particle_q)).all()
 
 
 def test_full_size_jittered_tet_block_with_springs_and_ground():
     """Full-size jittered Tet4 48^3 block (663,552 tets, 795,024 edge springs, ground): 3 frames of
-    10 substeps stay finite, every solve meets tol or its iteration cap, and the last substep's true
-    relative residual is re-checked in float64."""
+    10 substeps stay finite, every solve converges within its iteration cap, and the last substep's
+    true relative residual is re-checked in float64."""
     sp = pytest.importorskip("scipy.sparse")
     sc = scenes.tet_jittered_48()
     model, solver, _ = scene_pair(sc, with_oracle=False)
@@ -490,7 +489,7 @@ def test_full_size_jittered_tet_block_with_springs_and_ground():
         for k in range(sc.substeps):
             solver.step(a, b, None, None, sc.dt)
             st = solver.stats()
-            assert st["max_iterations"] <= sc.maxiter
+            assert st["max_iterations"] <= sc.maxiter and st["unconverged_scenes"] == 0, st
             a, b = b, a
     A = solver.A_bsr
     P = model.particle_count
@@ -499,8 +498,8 @@ def test_full_size_jittered_tet_block_with_springs_and_ground():
                        A.offsets.cpu().numpy()), shape=(3 * P, 3 * P))
     rhs = to_np(b.particle_f).ravel()
     res = np.linalg.norm(M @ to_np(solver.velocity_increment).ravel() - rhs) / np.linalg.norm(rhs)
-    if st["unconverged_scenes"] == 0:
-        assert res < sc.tolerance * 1.01
+    assert st["unconverged_scenes"] == 0, st
+    assert res < sc.tolerance * 1.01, res
     q = to_np(a.particle_q)
     assert np.isfinite(q).all()
     assert q[:, 2].min() > -0.01  # the ground holds the block (penetration below 1 cm)

@@ -21,12 +21,23 @@ def _pair(sc, **kw):
         inv, det = O.hex_builder_data(x, sc.hexes)
         args.update(hexes=sc.hexes, hex_inv_J0=inv.astype(np.float32), hex_det_J0_w=det.astype(np.float32),
                     hex_materials=sc.hex_materials)
+    if len(sc.springs):
+        rest = np.linalg.norm(x[sc.springs[:, 0]] - x[sc.springs[:, 1]], axis=1).astype(np.float32)
+        args.update(springs=sc.springs, spring_rest=rest, spring_ke=sc.spring_ke, spring_kd=sc.spring_kd)
     port = fem_port.PortFEM(x, m, ground=sc.ground, **args, **common)
     oracle = O.OracleFEM(x, m, ground_ke=ke, ground_kd=kd, ground_kf=kf, ground_mu=mu, **args, **common)
     return x, port, oracle
 
 
-@pytest.mark.parametrize("make", [scenes.tet_cantilever, lambda: scenes.hex_block_64(n=4)])
+def _jittered_in_contact():
+    """Jittered Tet4 4^3 block with edge springs, lowered so its bottom layer presses into the ground, moving."""
+    sc = scenes.tet_jittered_48(n=4)
+    sc.x = sc.x - (0.0, 0.0, 0.203)
+    sc.velocity = np.random.default_rng(11).normal(0.0, 0.05, sc.x.shape).astype(np.float32)
+    return sc
+
+
+@pytest.mark.parametrize("make", [scenes.tet_cantilever, lambda: scenes.hex_block_64(n=4), _jittered_in_contact])
 def test_port_matches_oracle(make):
     sc = make()
     x, port, oracle = _pair(sc)
