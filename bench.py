@@ -323,8 +323,91 @@ def batched_measurement(device: str, steps: int, warmup: int) -> dict:
     return out
 
 
+def launch_shape(solver) -> dict:
+    """The PCG launch configuration a handle uses (the tuning getters)."""
+    import ctypes
+
+    from newton_solver_fem_gb300 import _lib
+
+    lib = _lib.load()
+    out = {}
+    for name, key in (("pcg_ctas", _lib.FEM_TUNE_GRID), ("cta_threads", _lib.FEM_TUNE_CTA_THREADS),
+                      ("column_mode", _lib.FEM_TUNE_COMPACT_COLUMNS), ("l2_resident_slices", _lib.FEM_TUNE_RESIDENT_SLICES),
+                      ("resident_row_state", _lib.FEM_TUNE_RESIDENT_STATE), ("spmv_unroll", _lib.FEM_TUNE_SPMV_UNROLL),
+                      ("cg_variant", getattr(_lib, "FEM_TUNE_CG_VARIANT", None))):
+        if key is None:
+            continue
+        v = ctypes.c_int64()
+        _lib.check(lib.fem_get_tuning(solver._handle, key, ctypes.byref(v)))
+        out[name] = int(v.value)
+    return out
+
+
+class FrameWindow:
+    """Times K frames (tangent refresh + substeps, one captured CUDA graph each) starting from the
+    workload's initial state: before the warm-up replays and again before the timed replays the
+    state and the warm start are reset, so every run times the same simulated frames 0..K-1 whatever
+    the warm-up count.  CG iterations over the timed frames come from the solver's counters."""
+
+    def __init__(self, solver, model, substeps, dt, stream):
+        import torch
+
+        self.solver, self.substeps, self.dt, self.stream = solver, substeps, dt, stream
+        self.a, self.b = model.state(), model.state()
+        self.q0, self.v0 = self.a.particle_q.clone(), self.a.particle_qd.clone()
+        with torch.cuda.stream(stream):
+            self._frame()  # eager warm-up: first refresh, lazy setup
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            with torch.cuda.graph(self.graph, stream=stream):
+                self._frame()
+
+    def _frame(self):
+        x, y = self.a, self.b
+        self.solver.refresh_tangent(x.particle_q)
+        for _ in range(self.substeps):
+            self.solver.step(x, y, None, None, self.dt)
+            x, y = y, x
+        if self.substeps % 2:  # keep the frame's result in state a
+            self.a.particle_q.copy_(x.particle_q)
+            self.a.particle_qd.copy_(x.particle_qd)
+
+    def reset(self):
+        import torch
+
+        with torch.cuda.stream(self.stream):
+            self.a.particle_q.copy_(self.q0)
+            self.a.particle_qd.copy_(self.v0)
+            self.solver.reset()
+        torch.cuda.synchronize()
+
+    def run(self, steps, warmup, clocks=None):
+        """Returns (ms per frame, mean CG iterations per substep over the timed frames)."""
+        import torch
+
+        self.reset()
+        for _ in range(max(3, warmup)):
+            self.graph.replay()
+        self.reset()
+        it0 = self.solver.stats()["total_iterations"]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if clocks is not None:
+            clocks.start()
+        with torch.cuda.stream(self.stream):
+            e0.record(self.stream)
+            for _ in range(steps):
+                self.graph.replay()
+            e1.record(self.stream)
+        torch.cuda.synchronize()
+        clk = clocks.stop() if clocks is not None else None
+        iters = (self.solver.stats()["total_iterations"] - it0) / (steps * self.substeps)
+        return e0.elapsed_time(e1) / steps, iters, clk
+
+
 def tet_measurement(device: str, steps: int, warmup: int) -> dict:
-    """Jittered Tet4 48^3 block (663,552 tets, 795,024 edge springs, ground): frames as captured graphs."""
+    """Jittered Tet4 48^3 block (663,552 tets, 795,024 edge springs, ground): frames 0..K-1 from the
+    drop as captured graphs (the block lands on the ground at about frame 12)."""
     import torch
 
     from newton_solver_fem_gb300 import SolverFEM, model_from_arrays, scenes
@@ -338,40 +421,17 @@ def tet_measurement(device: str, steps: int, warmup: int) -> dict:
                        linear_solver_maxiter=sc.maxiter, linear_solver_tolerance=sc.tolerance, self_contact_ke=0.0,
                        ground_plane=sc.ground_plane, ground_ke=ke, ground_kd=kd, ground_kf=kf, ground_mu=mu)
     P = model.particle_count
-    a, b = model.state(), model.state()
-    stream = torch.cuda.Stream(device)
-
-    def frame():
-        x, y = a, b
-        solver.refresh_tangent(x.particle_q)
-        for _ in range(sc.substeps):
-            solver.step(x, y, None, None, sc.dt)
-            x, y = y, x
-
-    with torch.cuda.stream(stream):
-        frame()
-    torch.cuda.synchronize()
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.stream(stream):
-        with torch.cuda.graph(graph, stream=stream):
-            frame()
-    for _ in range(max(3, warmup)):
-        graph.replay()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        for _ in range(steps):
-            graph.replay()
-        e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    st = solver.stats()
-    del graph
+    window = FrameWindow(solver, model, sc.substeps, sc.dt, torch.cuda.Stream(device))
+    ms, iters, _ = window.run(steps, warmup)
+    finite = bool(torch.isfinite(window.a.particle_q).all())
+    shape = launch_shape(solver)
+    del window
     return {"workload": "tet4_jittered_48^3 (117,649 nodes, 663,552 tets, 795,024 springs, ground), "
-                        "10 substeps/frame, 50 CG at tol 1e-2",
+                        f"10 substeps/frame, 50 CG at tol 1e-2, frames 0..{steps - 1} from the drop",
             "ms_per_frame": ms, "value": 3 * P * sc.substeps / (ms / 1e3), "unit": UNIT,
-            "cg_iterations_last_substep": st["max_iterations"], "finite": bool(torch.isfinite(a.particle_q).all())}
+            "mean_cg_iterations": iters, "cg_iterations_timed": iters * steps * sc.substeps,
+            "launch": shape, "l2_resident_matrix_bytes": 40 * solver.matrix_info()["stored_blocks"]
+            if shape["l2_resident_slices"] else 0, "finite": finite}
 
 
 def adjoint_measurement(device: str, repeats: int) -> dict:
@@ -583,11 +643,23 @@ def run_gb300(args) -> None:
     with torch.cuda.stream(stream):
         with torch.cuda.graph(graph, stream=stream):
             frame(s0, s1)
+    q_init, v_init = model.particle_q.clone(), model.particle_qd.clone()
+
+    def reset_state():
+        """Frames 0..K-1 from the workload's initial state, whatever the warm-up count."""
+        with torch.cuda.stream(stream):
+            s0.particle_q.copy_(q_init)
+            s0.particle_qd.copy_(v_init)
+            solver.reset()
+        torch.cuda.synchronize()
+
+    reset_state()
     for _ in range(max(3, args.warmup)):
         graph.replay()
-    torch.cuda.synchronize()
+    reset_state()
     if world > 1:
         torch.distributed.barrier()
+    it_timed0 = solver.stats()["total_iterations"]
     clocks = ClockSampler(local)
     clocks.start()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -599,12 +671,14 @@ def run_gb300(args) -> None:
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = start.elapsed_time(end) / args.steps
+    timed_iterations = (solver.stats()["total_iterations"] - it_timed0) / (args.steps * substeps)
     from newton_solver_fem_gb300.replicas import max_over_ranks
 
     ms = max_over_ranks(ms, device)  # replicas: the slowest rank sets the job time
     value = world * 3 * P * substeps / (ms / 1e3)
 
-    # ---- roofline of the dominant kernel: eager frames with per-launch CUDA events
+    # ---- roofline of the dominant kernel: eager frames (0..2 from the initial state) with per-launch CUDA events
+    reset_state()
     stats0 = solver.stats()
     _lib.check(lib.fem_set_timing(solver._handle, 1))
     with torch.cuda.stream(stream):
@@ -637,9 +711,9 @@ def run_gb300(args) -> None:
     # ---- end to end through the public API with host buffers
     host_q = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
     host_v = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
-    host_q.copy_(s0.particle_q.cpu())
-    host_v.copy_(s0.particle_qd.cpu())
-    torch.cuda.synchronize()
+    host_q.copy_(q_init.cpu())  # frames 0..K-1 from the initial state, like the timed window
+    host_v.copy_(v_init.cpu())
+    reset_state()
     e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
@@ -674,7 +748,9 @@ def run_gb300(args) -> None:
             "config": {"workload": f"hex8_block_{args.cells}^3", "nodes": P, "hexes": int(model.fem.hex_count),
                        "dof": 3 * P, "substeps_per_step": substeps, "cg_tol": sc.tolerance,
                        "cg_maxiter": sc.maxiter, "preconditioner": "block_diag", "parallelism": "replicas",
-                       "nnzb": info["nnzb"], "mean_cg_iterations": iters,
+                       "nnzb": info["nnzb"], "mean_cg_iterations": timed_iterations,
+                       "frames": f"0..{args.steps - 1} from the initial state (reset after warm-up)",
+                       "launch": launch_shape(solver),
                        "pcg_split": "rows split over CTAs by calibrated SpMV speed (FEM_TUNE_BALANCE=1)",
                        "column_mode": int(cc.value), "column_index_bytes": round(col_bytes, 4),
                        "l2": "inputs larger than L2 (A values 259 MB, element blocks 614 MB at 64^3)"},
