@@ -205,6 +205,13 @@ int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);
 int fem_reset(FemHandle* handle, void* stream);
 float* fem_velocity_increment_ptr(FemHandle* handle);
+/* Largest final relative residual ||r|| / ||b|| of the handle's solves since
+ * the last reset: residuals[0] over step-mode solves (fem_step, rollouts),
+ * residuals[1] over solve-mode solves (fem_solve, adjoint solves); a
+ * non-finite residual reads 1e30.  Synchronises the stream; reset != 0 clears
+ * both.  Backs SolverFEM.check() of the differentiable mode (the reference's
+ * differentiation.check, differentiation.py:263-272, with its deferred checks). */
+int fem_get_solve_residuals(FemHandle* handle, float* residuals, int32_t reset, void* stream);
 int fem_get_stats(FemHandle* handle, FemStats* stats, int32_t* scene_iterations, void* stream);
 
 /* Measurement support: when enabled, every eager (not graph-captured)
@@ -276,6 +283,53 @@ int fem_force_vjp(FemHandle* handle, const float* q, const float* v, const float
 /* Accumulate the predictor's VJP into v_bar: -(A rhs_bar)_k + (sum_j A_kj)^T rhs_bar_k
  * plus the spring-damping term (implicit_predictor.py:9-41). */
 int fem_predictor_vjp(FemHandle* handle, const float* rhs_bar, float dt, float* v_bar, void* stream);
+/* fem_force_vjp plus the gradient wrt each element's raw material row (the
+ * force kernels' inputs, kernels.py:541-581 for Tet4 and 1481-1601 for Hex8):
+ * tet_material_bar [T,3] and hex_material_bar [H,3] receive dL/d(mu, lambda,
+ * k_d); either may be NULL.  Beyond the reference, whose differentiable mode
+ * holds materials fixed (differentiation.py:254-276); the matrix stays fixed
+ * at its assembly materials, as for every differentiable input. */
+int fem_force_vjp_materials(FemHandle* handle, const float* q, const float* v, const float* activations,
+                            const float* gravity, const float* force_bar, float* q_bar, float* v_bar,
+                            float* activation_bar, float* mu_scale_bar, float* tet_material_bar,
+                            float* hex_material_bar, void* stream);
+
+/* Device-side differentiable rollouts over the fixed matrix: whole segments of
+ * substeps enqueued from C++ on one stream, with no host synchronisation, in
+ * place of the reference's taped per-substep Python (differentiation.step,
+ * differentiation.py:287-394, driven per substep by the bear-training loop's
+ * frame checkpoints, examples/diffsim/_bear_training.py:239-310).
+ *
+ * fem_rollout_segment: `substeps` differentiable substeps from (q0, v0),
+ * writing the states before and after every substep into q_states / v_states
+ * ([substeps+1, P, 3]; q0 / v0 may already be slot 0).  Each substep is
+ * SolverFEM.step on the fixed matrix at (tolerance, maxiter).  warm_start 0:
+ * every solve starts from zero (the reference's checked solves); 1: the first
+ * from dv0 (NULL = zero), the rest from the previous increment, and the last
+ * increment goes to dv_out (optional).  refresh != 0 first assembles the
+ * tangent at q0, so a segment can be one frame of a frame loop.
+ *
+ * fem_adjoint_segment: the reverse pass over such a segment.  q_bar, v_bar
+ * [P,3] hold dL/d(state after the last substep) on entry and dL/d(state
+ * before the first) on return.  Per substep, in reverse: the adjoint solve
+ * with the same symmetric matrix, the predictor VJP and the force VJP.
+ * Accumulated (+=) when given: ext_bar [P,3] (a load held over the segment),
+ * activation_bar / mu_scale_bar [T], tet_material_bar [T,3], hex_material_bar
+ * [H,3].  adjoint_start [P,3] (optional) is the warm start of each adjoint solve
+ * and receives its solution (NULL = every adjoint solve from zero).  refresh
+ * != 0 first assembles the tangent at q_states[0] (the matrix the segment's
+ * forward used when it was rolled out with refresh).  dt must equal the
+ * assembled timestep.  The first call allocates scratch: call once before
+ * capturing either function in a CUDA graph. */
+int fem_rollout_segment(FemHandle* handle, const float* q0, const float* v0, const float* dv0, int32_t substeps,
+                        const float* external_forces, const float* activations, const float* gravity, float dt,
+                        float tolerance, int32_t maxiter, int32_t warm_start, int32_t refresh, float* q_states,
+                        float* v_states, float* dv_out, void* stream);
+int fem_adjoint_segment(FemHandle* handle, float* q_states, float* v_states, int32_t substeps,
+                        const float* external_forces, const float* activations, const float* gravity, float dt,
+                        float tolerance, int32_t maxiter, int32_t refresh, float* adjoint_start, float* q_bar,
+                        float* v_bar, float* ext_bar, float* activation_bar, float* mu_scale_bar,
+                        float* tet_material_bar, float* hex_material_bar, void* stream);
 
 /* Rebuild the constant matrix, the sparsity pattern, the slot map and the
  * preconditioner after in-place edits of tet connectivity, poses, materials

@@ -154,6 +154,7 @@ SIGNATURES = [
     ("fem_get_tuning", _i32, [_p, _i32, ctypes.POINTER(ctypes.c_int64)]),
     ("fem_reset", _i32, [_p, _p]),
     ("fem_velocity_increment_ptr", _p, [_p]),
+    ("fem_get_solve_residuals", _i32, [_p, _p, _i32, _p]),
     ("fem_get_stats", _i32, [_p, ctypes.POINTER(FemStats), _p, _p]),
     ("fem_set_soft_contacts", _i32, [_p, _p, _p, _p, _p, _p, _i32]),
     ("fem_set_surface_contacts", _i32, [_p, _i32, _p, _p, _p, _p, _f, _f, _p, _p]),
@@ -170,6 +171,10 @@ SIGNATURES = [
     ("fem_solve", _i32, [_p, _p, _p, _f, _i32, _p]),
     ("fem_force_vjp", _i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     ("fem_predictor_vjp", _i32, [_p, _p, _f, _p, _p]),
+    ("fem_force_vjp_materials", _i32, [_p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),
+    ("fem_rollout_segment", _i32, [_p, _p, _p, _p, _i32, _p, _p, _p, _f, _f, _i32, _i32, _i32, _p, _p, _p, _p]),
+    ("fem_adjoint_segment", _i32, [_p, _p, _p, _i32, _p, _p, _p, _f, _f, _i32, _i32, _p, _p, _p, _p, _p, _p, _p,
+                                   _p, _p]),
     ("fem_prepare_tet_updates", _i32, [_p, ctypes.POINTER(FemDesc), _i32, _p]),
     ("fem_update_tet_topology", _i32, [_p, ctypes.POINTER(FemDesc), _p, _f, _p, ctypes.POINTER(FemTopologyUpdate),
                                         _p]),

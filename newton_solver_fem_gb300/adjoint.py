@@ -56,6 +56,7 @@ class DifferentiableSolver:
             self.fixed[torch.as_tensor(solver.fixed_particle_indices, device=self.device, dtype=torch.long)] = True
         self._scale = None
         self.last_iterations = []
+        self.after_backward_solve = None  # hook run after every adjoint solve (SolverFEM's residual check)
 
     def _stream(self) -> int:
         return torch.cuda.current_stream(self.device).cuda_stream
@@ -141,6 +142,8 @@ class _Substep(torch.autograd.Function):
         vb[diff.fixed] = 0.0
         vt = vb + dt * qb
         rhs_bar = diff.solve(vt)
+        if diff.after_backward_solve is not None:
+            diff.after_backward_solve()
         v_bar = vt.clone()
         _lib.check(lib.fem_predictor_vjp(handle, rhs_bar.data_ptr(), dt, v_bar.data_ptr(), stream))
         q_bar = qb
@@ -200,3 +203,205 @@ def checkpointed_gradient(step, q0, v0, steps: int, every: int, loss_fn, params=
             if gp is not None:
                 grads[i] += gp
     return loss.detach(), qb, vb, grads
+
+
+class DeviceRollout:
+    """Checkpointed differentiable rollouts run segment by segment on the device.
+
+    The forward pass and the reverse pass are whole segments of substeps enqueued
+    by the library (``fem_rollout_segment``, ``fem_adjoint_segment``) on the
+    current stream, with no per-substep Python and no host synchronisation; a
+    full-length segment's recomputation and reverse pass are replayed from one
+    captured CUDA graph.  The contract is ``_Substep``'s: the matrix is held
+    fixed within a segment, every forward solve starts from zero unless
+    ``warm_start``, and the gradient is that of the linear solves.
+
+    Memory: with ``store_all`` every substep's state is kept (steps + 1 states,
+    no recomputation); otherwise only the checkpoint states every ``every``
+    substeps are kept and each segment is recomputed once in the reverse pass
+    (the reference's frame-checkpoint schedule, ``examples/diffsim/_bear_training.py:239-310``).
+    ``refresh`` assembles the tangent at the start of every segment (a segment is
+    then one frame of a frame loop), in the forward pass and again before the
+    segment's reverse pass.
+    """
+
+    def __init__(self, diff: DifferentiableSolver, steps: int, every: int, *, refresh: bool = False,
+                 warm_start: bool = False, warm_adjoint: bool = False, store_all: bool = False, graphs: bool = True):
+        if steps < 1 or every < 1:
+            raise ValueError("steps and every must be positive")
+        self.diff, self.steps, self.every = diff, int(steps), int(every)
+        self.refresh, self.warm_start, self.warm_adjoint = bool(refresh), bool(warm_start), bool(warm_adjoint)
+        self.store_all, self.graphs = bool(store_all), bool(graphs) and not store_all
+        s = diff.solver
+        P, dev = s.model.particle_count, s.device
+        self.P = P
+        self.bounds = [(k, min(k + self.every, self.steps)) for k in range(0, self.steps, self.every)]
+        n_states = self.steps + 1 if self.store_all else self.every + 1
+        self.q_states = torch.zeros((n_states, P, 3), dtype=torch.float32, device=dev)
+        self.v_states = torch.zeros_like(self.q_states)
+        nck = len(self.bounds) + 1
+        self.ck_q = None if self.store_all else torch.zeros((nck, P, 3), dtype=torch.float32, device=dev)
+        self.ck_v = None if self.store_all else torch.zeros_like(self.ck_q)
+        self.ck_dv = torch.zeros((nck, P, 3), dtype=torch.float32, device=dev) if self.warm_start else None
+        self.q_bar = torch.zeros((P, 3), dtype=torch.float32, device=dev)
+        self.v_bar = torch.zeros_like(self.q_bar)
+        self.adj_start = torch.zeros_like(self.q_bar) if self.warm_adjoint else None
+        self._graph = None
+        self._graph_key = None
+
+    # -- native calls ---------------------------------------------------------
+    def _rollout(self, q0, v0, dv0, n, q_states, v_states, dv_out, ext, act):
+        d, s = self.diff, self.diff.solver
+        _lib.check(d.lib.fem_rollout_segment(
+            s._handle, q0.data_ptr(), v0.data_ptr(), None if dv0 is None else dv0.data_ptr(), n,
+            None if ext is None else ext.data_ptr(), None if act is None else act.data_ptr(),
+            s.model.gravity.data_ptr(), s.dt, d.tolerance, d.maxiter, int(self.warm_start), int(self.refresh),
+            q_states.data_ptr(), v_states.data_ptr(), None if dv_out is None else dv_out.data_ptr(), d._stream()),
+            "rollout segment")
+
+    def _adjoint(self, q_states, v_states, n, refresh, ext, act, acc):
+        d, s = self.diff, self.diff.solver
+        ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        _lib.check(d.lib.fem_adjoint_segment(
+            s._handle, q_states.data_ptr(), v_states.data_ptr(), n, ptr(ext), ptr(act), s.model.gravity.data_ptr(),
+            s.dt, d.tolerance, d.maxiter, int(refresh), ptr(self.adj_start), self.q_bar.data_ptr(),
+            self.v_bar.data_ptr(), ptr(acc["ext"]), ptr(acc["act"]), ptr(acc["scale"]), ptr(acc["tet_mat"]),
+            ptr(acc["hex_mat"]), d._stream()), "adjoint segment")
+
+    # -- passes ----------------------------------------------------------------
+    def forward(self, q0, v0, *, external_forces=None, activations=None):
+        """Roll out from (q0, v0); returns the final state (q, v) (copies)."""
+        ext = None if external_forces is None else external_forces.detach().contiguous()
+        act = None if activations is None else activations.detach().contiguous()
+        q0, v0 = q0.detach().contiguous(), v0.detach().contiguous()
+        if self.ck_dv is not None:
+            self.ck_dv[0].zero_()
+        if self.store_all:
+            self.q_states[0].copy_(q0)
+            self.v_states[0].copy_(v0)
+            for i, (a, b) in enumerate(self.bounds):
+                dv0 = None if self.ck_dv is None else self.ck_dv[i]
+                dv1 = None if self.ck_dv is None else self.ck_dv[i + 1]
+                self._rollout(self.q_states[a], self.v_states[a], dv0, b - a, self.q_states[a:], self.v_states[a:],
+                              dv1, ext, act)
+            return self.q_states[self.steps].clone(), self.v_states[self.steps].clone()
+        self.ck_q[0].copy_(q0)
+        self.ck_v[0].copy_(v0)
+        for i, (a, b) in enumerate(self.bounds):
+            dv0 = None if self.ck_dv is None else self.ck_dv[i]
+            dv1 = None if self.ck_dv is None else self.ck_dv[i + 1]
+            self._rollout(self.ck_q[i], self.ck_v[i], dv0, b - a, self.q_states, self.v_states, dv1, ext, act)
+            self.ck_q[i + 1].copy_(self.q_states[b - a])
+            self.ck_v[i + 1].copy_(self.v_states[b - a])
+        return self.ck_q[-1].clone(), self.ck_v[-1].clone()
+
+    def _segment_reverse(self, i, ext, act, acc):
+        """Recompute segment i (unless every state is stored) and run its reverse pass."""
+        a, b = self.bounds[i]
+        n = b - a
+        if self.store_all:
+            self._adjoint(self.q_states[a:], self.v_states[a:], n, self.refresh, ext, act, acc)
+            return
+        dv0 = None if self.ck_dv is None else self.ck_dv[i]
+        self._rollout(self.q_states[0], self.v_states[0], dv0, n, self.q_states, self.v_states, None, ext, act)
+        self._adjoint(self.q_states, self.v_states, n, False, ext, act, acc)
+
+    def backward(self, q_bar, v_bar, *, external_forces=None, activations=None, mu_scale=None, materials=False):
+        """Reverse pass from the final-state gradients; returns a dict of input gradients."""
+        s = self.diff.solver
+        dev = s.device
+        ext = None if external_forces is None else external_forces.detach().contiguous()
+        act = None if activations is None else activations.detach().contiguous()
+        T, H = s.model.tet_count, s.hex_count
+        acc = {
+            "ext": torch.zeros((self.P, 3), dtype=torch.float32, device=dev) if ext is not None else None,
+            "act": torch.zeros(T, dtype=torch.float32, device=dev) if act is not None and T else None,
+            "scale": torch.zeros(T, dtype=torch.float32, device=dev) if mu_scale is not None and T else None,
+            "tet_mat": torch.zeros((T, 3), dtype=torch.float32, device=dev) if materials and T else None,
+            "hex_mat": torch.zeros((H, 3), dtype=torch.float32, device=dev) if materials and H else None,
+        }
+        self.q_bar.copy_(q_bar)
+        self.v_bar.copy_(v_bar)
+        if self.adj_start is not None:
+            self.adj_start.zero_()
+        key = (None if ext is None else ext.data_ptr(), None if act is None else act.data_ptr(),
+               tuple(None if t is None else t.data_ptr() for t in acc.values()))
+        for i in reversed(range(len(self.bounds))):
+            a, b = self.bounds[i]
+            full = (b - a) == self.every
+            if not self.store_all:
+                self.q_states[0].copy_(self.ck_q[i])
+                self.v_states[0].copy_(self.ck_v[i])
+            if self.graphs and full and (self.ck_dv is None or i > 0):
+                if self._graph is None or self._graph_key != (key, self.ck_dv is not None):
+                    self._capture(i, ext, act, acc)
+                    self._graph_key = (key, self.ck_dv is not None)
+                if self.ck_dv is not None:
+                    self._dv_in.copy_(self.ck_dv[i])
+                self._graph.replay()
+            else:
+                self._segment_reverse(i, ext, act, acc)
+        out = {"q0": self.q_bar.clone(), "v0": self.v_bar.clone()}
+        names = {"ext": "external_forces", "act": "activations", "scale": "mu_scale", "tet_mat": "tet_materials",
+                 "hex_mat": "hex_materials"}
+        for k, t in acc.items():
+            if t is not None:
+                out[names[k]] = t
+        return out
+
+    def _capture(self, i, ext, act, acc):
+        """Capture one full segment's recomputation + reverse pass (fixed buffers; the checkpoint is
+        copied into slot 0 of the state buffer before each replay)."""
+        stream = torch.cuda.Stream(self.diff.device)
+        stream.wait_stream(torch.cuda.current_stream(self.diff.device))
+        self._dv_in = torch.zeros((self.P, 3), dtype=torch.float32, device=self.diff.device) \
+            if self.ck_dv is not None else None
+        n = self.every
+        q_save, v_save = self.q_bar.clone(), self.v_bar.clone()
+        saved = {k: (None if t is None else t.clone()) for k, t in acc.items()}
+        adj_save = None if self.adj_start is None else self.adj_start.clone()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            with torch.cuda.graph(graph, stream=stream):
+                self._rollout(self.q_states[0], self.v_states[0], self._dv_in, n, self.q_states, self.v_states, None,
+                              ext, act)
+                self._adjoint(self.q_states, self.v_states, n, False, ext, act, acc)
+        torch.cuda.current_stream(self.diff.device).wait_stream(stream)
+        # capture does not run the work: restore nothing was changed, but keep the inputs intact regardless
+        self.q_bar.copy_(q_save)
+        self.v_bar.copy_(v_save)
+        for k, t in acc.items():
+            if t is not None:
+                t.copy_(saved[k])
+        if adj_save is not None:
+            self.adj_start.copy_(adj_save)
+        self._graph = graph
+
+
+def device_checkpointed_gradient(diff: DifferentiableSolver, q0, v0, steps: int, every: int, loss_fn, *,
+                                 external_forces=None, activations=None, mu_scale=None, materials=False,
+                                 refresh=False, warm_start=False, warm_adjoint=False, store_all=False, graphs=True,
+                                 rollout: DeviceRollout | None = None):
+    """Loss of a ``steps``-substep rollout and its gradients, computed on the device.
+
+    ``loss_fn(q, v)`` maps the final state to a scalar (differentiated by torch).
+    Returns (loss, grads) with grads keys ``q0``, ``v0`` and, when requested,
+    ``external_forces`` (a load held over the rollout), ``activations``,
+    ``mu_scale``, ``tet_materials``, ``hex_materials``.  Pass a ``DeviceRollout``
+    to reuse its buffers and captured graph across calls.
+    """
+    if mu_scale is not None:
+        diff.set_mu_scale(mu_scale)
+    ro = rollout or DeviceRollout(diff, steps, every, refresh=refresh, warm_start=warm_start,
+                                  warm_adjoint=warm_adjoint, store_all=store_all, graphs=graphs)
+    qf, vf = ro.forward(q0, v0, external_forces=external_forces, activations=activations)
+    qf.requires_grad_(True)
+    vf.requires_grad_(True)
+    with torch.enable_grad():
+        loss = loss_fn(qf, vf)
+        qb, vb = torch.autograd.grad(loss, (qf, vf), allow_unused=True)
+    qb = torch.zeros_like(qf) if qb is None else qb
+    vb = torch.zeros_like(vf) if vb is None else vb
+    grads = ro.backward(qb.detach(), vb.detach(), external_forces=external_forces, activations=activations,
+                        mu_scale=mu_scale, materials=materials)
+    return loss.detach(), grads

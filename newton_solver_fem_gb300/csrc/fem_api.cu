@@ -873,6 +873,7 @@ int fem::create_handle(const FemDesc* d, const std::vector<std::vector<int>>* ca
     h.status = b.alloc<int>(1);
     h.scene_stats = b.alloc<fem::SceneStats>(nscenes);
     h.cum_iters = b.alloc<long long>(nscenes);
+    h.resid_max = b.alloc<float>(2);
     if (b.status != FEM_OK) {
         int code = b.status;
         g_error = h.last_error;
@@ -1343,6 +1344,19 @@ int fem_reset(FemHandle* H, void* stream) {
 }
 
 float* fem_velocity_increment_ptr(FemHandle* H) { return H ? H->h.dv : nullptr; }
+int fem_get_solve_residuals(FemHandle* H, float* residuals, int32_t reset, void* stream) {
+    if (H == nullptr || residuals == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle or output");
+    Handle& h = H->h;
+    residuals[0] = residuals[1] = 0.0f;
+    if (h.P == 0) return FEM_OK;
+    DeviceGuard g(H->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t err = cudaStreamSynchronize(s);
+    if (err == cudaSuccess) err = cudaMemcpy(residuals, h.resid_max, 2 * sizeof(float), cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess && reset) err = cudaMemsetAsync(h.resid_max, 0, 2 * sizeof(float), s);
+    return cuda_status(err, &h);
+}
+
 
 int fem_get_stats(FemHandle* H, FemStats* stats, int32_t* scene_iterations, void* stream) {
     if (H == nullptr || stats == nullptr) return set_error(FEM_ERR_BAD_ARG, "null handle or stats");

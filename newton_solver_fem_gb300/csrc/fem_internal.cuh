@@ -101,6 +101,7 @@ struct PcgArgs {
     int* status;
     SceneStats* scene_stats;
     long long* cum_iters;  // [S] CG iterations summed over launches
+    float* resid_max;      // [2] running max of the final relative residual: [0] step mode, [1] solve mode
     int maxiter;
     float tol;
     float dt;
@@ -164,6 +165,9 @@ struct Handle {
     float* hex_mat = nullptr;   // [H*3]
     const float* mu_scale = nullptr;  // optional caller-owned per-tet shear scale [T]
     float4* elem_grad = nullptr;      // adjoint scratch [2 * (4T + 8H + 3Tri)], allocated on first VJP
+    float* roll_f = nullptr;          // rollout scratch [3P]: the substep right-hand side (first rollout call)
+    float* adj_vt = nullptr;          // adjoint scratch [3P]: the adjoint solve's right-hand side
+    float* adj_x = nullptr;           // adjoint scratch [3P]: the adjoint solution when the caller keeps none
     int* tri_idx = nullptr;     // [Tri*3]
     float4* tri_pose = nullptr; // [Tri] (Dm00, Dm01, Dm10, Dm11)
     float* tri_mat = nullptr;   // [Tri*5] (ke, ka, kd, drag, lift)
@@ -295,6 +299,7 @@ struct Handle {
     int* status = nullptr;
     SceneStats* scene_stats = nullptr;
     long long* cum_iters = nullptr;
+    float* resid_max = nullptr;  // [2] largest relative residual of step-mode / solve-mode solves since the last read
     // optional timing of PCG launches (eager launches only)
     bool timing = false;
     std::vector<cudaEvent_t> timing_events;  // start/end pairs

@@ -831,6 +831,10 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             o.converged = st.rr <= st.atol_sq;
             a.scene_stats[s] = o;
             a.cum_iters[s] += st.iters;
+            // running max of the relative residual (non-negative floats order like their bit patterns)
+            float rel = st.bb > 0.0 ? (float)sqrt(st.rr / st.bb) : 0.0f;
+            if (!isfinite(rel)) rel = 1.0e30f;
+            atomicMax(reinterpret_cast<int*>(a.resid_max + (a.solve_rhs != nullptr ? 1 : 0)), __float_as_int(rel));
         }
     }
 }
@@ -1014,6 +1018,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.status = h.status;
     a.scene_stats = h.scene_stats;
     a.cum_iters = h.cum_iters;
+    a.resid_max = h.resid_max;
     a.maxiter = maxiter >= 0 ? maxiter : h.maxiter;
     a.tol = tol > 0.0f ? tol : h.tol;
     a.dt = dt;

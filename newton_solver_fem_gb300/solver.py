@@ -171,8 +171,6 @@ class SolverFEM:
                 raise ValueError(f"spring_rest_direction shape {srd.shape} != (spring_count={model.spring_count}, 3)")
             self.spring_rest_direction = np.ascontiguousarray(srd, dtype=np.float32)
         self._torque = self.torque_stiffness > 0.0 and spring_rest_direction is not None and model.spring_count > 0
-        if differentiable:
-            raise NotImplementedError("use newton_solver_fem_gb300.adjoint for differentiable rollouts")
         if tet_volume_weights is not None:
             w = torch.as_tensor(tet_volume_weights)
             if tuple(w.shape) != (model.tet_count,) or not torch.isfinite(w).all() or (w < 0).any():
@@ -185,7 +183,10 @@ class SolverFEM:
         self.min_stretch = float(min_stretch)
         self.max_stretch = float(max_stretch)
         self.linear_damping = float(linear_damping)
-        self.differentiable = False
+        self.differentiable = bool(differentiable)
+        self.defer_differentiation_checks = bool(defer_differentiation_checks)
+        self.last_differentiation_residuals = None
+        self._diff = None
         self.enable_tet_activations = bool(enable_tet_activations)
         self.linear_solver_use_cuda_graph = bool(linear_solver_use_cuda_graph)
         self.linear_solver_check_every = 0
@@ -483,6 +484,8 @@ class SolverFEM:
         ``h*sum(f) - h^2 K v`` (projected); fixed nodes of ``state_in`` are
         restored in place, as in the reference.
         """
+        if self.differentiable:
+            return self._differentiable_step(state_in, state_out, control, contacts, dt, external_forces)
         P = self.model.particle_count
         dev = self.device
         ext = None
@@ -506,6 +509,89 @@ class SolverFEM:
         if self.linear_solver_check_every > 0:
             stats = self.stats()
             self.last_cg_iters = stats["max_iterations"]
+        return state_out
+
+    # ------------------------------------------------------------------ differentiable mode
+    # Reference differentiation.step (differentiation.py:287-394): the matrix is held fixed, every solve
+    # is a checked solve from zero at tolerance 1e-8 within linear_solver_maxiter, and the step is
+    # recorded on the tape -- here torch autograd: outputs are attached to state_out.
+    DIFF_RESIDUAL_BUDGET = 2.0e-5  # differentiation.py:162-166: residual <= 2e-5 ||b|| (+ 1e-10)
+
+    def _differentiation(self):
+        if self._diff is None:
+            if self._streaming is not None:
+                raise NotImplementedError("Differentiation requires fixed topology without streaming/component "
+                                          "scaling")
+            if self._soft_surface_contacts is not None or self.model.particle_ke > 0.0:
+                raise NotImplementedError("Differentiation supports analytic ground contact; disable "
+                                          "particle/surface contacts")
+            for name in ("particle_mass", "particle_inv_mass", "particle_radius", "tet_poses", "tet_materials",
+                         "tri_poses", "tri_materials", "spring_stiffness", "spring_damping", "spring_rest_length",
+                         "gravity"):
+                value = getattr(self.model, name, None)
+                if isinstance(value, torch.Tensor) and value.requires_grad:
+                    raise ValueError(f"{name} is fixed: finalize the model without gradients and enable "
+                                     f"state/control gradients")
+            if torch.cuda.is_current_stream_capturing():
+                raise RuntimeError("Call prepare_differentiation() before CUDA graph capture")
+            from .adjoint import DifferentiableSolver
+
+            self._diff = DifferentiableSolver(self, tolerance=1.0e-8, maxiter=self.linear_solver_maxiter)
+            self._diff.after_backward_solve = self._after_adjoint_solve
+        return self._diff
+
+    def prepare_differentiation(self):
+        """Set up the differentiable mode before capture (reference ``prepare``, differentiation.py:236-270)."""
+        return self._differentiation()
+
+    def _after_adjoint_solve(self):
+        if not self.defer_differentiation_checks:
+            self.check()
+
+    def check(self, *, reset: bool = True) -> dict:
+        """Largest forward / adjoint relative residuals since the last check; raises when either exceeds
+        the reference's budget (``differentiation.check``, differentiation.py:263-272)."""
+        if torch.cuda.is_current_stream_capturing():
+            raise RuntimeError("Check differentiable residuals after launching the CUDA graph")
+        out = (ctypes.c_float * 2)()
+        _lib.check(self._lib.fem_get_solve_residuals(self._handle, out, int(reset), self._stream()))
+        result = {"forward_relative_residual": float(out[0]), "backward_relative_residual": float(out[1])}
+        self.last_differentiation_residuals = result
+        if not all(math.isfinite(v) for v in result.values()) or \
+                max(result.values()) > self.DIFF_RESIDUAL_BUDGET:
+            raise RuntimeError(f"FEM differentiable linear solve did not converge: {result}")
+        return result
+
+    def _differentiable_step(self, state_in, state_out, control, contacts, dt, external_forces):
+        if float(dt) != self.dt:
+            raise ValueError("Differentiable dt must match the fixed matrix assembly timestep")
+        if contacts is not None:
+            raise NotImplementedError("Differentiation supports only the analytic ground contact law")
+        if state_in.particle_q is state_out.particle_q or state_in.particle_qd is state_out.particle_qd or \
+                state_in.particle_q.data_ptr() == state_out.particle_q.data_ptr() or \
+                state_in.particle_qd.data_ptr() == state_out.particle_qd.data_ptr():
+            raise ValueError("Use unique input/output states for every taped step")
+        P = self.model.particle_count
+        if external_forces is not None and (not isinstance(external_forces, torch.Tensor) or
+                                            tuple(external_forces.shape) != (P, 3) or
+                                            external_forces.device != self.device):
+            raise ValueError("external_forces must be a model-sized wp.vec3 array on the model device")
+        diff = self._differentiation()
+        act = None
+        if self.enable_tet_activations and self.model.tet_count:
+            act = control.tet_activations if control is not None else self.model.tet_activations
+        from .adjoint import _Substep
+
+        q_out, v_out = _Substep.apply(diff, state_in.particle_q, state_in.particle_qd, float(dt), external_forces,
+                                      act, None)
+        if torch.is_grad_enabled() and (q_out.requires_grad or v_out.requires_grad):
+            state_out.particle_q, state_out.particle_qd = q_out, v_out  # the taped outputs
+        else:
+            state_out.particle_q.copy_(q_out)
+            state_out.particle_qd.copy_(v_out)
+        self._stepped = True
+        if not self.defer_differentiation_checks:
+            self.check()
         return state_out
 
     def _register_contacts(self, contacts) -> None:
