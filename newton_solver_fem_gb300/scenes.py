@@ -289,15 +289,21 @@ def tet_beam(seed: int = 4) -> Scene:
 
 
 def batched_scenes(count: int = 256, seed: int = 5, cell: float = 0.05, dims=(4, 32)) -> Scene:
-    """``count`` independent meshes (half Tet4, half Hex8) with per-axis dims U{lo..hi}, one x=0 face fixed each."""
+    """``count`` independent meshes (half Tet4, half Hex8) with per-axis dims U{lo..hi}, one x=0 face fixed each.
+
+    Every mesh is built at the origin: the scenes do not interact, and the Hex8
+    deformation gradient sums absolute node positions times shape gradients
+    (kernels.py:1551-1560), so in float32 its error grows with the distance from
+    the origin over the cell size (a mesh 235 m out with 5 cm cells loses about
+    four digits of F).
+    """
     rng = np.random.default_rng(seed)
     xs, masses, tets, tmats, hexes, hmats, fixed, offsets = [], [], [], [], [], [], [], [0]
-    spacing = 0.0
     for s in range(count):
         nx, ny, nz = (int(v) for v in rng.integers(dims[0], dims[1] + 1, size=3))
         E = float(np.exp(rng.uniform(np.log(1.0e4), np.log(1.0e6))))
         nu = float(rng.uniform(0.3, 0.48))
-        origin = (spacing, 0.0, 0.0)
+        origin = (0.0, 0.0, 0.0)
         base = offsets[-1]
         if s % 2 == 0:
             x, el, mats, mass = tet_block(nx, ny, nz, cell, origin, E, nu, 1000.0)
@@ -307,11 +313,10 @@ def batched_scenes(count: int = 256, seed: int = 5, cell: float = 0.05, dims=(4,
             x, el, mats, mass = hex_block(nx, ny, nz, cell, origin, E, nu, 1000.0)
             hexes.append(el + base)
             hmats.append(mats)
-        fixed.append(np.nonzero(np.isclose(x[:, 0], spacing))[0].astype(np.int32) + base)
+        fixed.append(np.nonzero(np.isclose(x[:, 0], 0.0))[0].astype(np.int32) + base)
         xs.append(x)
         masses.append(mass)
         offsets.append(base + len(x))
-        spacing += (nx + 2) * cell
     cat = lambda parts, shape, dtype: np.concatenate(parts).astype(dtype) if parts else np.zeros(shape, dtype)  # noqa: E731
     return Scene(
         f"batched_{count}_scenes",
