@@ -209,12 +209,12 @@ class DeviceRollout:
     """Checkpointed differentiable rollouts run segment by segment on the device.
 
     The forward pass and the reverse pass are whole segments of substeps enqueued
-    by the library (``fem_rollout_segment``, ``fem_adjoint_segment``) on the
-    current stream, with no per-substep Python and no host synchronisation; a
-    full-length segment's recomputation and reverse pass are replayed from one
-    captured CUDA graph.  The contract is ``_Substep``'s: the matrix is held
-    fixed within a segment, every forward solve starts from zero unless
-    ``warm_start``, and the gradient is that of the linear solves.
+    by the library (``fem_rollout_segment``, ``fem_adjoint_segment``) on a
+    stream, with no per-substep Python and no host synchronisation; full-length
+    segments are replayed from captured CUDA graphs.  The contract is
+    ``_Substep``'s: the matrix is held fixed within a segment, every forward
+    solve starts from zero unless ``warm_start``, and the gradient is that of the
+    linear solves.
 
     Memory: with ``store_all`` every substep's state is kept (steps + 1 states,
     no recomputation); otherwise only the checkpoint states every ``every``
@@ -223,22 +223,41 @@ class DeviceRollout:
     ``refresh`` assembles the tangent at the start of every segment (a segment is
     then one frame of a frame loop), in the forward pass and again before the
     segment's reverse pass.
+
+    ``overlap``: a ``DifferentiableSolver`` over a second handle with the same
+    model and the same assembled matrix.  The reverse pass then recomputes
+    segment i-1 on that handle, on its own stream, while segment i's reverse
+    pass runs on the first (two state buffers alternate).  A small mesh leaves
+    most SMs idle, so the recomputation comes almost for free; the two
+    cooperative PCG grids together must fit on the device, which is checked.
     """
 
     def __init__(self, diff: DifferentiableSolver, steps: int, every: int, *, refresh: bool = False,
-                 warm_start: bool = False, warm_adjoint: bool = False, store_all: bool = False, graphs: bool = True):
+                 warm_start: bool = False, warm_adjoint: bool = False, store_all: bool = False, graphs: bool = True,
+                 overlap: DifferentiableSolver | None = None):
         if steps < 1 or every < 1:
             raise ValueError("steps and every must be positive")
         self.diff, self.steps, self.every = diff, int(steps), int(every)
         self.refresh, self.warm_start, self.warm_adjoint = bool(refresh), bool(warm_start), bool(warm_adjoint)
         self.store_all, self.graphs = bool(store_all), bool(graphs) and not store_all
+        self.overlap = None if store_all else overlap
+        if self.overlap is not None:
+            if self.overlap.solver is diff.solver or self.overlap.model.particle_count != diff.model.particle_count:
+                raise ValueError("overlap needs a second solver over the same model")
+            if (self.overlap.tolerance, self.overlap.maxiter, self.overlap.solver.dt) != \
+                    (diff.tolerance, diff.maxiter, diff.solver.dt):
+                raise ValueError("overlap needs the same tolerance, iteration cap and timestep")
+            if not self.overlap_fits():
+                self.overlap = None  # the two PCG grids would not be co-resident: recompute in line
         s = diff.solver
         P, dev = s.model.particle_count, s.device
-        self.P = P
+        self.P, self.device = P, dev
         self.bounds = [(k, min(k + self.every, self.steps)) for k in range(0, self.steps, self.every)]
+        nbuf = 2 if self.overlap is not None else 1
         n_states = self.steps + 1 if self.store_all else self.every + 1
-        self.q_states = torch.zeros((n_states, P, 3), dtype=torch.float32, device=dev)
-        self.v_states = torch.zeros_like(self.q_states)
+        self.q_states = [torch.zeros((n_states, P, 3), dtype=torch.float32, device=dev) for _ in range(nbuf)]
+        self.v_states = [torch.zeros_like(t) for t in self.q_states]
+        self.dv_in = [torch.zeros((P, 3), dtype=torch.float32, device=dev) for _ in range(nbuf)]
         nck = len(self.bounds) + 1
         self.ck_q = None if self.store_all else torch.zeros((nck, P, 3), dtype=torch.float32, device=dev)
         self.ck_v = None if self.store_all else torch.zeros_like(self.ck_q)
@@ -246,12 +265,23 @@ class DeviceRollout:
         self.q_bar = torch.zeros((P, 3), dtype=torch.float32, device=dev)
         self.v_bar = torch.zeros_like(self.q_bar)
         self.adj_start = torch.zeros_like(self.q_bar) if self.warm_adjoint else None
-        self._graph = None
-        self._graph_key = None
+        self._graphs = {}
+        self._primed = False
+
+    def overlap_fits(self) -> bool:
+        """Both handles' cooperative PCG grids fit on the device side by side (one CTA per SM each at most)."""
+        lib = self.diff.lib
+        total = 0
+        for d in (self.diff, self.overlap):
+            v = ctypes.c_int64()
+            _lib.check(lib.fem_get_tuning(d.solver._handle, _lib.FEM_TUNE_GRID, ctypes.byref(v)))
+            total += int(v.value)
+        sms = torch.cuda.get_device_properties(self.diff.device).multi_processor_count
+        return total <= sms
 
     # -- native calls ---------------------------------------------------------
-    def _rollout(self, q0, v0, dv0, n, q_states, v_states, dv_out, ext, act):
-        d, s = self.diff, self.diff.solver
+    def _rollout(self, d, q0, v0, dv0, n, q_states, v_states, dv_out, ext, act):
+        s = d.solver
         _lib.check(d.lib.fem_rollout_segment(
             s._handle, q0.data_ptr(), v0.data_ptr(), None if dv0 is None else dv0.data_ptr(), n,
             None if ext is None else ext.data_ptr(), None if act is None else act.data_ptr(),
@@ -268,43 +298,113 @@ class DeviceRollout:
             self.v_bar.data_ptr(), ptr(acc["ext"]), ptr(acc["act"]), ptr(acc["scale"]), ptr(acc["tet_mat"]),
             ptr(acc["hex_mat"]), d._stream()), "adjoint segment")
 
+    def _prime(self, ext, act, acc):
+        """First calls allocate the handles' rollout and adjoint scratch: make them outside any capture."""
+        if self._primed:
+            return
+        for d in (self.diff, self.overlap):
+            if d is None:
+                continue
+            if d is self.overlap and self.diff._scale is not None:
+                d.set_mu_scale(self.diff._scale)
+            _lib.check(d.lib.fem_rollout_segment(
+                d.solver._handle, self.q_states[0].data_ptr(), self.v_states[0].data_ptr(), None, 0, None, None, None,
+                d.solver.dt, d.tolerance, d.maxiter, 0, 0, self.q_states[0].data_ptr(), self.v_states[0].data_ptr(),
+                None, d._stream()), "rollout segment")
+        self._primed = True
+
+    def _replay(self, key, stream, build):
+        """Replay the graph `key` on `stream`, capturing it from `build()` on first use.  A graph holds
+        the pointers it was captured with, so the key carries the control and shear-scale pointers."""
+        key = key + (None if self.diff._scale is None else self.diff._scale.data_ptr(),)
+        g = self._graphs.get(key)
+        if g is None:
+            cap = torch.cuda.Stream(self.device)
+            cap.wait_stream(stream)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(cap):
+                with torch.cuda.graph(g, stream=cap):
+                    build()
+            stream.wait_stream(cap)
+            self._graphs[key] = g
+        with torch.cuda.stream(stream):
+            g.replay()
+
+    @staticmethod
+    def _ptrs(*tensors):
+        return tuple(None if t is None else t.data_ptr() for t in tensors)
+
     # -- passes ----------------------------------------------------------------
     def forward(self, q0, v0, *, external_forces=None, activations=None):
         """Roll out from (q0, v0); returns the final state (q, v) (copies)."""
         ext = None if external_forces is None else external_forces.detach().contiguous()
         act = None if activations is None else activations.detach().contiguous()
         q0, v0 = q0.detach().contiguous(), v0.detach().contiguous()
+        self._prime(ext, act, None)
+        d = self.diff
         if self.ck_dv is not None:
             self.ck_dv[0].zero_()
+        qs, vs = self.q_states[0], self.v_states[0]
         if self.store_all:
-            self.q_states[0].copy_(q0)
-            self.v_states[0].copy_(v0)
+            qs[0].copy_(q0)
+            vs[0].copy_(v0)
             for i, (a, b) in enumerate(self.bounds):
                 dv0 = None if self.ck_dv is None else self.ck_dv[i]
                 dv1 = None if self.ck_dv is None else self.ck_dv[i + 1]
-                self._rollout(self.q_states[a], self.v_states[a], dv0, b - a, self.q_states[a:], self.v_states[a:],
-                              dv1, ext, act)
-            return self.q_states[self.steps].clone(), self.v_states[self.steps].clone()
+                self._rollout(d, qs[a], vs[a], dv0, b - a, qs[a:], vs[a:], dv1, ext, act)
+            return qs[self.steps].clone(), vs[self.steps].clone()
         self.ck_q[0].copy_(q0)
         self.ck_v[0].copy_(v0)
+        stream = torch.cuda.current_stream(self.device)
         for i, (a, b) in enumerate(self.bounds):
-            dv0 = None if self.ck_dv is None else self.ck_dv[i]
-            dv1 = None if self.ck_dv is None else self.ck_dv[i + 1]
-            self._rollout(self.ck_q[i], self.ck_v[i], dv0, b - a, self.q_states, self.v_states, dv1, ext, act)
-            self.ck_q[i + 1].copy_(self.q_states[b - a])
-            self.ck_v[i + 1].copy_(self.v_states[b - a])
+            n = b - a
+            qs[0].copy_(self.ck_q[i])
+            vs[0].copy_(self.ck_v[i])
+            if self.ck_dv is not None:
+                self.dv_in[0].copy_(self.ck_dv[i])
+            dv_in = None if self.ck_dv is None else self.dv_in[0]
+            if self.graphs and n == self.every:
+                self._replay(("fwd", self._ptrs(ext, act)), stream,
+                             lambda: self._rollout(d, qs[0], vs[0], dv_in, n, qs, vs, dv_in, ext, act))
+            else:
+                self._rollout(d, qs[0], vs[0], dv_in, n, qs, vs, dv_in, ext, act)
+            self.ck_q[i + 1].copy_(qs[n])
+            self.ck_v[i + 1].copy_(vs[n])
+            if self.ck_dv is not None:
+                self.ck_dv[i + 1].copy_(self.dv_in[0])
         return self.ck_q[-1].clone(), self.ck_v[-1].clone()
 
-    def _segment_reverse(self, i, ext, act, acc):
-        """Recompute segment i (unless every state is stored) and run its reverse pass."""
+    def _recompute(self, i, buf, stream, ext, act):
+        """Segment i's states into buffer `buf`, on the recomputing handle and `stream`."""
         a, b = self.bounds[i]
         n = b - a
-        if self.store_all:
-            self._adjoint(self.q_states[a:], self.v_states[a:], n, self.refresh, ext, act, acc)
-            return
-        dv0 = None if self.ck_dv is None else self.ck_dv[i]
-        self._rollout(self.q_states[0], self.v_states[0], dv0, n, self.q_states, self.v_states, None, ext, act)
-        self._adjoint(self.q_states, self.v_states, n, False, ext, act, acc)
+        d = self.overlap if self.overlap is not None else self.diff
+        qs, vs, dv = self.q_states[buf], self.v_states[buf], self.dv_in[buf]
+        with torch.cuda.stream(stream):
+            qs[0].copy_(self.ck_q[i])
+            vs[0].copy_(self.ck_v[i])
+            if self.ck_dv is not None:
+                dv.copy_(self.ck_dv[i])
+        dv_in = None if self.ck_dv is None else dv
+        if self.graphs and n == self.every:
+            self._replay(("rec", buf, self._ptrs(ext, act)), stream,
+                         lambda: self._rollout(d, qs[0], vs[0], dv_in, n, qs, vs, None, ext, act))
+        else:
+            with torch.cuda.stream(stream):
+                self._rollout(d, qs[0], vs[0], dv_in, n, qs, vs, None, ext, act)
+
+    def _reverse(self, i, buf, stream, ext, act, acc, key):
+        """Segment i's reverse pass over buffer `buf` on the first handle and `stream`."""
+        a, b = self.bounds[i]
+        n = b - a
+        qs, vs = self.q_states[buf], self.v_states[buf]
+        # the matrix: refreshed by an in-line recomputation on this handle, else refreshed here
+        refresh = self.refresh and self.overlap is not None
+        if self.graphs and n == self.every:
+            self._replay(("adj", buf, key), stream, lambda: self._adjoint(qs, vs, n, refresh, ext, act, acc))
+        else:
+            with torch.cuda.stream(stream):
+                self._adjoint(qs, vs, n, refresh, ext, act, acc)
 
     def backward(self, q_bar, v_bar, *, external_forces=None, activations=None, mu_scale=None, materials=False):
         """Reverse pass from the final-state gradients; returns a dict of input gradients."""
@@ -320,27 +420,54 @@ class DeviceRollout:
             "tet_mat": torch.zeros((T, 3), dtype=torch.float32, device=dev) if materials and T else None,
             "hex_mat": torch.zeros((H, 3), dtype=torch.float32, device=dev) if materials and H else None,
         }
+        self._prime(ext, act, acc)
+        if self.overlap is not None and self.diff._scale is not None:
+            self.overlap.set_mu_scale(self.diff._scale)
         self.q_bar.copy_(q_bar)
         self.v_bar.copy_(v_bar)
         if self.adj_start is not None:
             self.adj_start.zero_()
+        # captured graphs bake in the accumulator pointers: one set of graphs per pointer set
         key = (None if ext is None else ext.data_ptr(), None if act is None else act.data_ptr(),
                tuple(None if t is None else t.data_ptr() for t in acc.values()))
-        for i in reversed(range(len(self.bounds))):
-            a, b = self.bounds[i]
-            full = (b - a) == self.every
-            if not self.store_all:
-                self.q_states[0].copy_(self.ck_q[i])
-                self.v_states[0].copy_(self.ck_v[i])
-            if self.graphs and full and (self.ck_dv is None or i > 0):
-                if self._graph is None or self._graph_key != (key, self.ck_dv is not None):
-                    self._capture(i, ext, act, acc)
-                    self._graph_key = (key, self.ck_dv is not None)
-                if self.ck_dv is not None:
-                    self._dv_in.copy_(self.ck_dv[i])
-                self._graph.replay()
-            else:
-                self._segment_reverse(i, ext, act, acc)
+        main = torch.cuda.current_stream(dev)
+        nseg = len(self.bounds)
+        if self.store_all:
+            for i in reversed(range(nseg)):
+                a, b = self.bounds[i]
+                self._adjoint(self.q_states[0][a:], self.v_states[0][a:], b - a, self.refresh, ext, act, acc)
+        elif self.overlap is None:
+            for i in reversed(range(nseg)):
+                self._recompute(i, 0, main, ext, act)
+                self._reverse(i, 0, main, ext, act, acc, key)
+        else:
+            rec = torch.cuda.Stream(dev)
+            adj = torch.cuda.Stream(dev)
+            rec.wait_stream(main)
+            adj.wait_stream(main)
+            done_rec = [torch.cuda.Event(), torch.cuda.Event()]
+            done_adj = [torch.cuda.Event(), torch.cuda.Event()]
+            used = [False, False]
+            self._recompute(nseg - 1, (nseg - 1) % 2, rec, ext, act)
+            done_rec[(nseg - 1) % 2].record(rec)
+            for i in reversed(range(nseg)):
+                buf = i % 2
+                if i > 0:  # recompute the previous segment while this one runs its reverse pass
+                    nb = (i - 1) % 2
+                    if used[nb]:
+                        rec.wait_event(done_adj[nb])
+                    self._recompute(i - 1, nb, rec, ext, act)
+                    done_rec[nb].record(rec)
+                adj.wait_event(done_rec[buf])
+                self._reverse(i, buf, adj, ext, act, acc, key)
+                done_adj[buf].record(adj)
+                used[buf] = True
+            main.wait_stream(adj)
+            main.wait_stream(rec)
+            for t in list(self.q_states) + list(self.v_states) + list(self.dv_in) + \
+                    [self.q_bar, self.v_bar] + [t for t in acc.values() if t is not None]:
+                t.record_stream(adj)
+                t.record_stream(rec)
         out = {"q0": self.q_bar.clone(), "v0": self.v_bar.clone()}
         names = {"ext": "external_forces", "act": "activations", "scale": "mu_scale", "tet_mat": "tet_materials",
                  "hex_mat": "hex_materials"}
@@ -349,51 +476,25 @@ class DeviceRollout:
                 out[names[k]] = t
         return out
 
-    def _capture(self, i, ext, act, acc):
-        """Capture one full segment's recomputation + reverse pass (fixed buffers; the checkpoint is
-        copied into slot 0 of the state buffer before each replay)."""
-        stream = torch.cuda.Stream(self.diff.device)
-        stream.wait_stream(torch.cuda.current_stream(self.diff.device))
-        self._dv_in = torch.zeros((self.P, 3), dtype=torch.float32, device=self.diff.device) \
-            if self.ck_dv is not None else None
-        n = self.every
-        q_save, v_save = self.q_bar.clone(), self.v_bar.clone()
-        saved = {k: (None if t is None else t.clone()) for k, t in acc.items()}
-        adj_save = None if self.adj_start is None else self.adj_start.clone()
-        graph = torch.cuda.CUDAGraph()
-        with torch.cuda.stream(stream):
-            with torch.cuda.graph(graph, stream=stream):
-                self._rollout(self.q_states[0], self.v_states[0], self._dv_in, n, self.q_states, self.v_states, None,
-                              ext, act)
-                self._adjoint(self.q_states, self.v_states, n, False, ext, act, acc)
-        torch.cuda.current_stream(self.diff.device).wait_stream(stream)
-        # capture does not run the work: restore nothing was changed, but keep the inputs intact regardless
-        self.q_bar.copy_(q_save)
-        self.v_bar.copy_(v_save)
-        for k, t in acc.items():
-            if t is not None:
-                t.copy_(saved[k])
-        if adj_save is not None:
-            self.adj_start.copy_(adj_save)
-        self._graph = graph
-
 
 def device_checkpointed_gradient(diff: DifferentiableSolver, q0, v0, steps: int, every: int, loss_fn, *,
                                  external_forces=None, activations=None, mu_scale=None, materials=False,
                                  refresh=False, warm_start=False, warm_adjoint=False, store_all=False, graphs=True,
-                                 rollout: DeviceRollout | None = None):
+                                 overlap: DifferentiableSolver | None = None, rollout: DeviceRollout | None = None):
     """Loss of a ``steps``-substep rollout and its gradients, computed on the device.
 
     ``loss_fn(q, v)`` maps the final state to a scalar (differentiated by torch).
     Returns (loss, grads) with grads keys ``q0``, ``v0`` and, when requested,
     ``external_forces`` (a load held over the rollout), ``activations``,
     ``mu_scale``, ``tet_materials``, ``hex_materials``.  Pass a ``DeviceRollout``
-    to reuse its buffers and captured graph across calls.
+    to reuse its buffers and captured graphs across calls, and ``overlap`` (a
+    second solver over the same model) to recompute segments concurrently with
+    the reverse pass.
     """
     if mu_scale is not None:
         diff.set_mu_scale(mu_scale)
     ro = rollout or DeviceRollout(diff, steps, every, refresh=refresh, warm_start=warm_start,
-                                  warm_adjoint=warm_adjoint, store_all=store_all, graphs=graphs)
+                                  warm_adjoint=warm_adjoint, store_all=store_all, graphs=graphs, overlap=overlap)
     qf, vf = ro.forward(q0, v0, external_forces=external_forces, activations=activations)
     qf.requires_grad_(True)
     vf.requires_grad_(True)

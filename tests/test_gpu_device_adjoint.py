@@ -177,7 +177,11 @@ def test_device_beam_gradient_costs_at_most_three_plain_rollouts():
     with torch.cuda.stream(stream):
         with torch.cuda.graph(graph, stream=stream):
             plain_frame()
-    ro = DeviceRollout(diff, steps, every)
+    # a second handle over the same beam recomputes segments concurrently with the reverse pass
+    _, _, _, diff2, _, _ = _beam()
+    diff2.set_mu_scale(s_t)
+    ro = DeviceRollout(diff, steps, every, overlap=diff2)
+    assert ro.overlap is not None
 
     def plain():
         with torch.cuda.stream(stream):
@@ -200,6 +204,23 @@ def test_device_beam_gradient_costs_at_most_three_plain_rollouts():
     plain(), gradient()  # warm-up (graph capture of the segment)
     t_plain, t_grad = best(plain), best(gradient)
     assert t_grad <= 3.0 * t_plain, (t_plain, t_grad)
+
+
+def test_overlapped_recomputation_gives_the_in_line_gradients():
+    """Recomputing segments on a second handle and stream gives bit-identical gradients."""
+    sc, model, solver, diff, s_t, loss_fn = _beam()
+    _, _, _, diff2, _, _ = _beam()
+    diff2.set_mu_scale(s_t)
+    q0 = model.particle_q.clone()
+    v0 = torch.zeros_like(q0)
+    steps, every = 10 * sc.substeps, 2 * sc.substeps
+    _, g_line = device_checkpointed_gradient(diff, q0, v0, steps, every, loss_fn, mu_scale=s_t)
+    ro = DeviceRollout(diff, steps, every, overlap=diff2)
+    assert ro.overlap is not None
+    for _ in range(2):  # the second call replays the graphs captured by the first
+        _, g_over = device_checkpointed_gradient(diff, q0, v0, steps, every, loss_fn, mu_scale=s_t, rollout=ro)
+        for k in ("q0", "v0", "mu_scale"):
+            np.testing.assert_array_equal(to_np(g_over[k]), to_np(g_line[k]))
 
 
 def _material_vjp(solver, q, v, g):
