@@ -200,6 +200,9 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
                                         streams from DRAM, 1 when all of it is kept in L2.  The getter returns the mode
                                         in use (0 when the offsets do not fit) */
 #define FEM_TUNE_UNIFORM_COLUMN_BLOCKS 13  /* read-only: stored blocks whose column offset mode 2 reads once per slice */
+#define FEM_TUNE_CG_VARIANT 14       /* CG recurrence of the persistent PCG: 0 standard (two grid reductions per
+                                        iteration); 1 Chronopoulos-Gear (one reduction per iteration; neighbours'
+                                        next preconditioned residual recomputed at every gathered column) */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);

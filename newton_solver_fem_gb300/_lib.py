@@ -35,6 +35,7 @@ FEM_TUNE_SPLIT_HEADROOM = 10
 FEM_TUNE_TAIL_PREFETCH = 11
 FEM_TUNE_COMPACT_COLUMNS = 12
 FEM_TUNE_UNIFORM_COLUMN_BLOCKS = 13
+FEM_TUNE_CG_VARIANT = 14
 
 FEM_TERM_SPRING = 1
 FEM_TERM_TET = 2

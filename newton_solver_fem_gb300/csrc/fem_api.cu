@@ -258,6 +258,19 @@ int configure_launch(Handle& h) {
     h.resident_slices = rs;
     cudaError_t err = fem::pcg_configure(h);
     if (err != cudaSuccess) return cuda_status(err, &h);
+    h.rec0 = h.rec1 = h.p4 = h.s4 = h.w4 = nullptr;
+    if (h.cg_variant == 1) {  // records and non-resident own-row state of the single-reduction variant
+        std::vector<float4> zeros3(3 * (size_t)h.P, make_float4(0.f, 0.f, 0.f, 0.f));
+        std::vector<float4> zeros1((size_t)h.P, make_float4(0.f, 0.f, 0.f, 0.f));
+        h.rec0 = upload_plain(zeros3, h.launch_allocations, err);
+        h.rec1 = upload_plain(zeros3, h.launch_allocations, err);
+        if (!h.resident) {
+            h.p4 = upload_plain(zeros1, h.launch_allocations, err);
+            h.s4 = upload_plain(zeros1, h.launch_allocations, err);
+            h.w4 = upload_plain(zeros1, h.launch_allocations, err);
+        }
+        if (err != cudaSuccess) return cuda_status(err, &h);
+    }
     const std::vector<int>& slice_scene = h.host_slice_scene;
     const int nscenes = h.nscenes;
     // Slices per CTA, at most slices_per_cta each, balanced by slice cost (or by
@@ -1090,6 +1103,7 @@ int fem_prepare_tet_updates(FemHandle* H, const FemDesc* d, int32_t original_nod
     n.tail_prefetch = h.tail_prefetch;
     n.compact_cols = h.compact_cols;
     n.resident_pref = h.resident_pref;
+    n.cg_variant = h.cg_variant;
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
     if (code == FEM_OK) code = configure_launch(n);
@@ -1172,6 +1186,7 @@ int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, voi
     n.tail_prefetch = h.tail_prefetch;
     n.compact_cols = h.compact_cols;
     n.resident_pref = h.resident_pref;
+    n.cg_variant = h.cg_variant;
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
     if (code == FEM_OK) code = configure_launch(n);
@@ -1273,6 +1288,9 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
     } else if (key == FEM_TUNE_COMPACT_COLUMNS) {
         if (value < -1 || value > 2) return set_error(FEM_ERR_BAD_ARG, "compact columns must be -1, 0, 1 or 2");
         h.compact_cols = (int)value;
+    } else if (key == FEM_TUNE_CG_VARIANT) {
+        if (value != 0 && value != 1) return set_error(FEM_ERR_BAD_ARG, "CG variant must be 0 or 1");
+        h.cg_variant = (int)value;
     } else if (key == FEM_TUNE_TAIL_PREFETCH) {
         if (value < 0 || value > 100) return set_error(FEM_ERR_BAD_ARG, "tail prefetch must be 0..100 percent");
         h.tail_prefetch = (int)value;
@@ -1314,6 +1332,7 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_TAIL_PREFETCH: *value = h.tail_prefetch; return FEM_OK;
         case FEM_TUNE_COMPACT_COLUMNS: *value = column_mode(h); return FEM_OK;
         case FEM_TUNE_UNIFORM_COLUMN_BLOCKS: *value = column_mode(h) == 2 ? h.uniform_blocks : 0; return FEM_OK;
+        case FEM_TUNE_CG_VARIANT: *value = h.cg_variant; return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
 }

@@ -95,7 +95,15 @@ struct PcgArgs {
     float4* zp1;
     float4* stage;   // [2P] (p_i, y_i) handed from phase A to phase B when not staged in shared memory
     int stage_smem;  // 1: the staging lives in the CTA's shared memory
-    int resident;    // rows' state in shared memory: 0 none, 1 x/r/z, 2 x/r/z and the inverse diagonal blocks
+    int resident;    // rows' state in shared memory: 0 none, 1 x/r/z (x/r/p/s/w in the single-reduction
+                     // variant), 2 the same and the inverse diagonal blocks
+    // single-reduction variant: records (u, Mw, Ms) per node as 3 float4 in two alternating buffers,
+    // own-row p, s, w in global memory when not resident
+    float4* rec0;
+    float4* rec1;
+    float4* p4;
+    float4* s4;
+    float4* w4;
     // control
     unsigned* barrier;
     int* status;
@@ -133,6 +141,7 @@ struct Handle {
     int split_headroom = 0;          // % more slices per CTA than the even share a calibrated split may use
     int tail_prefetch = 50;          // FEM_TUNE_TAIL_PREFETCH (percent of warps busy in the last round)
     int resident_pref = -1;          // resident row-state layout: -1 automatic, 0 none, 1 x/r/z, 2 x/r/z + inverse
+    int cg_variant = 0;              // FEM_TUNE_CG_VARIANT: 0 standard CG, 1 single-reduction (Chronopoulos-Gear)
     std::vector<double> cta_speed;   // calibrated SpMV speed per CTA index (cost units per ns)
     std::vector<int64_t> host_slice_cost;  // stored blocks + 4 per live row, per slice
     std::vector<int> host_cta_slice0;      // the partition in use: CTA c owns host_cta_list[cta_slice0[c] ..)
@@ -281,6 +290,9 @@ struct Handle {
     float4 *x = nullptr, *r = nullptr;
     float4 *zp0 = nullptr, *zp1 = nullptr;  // [2P] each: (z_i, p_i) records
     float4* stage = nullptr;                // [2P] (p_i, y_i) phase A -> phase B staging
+    // single-reduction variant (launch allocations): (u, Mw, Ms) records in two alternating buffers
+    // [3P] each, and the own-row p, s, w when they are not resident in shared memory [P] each
+    float4 *rec0 = nullptr, *rec1 = nullptr, *p4 = nullptr, *s4 = nullptr, *w4 = nullptr;
     int stage_smem = 0;
     int resident = 0;                       // row state resident in shared memory (see PcgArgs)
     float* dv = nullptr;

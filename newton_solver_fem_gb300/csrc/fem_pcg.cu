@@ -45,6 +45,7 @@ struct SceneState {
     int active;
     int iters;
     int zero;
+    int primed;  // single-reduction variant: the first SpMV (w0 = A u0) has been reduced
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -253,6 +254,53 @@ __device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int le
     return acc;
 }
 
+// Single-reduction (Chronopoulos-Gear) records: node j's (u_j, Mw_j, Ms_j) as 3 float4 = (u.xyz, mw.x),
+// (mw.yz, ms.xy), (ms.z, -, -, -).  The next preconditioned residual u' = M r' = u - alpha (Mw + beta Ms)
+// follows from the record alone, so a gathering row recomputes it with the same expression the owner
+// uses (bit-identical everywhere) instead of waiting at a second grid barrier for the owner to write it.
+__device__ __forceinline__ float3 next_u(float4 r0, float4 r1, float r2x, float alpha, float beta, float3& t) {
+    t = f3(fmaf(beta, r1.z, r0.w), fmaf(beta, r1.w, r1.x), fmaf(beta, r2x, r1.y));  // M s = Mw + beta Ms
+    return f3(fmaf(-alpha, t.x, r0.x), fmaf(-alpha, t.y, r0.y), fmaf(-alpha, t.z, r0.z));
+}
+template <bool PRIME>
+__device__ __forceinline__ float3 gather_u(const float4* rec, int j, float alpha, float beta) {
+    const float4* q = rec + 3 * (size_t)j;
+    const float4 r0 = q[0];
+    if (PRIME) return xyz(r0);
+    const float4 r1 = q[1];
+    const float r2x = reinterpret_cast<const float*>(q + 2)[0];
+    float3 t;
+    return next_u(r0, r1, r2x, alpha, beta, t);
+}
+
+// w_row = sum_k A_k u'_{j_k} (the single-reduction variant's SpMV), U block columns in flight.
+template <int U, int CM, bool PRIME>
+__device__ __forceinline__ float3 row_times_u(const PcgArgs& a, int base, int len, int lane, int row,
+                                              const SliceCols& sc, const float4* rec, float alpha, float beta,
+                                              unsigned long long pol) {
+    float3 acc = f3(0.f, 0.f, 0.f);
+    int k = 0;
+    if (U > 1) {
+        for (; k + U <= len; k += U) {
+            Entry m[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                m[u] = load_entry<CM>(a, (size_t)(base + k + u) * kSlice + lane, k + u, row, sc, pol);
+            float3 g[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) g[u] = gather_u<PRIME>(rec, m[u].j, alpha, beta);
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc = acc + bmul(m[u].A, m[u].B, m[u].C, g[u]);
+        }
+    }
+    for (; k < len; ++k) {
+        Entry m = load_entry<CM>(a, (size_t)(base + k) * kSlice + lane, k, row, sc, pol);
+        float3 g = gather_u<PRIME>(rec, m.j, alpha, beta);
+        acc = acc + bmul(m.A, m.B, m.C, g);
+    }
+    return acc;
+}
+
 // Prologue pass: cv = sum_k A_k (v_j - v_i) and ax = sum_k A_k x_j in one read of the row.
 template <int U, int CM>
 __device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int len, int lane, int row,
@@ -306,11 +354,16 @@ struct Smem {
 // layout 2, the block-Jacobi inverse (9-17; layout 1 reads it from global
 // memory).  With it, the x/r/z update reads and writes shared memory only; the
 // (z, p) record is still written for the gathers.
-__host__ __device__ __forceinline__ int res_floats(int layout) { return layout == 2 ? 18 : 9; }
+// Single-reduction variant (V = 1): x (0-2), r (3-5), p (6-8), s (9-11), w (12-14) and, in layout 2,
+// the inverse (15-23).
+__host__ __device__ __forceinline__ int res_floats(int layout, int V = 0) {
+    return V == 1 ? (layout == 2 ? 24 : 15) : (layout == 2 ? 18 : 9);
+}
+__host__ __device__ __forceinline__ int res_minv_offset(int V) { return V == 1 ? 15 : 9; }
 
 // The resident state of row `row` (lane `lane` of slice `sl`).
-__device__ __forceinline__ float* res_slot(const Smem& sm, int sl, int first, int lane, int layout) {
-    return sm.res + (size_t)((sl - first) * kSlice + lane) * res_floats(layout);
+__device__ __forceinline__ float* res_slot(const Smem& sm, int sl, int first, int lane, int layout, int V = 0) {
+    return sm.res + (size_t)((sl - first) * kSlice + lane) * res_floats(layout, V);
 }
 __device__ __forceinline__ float3 res3(const float* s, int k) { return f3(s[k], s[k + 1], s[k + 2]); }
 __device__ __forceinline__ void res3_store(float* s, int k, float3 v) {
@@ -318,8 +371,8 @@ __device__ __forceinline__ void res3_store(float* s, int k, float3 v) {
     s[k + 1] = v.y;
     s[k + 2] = v.z;
 }
-__device__ __forceinline__ float3 res_minv_mul(const float* s, float3 r) {
-    const float* b = s + 9;
+__device__ __forceinline__ float3 res_minv_mul(const float* s, float3 r, int off = 9) {
+    const float* b = s + off;
     return f3(b[0] * r.x + b[1] * r.y + b[2] * r.z, b[3] * r.x + b[4] * r.y + b[5] * r.z,
               b[6] * r.x + b[7] * r.y + b[8] * r.z);
 }
@@ -342,7 +395,8 @@ struct SmemLayout {
     size_t part, st, tot, segb, sseg, slc, kmask, kval, rinfo, stage, res, total;
 };
 __host__ __device__ __forceinline__ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
-__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage, int resident, bool uni) {
+__host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool stage, int resident, bool uni,
+                                                             int V = 0) {
     SmemLayout m;
     m.part = 0;
     m.st = m.part + align16((size_t)L * 3 * sizeof(float));
@@ -355,7 +409,7 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool st
     m.rinfo = m.kval + (uni ? align16((size_t)L * 64 * sizeof(short)) : 0);
     m.stage = m.rinfo + align16((size_t)L * kSlice * sizeof(unsigned));
     m.res = m.stage + (stage ? (size_t)L * kSlice * 2 * sizeof(float4) : 0);
-    m.total = m.res + (resident ? (size_t)L * kSlice * res_floats(resident) * sizeof(float) : 0);
+    m.total = m.res + (resident ? (size_t)L * kSlice * res_floats(resident, V) * sizeof(float) : 0);
     return m;
 }
 
@@ -501,7 +555,7 @@ __device__ __forceinline__ float rhs_scale(float maximum) {
     return scale;
 }
 
-template <int U, int CM>
+template <int U, int CM, int V>
 __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const unsigned long long pol_last = policy_evict_last();
     const unsigned long long pol_first = policy_evict_first();
@@ -511,7 +565,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     const int S = a.nscenes;
     const int L = a.slices_per_cta;
     Smem sm;
-    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0, a.resident, CM == 2);
+    const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0, a.resident, CM == 2, V);
     sm.part = reinterpret_cast<float*>(smem_raw + lay.part);
     sm.st = reinterpret_cast<SceneState*>(smem_raw + lay.st);
     sm.tot = reinterpret_cast<float*>(smem_raw + lay.tot);
@@ -602,7 +656,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 }
                 store3(a.f_ws, row, rhs);
             }
-            if (a.resident) res3_store(res_slot(sm, sl, first, lane, a.resident), 3, u);
+            if (a.resident) res3_store(res_slot(sm, sl, first, lane, a.resident, V), 3, u);
             else a.r[row] = f4(u);
             mx = fmaxf(fabsf(rhs.x), fmaxf(fabsf(rhs.y), fabsf(rhs.z)));
         }
@@ -628,7 +682,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             int row = meta.x + lane;
             float sc = st.scale;
             float3 x = f3(0.f, 0.f, 0.f), r = f3(0.f, 0.f, 0.f);
-            float* rs = a.resident ? res_slot(sm, sl, first, lane, a.resident) : nullptr;
+            float* rs = a.resident ? res_slot(sm, sl, first, lane, a.resident, V) : nullptr;
             if (!st.zero) {
                 if (a.solve_rhs == nullptr || a.solve_warm) x = xyz(a.x[row]) * sc;  // else solve mode starts from zero
                 r = (a.resident ? res3(rs, 3) : xyz(a.r[row])) * sc;
@@ -640,23 +694,42 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             else
                 b = load3(a.f_ws, row) * sc;
             float3 z;
+            const int mo = res_minv_offset(V);
             if (a.resident) {
                 if (a.resident == 2) {
-                    for (int k = 0; k < 9; ++k) rs[9 + k] = a.minv[9 * (size_t)row + k];
-                    z = res_minv_mul(rs, r);
+                    for (int k = 0; k < 9; ++k) rs[mo + k] = a.minv[9 * (size_t)row + k];
+                    z = res_minv_mul(rs, r, mo);
                 } else {
                     z = minv_mul(a.minv, row, r);
                 }
                 res3_store(rs, 0, x);
                 res3_store(rs, 3, r);
-                res3_store(rs, 6, z);
+                if (V == 0) {
+                    res3_store(rs, 6, z);
+                } else {  // p, s, w start at zero
+                    res3_store(rs, 6, f3(0.f, 0.f, 0.f));
+                    res3_store(rs, 9, f3(0.f, 0.f, 0.f));
+                    res3_store(rs, 12, f3(0.f, 0.f, 0.f));
+                }
             } else {
                 z = minv_mul(a.minv, row, r);
                 a.x[row] = f4(x);
                 a.r[row] = f4(r);
+                if (V == 1) {
+                    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                    a.p4[row] = zero4;
+                    a.s4[row] = zero4;
+                    a.w4[row] = zero4;
+                }
             }
-            a.zp0[2 * (size_t)row] = f4(z);
-            a.zp0[2 * (size_t)row + 1] = f4(f3(0.f, 0.f, 0.f));  // full record; p unused in the first iteration
+            if (V == 0) {
+                a.zp0[2 * (size_t)row] = f4(z);
+                a.zp0[2 * (size_t)row + 1] = f4(f3(0.f, 0.f, 0.f));  // full record; p unused in the first iteration
+            } else {  // record (u0, Mw = 0, Ms = 0) for the first SpMV, w0 = A u0
+                a.rec0[3 * (size_t)row] = make_float4(z.x, z.y, z.z, 0.f);
+                a.rec0[3 * (size_t)row + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                a.rec0[3 * (size_t)row + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
             rr = dot3(r, r);
             rz = dot3(r, z);
             bb = dot3(b, b);
@@ -678,6 +751,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         st.iters = 0;
         st.beta = 0.0f;
         st.alpha = 0.0f;
+        st.primed = 0;
         st.active = (st.rr > st.atol_sq) && (a.maxiter > 0);
         if (!isfinite(st.rr)) {
             st.active = 0;
@@ -688,6 +762,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     if (!reduce_across_grid(a, sm, buf1, 3, false, first, last, epoch, &s_ok, &s_any, start_cg)) return;
 
     // ---------------- CG iterations
+    if constexpr (V == 0) {
     for (int it = 0; s_any; ++it) {
         const float4* rec = (it & 1) ? a.zp1 : a.zp0;  // z and p of this iteration
         float4* rec_next = (it & 1) ? a.zp0 : a.zp1;   // (z, p) for the next, written by phase B
@@ -797,6 +872,131 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         };
         if (!reduce_across_grid(a, sm, buf1, 2, false, first, last, epoch, &s_ok, &s_any, next_iteration)) return;
     }
+    } else {
+    // Single-reduction (Chronopoulos-Gear) CG: one pass and one grid reduction per iteration.  Pass k
+    // first applies update k with the scalars of reduction k-1 to the CTA's own rows
+    //   p = u + beta p,  s = w + beta s,  x += alpha p,  r -= alpha s,
+    //   u' = u - alpha (Mw + beta Ms)  (= M r'),  Ms' = Mw + beta Ms,
+    // then forms w' = A u' from the neighbours' records (u' recomputed at the gather), Mw' = M w', writes
+    // the row's next record (u', Mw', Ms') and the partials (r', u'), (w', u'), (r', r').  Pass 0 only
+    // forms w0 = A u0 (alpha0 = gamma0 / delta0).  The convergence test of update k comes with the
+    // reduction that follows its SpMV, so a converged solve has done one SpMV more than standard CG.
+    for (int pass = 0; s_any; ++pass) {
+        const float4* rc = (pass & 1) ? a.rec1 : a.rec0;  // (u, Mw, Ms) of this pass
+        float4* rn = (pass & 1) ? a.rec0 : a.rec1;         // written for the next one
+        if (a.cta_time != nullptr && threadIdx.x == 0) s_t0 = global_ns();
+        if (a.tail_prefetch && a.contiguous && warp == W - 1) prefetch_last_round(a, sm, first, last, W, lane);
+        for (int sl = first + warp; sl < last; sl += W) {
+            const int4 sl4 = sm.slc[sl - first];
+            const SceneState& st = sm.st[sl4.z & ~kResidentSlice];
+            float gam = 0.f, del = 0.f, rrl = 0.f;
+            if (st.active && lane < sl4.y) {
+                const int row = sl4.x + lane;
+                const unsigned info = sm.rinfo[(sl - first) * kSlice + lane];
+                const bool prime = !st.primed;
+                const float alpha = st.alpha, beta = st.beta;
+                float* rs = a.resident ? res_slot(sm, sl, first, lane, a.resident, 1) : nullptr;
+                const float4* own = rc + 3 * (size_t)row;
+                const float4 o0 = own[0];
+                float3 un, msn, r;
+                if (prime) {
+                    un = xyz(o0);
+                    msn = f3(0.f, 0.f, 0.f);
+                    r = rs ? res3(rs, 3) : xyz(a.r[row]);
+                } else {
+                    const float4 o1 = own[1];
+                    const float o2 = reinterpret_cast<const float*>(own + 2)[0];
+                    un = next_u(o0, o1, o2, alpha, beta, msn);
+                    const float3 uo = xyz(o0);
+                    float3 pv = rs ? res3(rs, 6) : xyz(a.p4[row]);
+                    float3 sv = rs ? res3(rs, 9) : xyz(a.s4[row]);
+                    const float3 wv = rs ? res3(rs, 12) : xyz(a.w4[row]);
+                    float3 x = rs ? res3(rs, 0) : xyz(a.x[row]);
+                    r = rs ? res3(rs, 3) : xyz(a.r[row]);
+                    pv = f3(fmaf(beta, pv.x, uo.x), fmaf(beta, pv.y, uo.y), fmaf(beta, pv.z, uo.z));
+                    sv = f3(fmaf(beta, sv.x, wv.x), fmaf(beta, sv.y, wv.y), fmaf(beta, sv.z, wv.z));
+                    x = f3(fmaf(alpha, pv.x, x.x), fmaf(alpha, pv.y, x.y), fmaf(alpha, pv.z, x.z));
+                    r = f3(fmaf(-alpha, sv.x, r.x), fmaf(-alpha, sv.y, r.y), fmaf(-alpha, sv.z, r.z));
+                    if (rs) {
+                        res3_store(rs, 0, x);
+                        res3_store(rs, 3, r);
+                        res3_store(rs, 6, pv);
+                        res3_store(rs, 9, sv);
+                    } else {
+                        a.x[row] = f4(x);
+                        a.r[row] = f4(r);
+                        a.p4[row] = f4(pv);
+                        a.s4[row] = f4(sv);
+                    }
+                }
+                float3 w = un;  // fixed rows: identity (their u is zero)
+                if (!(info & kFixedBit)) {
+                    const int len = (int)(info & ~kFixedBit);
+                    const unsigned long long pol = (sl4.z & kResidentSlice) ? pol_last : pol_first;
+                    const SliceCols sc = slice_cols(sl);
+                    w = prime ? row_times_u<U, CM, true>(a, sl4.w, len, lane, row, sc, rc, alpha, beta, pol)
+                              : row_times_u<U, CM, false>(a, sl4.w, len, lane, row, sc, rc, alpha, beta, pol);
+                }
+                const float3 mw = a.resident == 2 ? res_minv_mul(rs, w, 15) : minv_mul(a.minv, row, w);
+                if (rs) res3_store(rs, 12, w);
+                else a.w4[row] = f4(w);
+                float4* nx = rn + 3 * (size_t)row;
+                nx[0] = make_float4(un.x, un.y, un.z, mw.x);
+                nx[1] = make_float4(mw.y, mw.z, msn.x, msn.y);
+                nx[2] = make_float4(msn.z, 0.f, 0.f, 0.f);
+                gam = dot3(r, un);
+                del = dot3(w, un);
+                rrl = dot3(r, r);
+            }
+            gam = warp_sum(gam);
+            del = warp_sum(del);
+            rrl = warp_sum(rrl);
+            if (lane == 0) {
+                float* pp = sm.part + (sl - first) * 3;
+                pp[0] = gam; pp[1] = del; pp[2] = rrl;
+            }
+        }
+        if (a.cta_time != nullptr) {  // speed calibration: this CTA's pass time
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                a.cta_time[2 * blockIdx.x] += global_ns() - s_t0;
+                a.cta_time[2 * blockIdx.x + 1] += 1;
+            }
+        }
+        auto next_pass = [&](int s) {
+            SceneState& st = sm.st[s];
+            if (!st.active) return;
+            const double gam = sm.tot[s * 3], del = sm.tot[s * 3 + 1], rr = sm.tot[s * 3 + 2];
+            if (!st.primed) {  // gamma0 = r0.u0 came with the start reduction
+                st.primed = 1;
+                st.beta = 0.0f;
+                st.alpha = (float)(st.rz / del);
+                if (!isfinite(st.alpha)) {
+                    st.active = 0;
+                    atomicOr(a.status, kStatusNonFinite);
+                }
+            } else {
+                st.iters += 1;
+                st.rr = rr;
+                st.active = (rr > st.atol_sq) && (st.iters < a.maxiter);
+                if (!isfinite(rr)) {
+                    st.active = 0;
+                    atomicOr(a.status, kStatusNonFinite);
+                }
+                if (st.active) {
+                    const float beta = (float)(gam / st.rz);
+                    st.alpha = (float)(gam / (del - (double)beta * gam / (double)st.alpha));
+                    st.beta = beta;
+                    st.rz = gam;
+                }
+            }
+            if (st.active) atomicOr(&s_any, 1);
+        };
+        if (!reduce_across_grid(a, sm, (pass & 1) ? buf1 : buf0, 3, false, first, last, epoch, &s_ok, &s_any,
+                                next_pass))
+            return;
+    }
+    }
 
     // ---------------- epilogue: restore scale, integrate, fixed restore
     for (int sl = first + warp; sl < last; sl += W) {
@@ -805,7 +1005,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         if (lane >= meta.y) continue;
         const SceneState& st = sm.st[sl4.z & ~kResidentSlice];
         int row = meta.x + lane;
-        float3 dv = a.resident ? res3(res_slot(sm, sl, first, lane, a.resident), 0) : xyz(a.x[row]);
+        float3 dv = a.resident ? res3(res_slot(sm, sl, first, lane, a.resident, V), 0) : xyz(a.x[row]);
         float sc = st.scale;
         dv = f3(dv.x / sc, dv.y / sc, dv.z / sc);
         store3(a.dv, row, dv);
@@ -843,16 +1043,20 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
 
 using PcgKernel = void (*)(PcgArgs);
 
-template <int CM>
+template <int CM, int V>
 PcgKernel pcg_kernel_cm(int unroll) {
     switch (unroll) {
-        case 2: return pcg_kernel<2, CM>;
-        case 4: return pcg_kernel<4, CM>;
-        default: return pcg_kernel<1, CM>;
+        case 2: return pcg_kernel<2, CM, V>;
+        case 4: return pcg_kernel<4, CM, V>;
+        default: return pcg_kernel<1, CM, V>;
     }
 }
-PcgKernel pcg_kernel_for(int unroll, int cm) {
-    return cm == 2 ? pcg_kernel_cm<2>(unroll) : (cm == 1 ? pcg_kernel_cm<1>(unroll) : pcg_kernel_cm<0>(unroll));
+template <int V>
+PcgKernel pcg_kernel_v(int unroll, int cm) {
+    return cm == 2 ? pcg_kernel_cm<2, V>(unroll) : (cm == 1 ? pcg_kernel_cm<1, V>(unroll) : pcg_kernel_cm<0, V>(unroll));
+}
+PcgKernel pcg_kernel_for(int unroll, int cm, int variant) {
+    return variant == 1 ? pcg_kernel_v<1>(unroll, cm) : pcg_kernel_v<0>(unroll, cm);
 }
 
 
@@ -871,7 +1075,8 @@ cudaError_t pcg_configure(Handle& h) {
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return cudaErrorNotSupported;
     const int cm = column_mode(h);
-    PcgKernel kern = pcg_kernel_for(h.spmv_unroll, cm);
+    const int V = h.cg_variant;
+    PcgKernel kern = pcg_kernel_for(h.spmv_unroll, cm, V);
     // Automatic CTA size: 1024-thread CTAs once there are 8 slices per SM (fewer
     // CTAs make the grid reductions cheaper: on a 3,677-slice Tet4 system 115
     // such CTAs beat 460 of 256 threads by 8% per CG iteration); small systems
@@ -898,12 +1103,14 @@ cudaError_t pcg_configure(Handle& h) {
         for (int pass = 0;; ++pass) {
             int L = (h.nslices + grid - 1) / grid > 0 ? (h.nslices + grid - 1) / grid : 1;
             if (slack_pct > 0) L += std::max(1, (L * slack_pct + 99) / 100);
-            bool stage = stage_in_smem(L, threads) && pass < 16;  // give up shared staging if it never settles
-            int res = stage ? want_resident : 0;
+            // the single-reduction variant hands nothing from one phase to another: no staging, and its
+            // row state may be resident on its own
+            bool stage = V == 0 && stage_in_smem(L, threads) && pass < 16;  // give up if it never settles
+            int res = (stage || (V == 1 && pass < 16)) ? want_resident : 0;
             int per_sm = 0;
             size_t smem = 0;
             for (int attempt = 0; attempt < 3; ++attempt) {
-                const SmemLayout lay = smem_layout(L, h.nscenes, stage, res, cm == 2);
+                const SmemLayout lay = smem_layout(L, h.nscenes, stage, res, cm == 2, V);
                 if ((lay.st | lay.tot | lay.segb | lay.sseg | lay.slc | lay.kmask | lay.kval | lay.rinfo | lay.stage |
                      lay.res) & 15)
                     return cudaErrorMisalignedAddress;
@@ -1014,6 +1221,11 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     a.stage = h.stage;
     a.stage_smem = h.stage_smem;
     a.resident = h.resident;
+    a.rec0 = h.rec0;
+    a.rec1 = h.rec1;
+    a.p4 = h.p4;
+    a.s4 = h.s4;
+    a.w4 = h.w4;
     a.barrier = h.barrier;
     a.status = h.status;
     a.scene_stats = h.scene_stats;
@@ -1039,7 +1251,7 @@ cudaError_t launch_pcg(Handle& h, float dt, int write_state, float* q_out, float
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, pcg_kernel_for(h.spmv_unroll, cm), a);
+    return cudaLaunchKernelEx(&cfg, pcg_kernel_for(h.spmv_unroll, cm, h.cg_variant), a);
 }
 
 }  // namespace fem

@@ -438,6 +438,33 @@ def test_batched_scenes_match_oracle_fixed_iterations():
         assert rel_l2(dv[sl], oracle.dv[sl]) < 1e-4
 
 
+def test_single_reduction_cg_matches_oracle_fixed_iterations_on_a_batch():
+    """The single-reduction (Chronopoulos-Gear) recurrence is CG: at a fixed iteration count each scene of
+    a batch (fixed faces, spread over CTAs) matches the oracle's standard PCG."""
+    sc = scenes.batched_scenes(count=24, seed=5, dims=(3, 10))
+    model, solver, oracle = scene_pair(sc, linear_solver_maxiter=10, linear_solver_tolerance=1e-30)
+    _lib.check(_lib.load().fem_set_tuning(solver._handle, _lib.FEM_TUNE_CG_VARIANT, 1))
+    rng = np.random.default_rng(8)
+    q = rounded(sc.x + rng.normal(0, 0.001, sc.x.shape))
+    q[sc.fixed] = rounded(sc.x[sc.fixed])
+    v = rounded(rng.normal(0, 0.05, sc.x.shape))
+    v[sc.fixed] = 0.0
+    s0, s1 = model.state(), model.state()
+    s0.particle_q.copy_(tensor(q))
+    s0.particle_qd.copy_(tensor(v))
+    solver.refresh_tangent(s0.particle_q)
+    solver.step(s0, s1, None, None, sc.dt)
+    stats = solver.stats()
+    assert stats["scene_iterations"] == [10] * (len(sc.scene_offsets) - 1)
+    oracle.refresh_tangent(q)
+    oracle.step(q, v, sc.dt, fixed_iterations=10)
+    dv = to_np(solver.velocity_increment)
+    offs = sc.scene_offsets
+    for s in range(len(offs) - 1):
+        sl = slice(offs[s], offs[s + 1])
+        assert rel_l2(dv[sl], oracle.dv[sl]) < 1e-4, s
+
+
 def test_barrier_wait_limit_reports_timeout_and_recovers():
     """A bounded grid-barrier wait that runs out returns a status, not a hang or fault; the context stays usable."""
     sc = scenes.hex_block_64(n=24)  # many CTAs in the cooperative grid

@@ -1,10 +1,11 @@
 """PCG launch tuning on the GPU (``-m gpu``): every launch variant solves the same system.
 
 The variants (SpMV unroll, CTA size, resident row-state layout, row split by
-calibrated CTA speed) change only the summation order of the grid reductions and
-where row state lives, so a substep agrees with the default configuration to
-float32 round-off (relative 1e-5 on the velocity increment at a tight
-tolerance), and repeated substeps of one configuration are bit-identical.
+calibrated CTA speed, the single-reduction CG recurrence) change only the
+summation order of the grid reductions, where row state lives or the rounding of
+mathematically equal recurrences, so a substep agrees with the default
+configuration to float32 round-off (relative 1e-5 on the velocity increment at a
+tight tolerance), and repeated substeps of one configuration are bit-identical.
 """
 
 import ctypes
@@ -57,6 +58,11 @@ VARIANTS = [
     {_lib.FEM_TUNE_COMPACT_COLUMNS: 2, _lib.FEM_TUNE_SPMV_UNROLL: 1},
     {_lib.FEM_TUNE_L2_RESIDENT_BYTES: 0},
     {_lib.FEM_TUNE_L2_RESIDENT_BYTES: 1 << 20, _lib.FEM_TUNE_COMPACT_COLUMNS: 2},
+    {_lib.FEM_TUNE_CG_VARIANT: 1},
+    {_lib.FEM_TUNE_CG_VARIANT: 1, _lib.FEM_TUNE_RESIDENT_LAYOUT: 0},
+    {_lib.FEM_TUNE_CG_VARIANT: 1, _lib.FEM_TUNE_RESIDENT_LAYOUT: 2},
+    {_lib.FEM_TUNE_CG_VARIANT: 1, _lib.FEM_TUNE_COMPACT_COLUMNS: 1, _lib.FEM_TUNE_SPMV_UNROLL: 2},
+    {_lib.FEM_TUNE_CG_VARIANT: 1, _lib.FEM_TUNE_BALANCE: 1},
 ]
 
 
