@@ -337,7 +337,7 @@ int configure_launch(Handle& h) {
     h.seg_start = upload_plain(seg_start, h.launch_allocations, err);
     h.seg_pos = upload_plain(seg_pos, h.launch_allocations, err);
     h.scene_seg0 = upload_plain(scene_seg0, h.launch_allocations, err);
-    std::vector<float> zeros(2 * 8 * (size_t)std::max(1, nseg), 0.0f);  // up to 8 values per reduction
+    std::vector<float> zeros(2 * 3 * (size_t)std::max(1, nseg), 0.0f);
     h.seg_part = upload_plain(zeros, h.launch_allocations, err);
     if (err != cudaSuccess) return cuda_status(err, &h);
     return FEM_OK;

@@ -46,8 +46,6 @@ struct SceneState {
     int iters;
     int zero;
     int primed;  // single-reduction variant: the first SpMV (w0 = A u0) has been reduced
-    int final;   // single-reduction variant: the last update (x += alpha p) is left to the epilogue
-    int last;    // single-reduction variant: the scene's last pass (its records are in buffer (last + 1) & 1)
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -256,12 +254,12 @@ __device__ __forceinline__ float3 row_times_p(const PcgArgs& a, int base, int le
     return acc;
 }
 
-// Single-reduction (Chronopoulos-Gear) records: node j's (u_j, Mw_j, Ms_j) as 3 float4 = (u.xyz, ms.x),
-// (mw.xyz, ms.y), (ms.z, -, -, -).  The next preconditioned residual u' = M r' = u - alpha (Mw + beta Ms)
+// Single-reduction (Chronopoulos-Gear) records: node j's (u_j, Mw_j, Ms_j) as 3 float4 = (u.xyz, mw.x),
+// (mw.yz, ms.xy), (ms.z, -, -, -).  The next preconditioned residual u' = M r' = u - alpha (Mw + beta Ms)
 // follows from the record alone, so a gathering row recomputes it with the same expression the owner
 // uses (bit-identical everywhere) instead of waiting at a second grid barrier for the owner to write it.
 __device__ __forceinline__ float3 next_u(float4 r0, float4 r1, float r2x, float alpha, float beta, float3& t) {
-    t = f3(fmaf(beta, r0.w, r1.x), fmaf(beta, r1.w, r1.y), fmaf(beta, r2x, r1.z));  // M s = Mw + beta Ms
+    t = f3(fmaf(beta, r1.z, r0.w), fmaf(beta, r1.w, r1.x), fmaf(beta, r2x, r1.y));  // M s = Mw + beta Ms
     return f3(fmaf(-alpha, t.x, r0.x), fmaf(-alpha, t.y, r0.y), fmaf(-alpha, t.z, r0.z));
 }
 template <bool PRIME>
@@ -337,9 +335,9 @@ __device__ __forceinline__ void row_predictor(const PcgArgs& a, int base, int le
 }
 
 struct Smem {
-    float* part;      // [L * RS] slice partials (RS values per reduction: 3, or 8 in the single-reduction variant)
+    float* part;      // [L * 3] slice partials
     SceneState* st;   // [S]
-    float* tot;       // [S * RS] per-scene totals of the last reduction
+    float* tot;       // [S * 3] per-scene totals of the last reduction
     float4* stage;    // [L * 32 * 2] (p, y) per row, when staged in shared memory
     int* segb;        // [L + 1] bounds (positions in the CTA's slice list) of its per-scene segments,
                       // then [L] where each segment's partials go in the segment buffer
@@ -401,10 +399,9 @@ __host__ __device__ __forceinline__ SmemLayout smem_layout(int L, int S, bool st
                                                              int V = 0) {
     SmemLayout m;
     m.part = 0;
-    const int rs = V == 1 ? 8 : 3;  // values per reduction
-    m.st = m.part + align16((size_t)L * rs * sizeof(float));
+    m.st = m.part + align16((size_t)L * 3 * sizeof(float));
     m.tot = m.st + align16((size_t)S * sizeof(SceneState));
-    m.segb = m.tot + align16((size_t)S * rs * sizeof(float));
+    m.segb = m.tot + align16((size_t)S * 3 * sizeof(float));
     m.sseg = m.segb + align16((size_t)(2 * L + 1) * sizeof(int));
     m.slc = m.sseg + align16((size_t)(S + 1) * sizeof(int));
     m.kmask = m.slc + align16((size_t)L * sizeof(int4));
@@ -443,22 +440,21 @@ constexpr int kResidentSlice = 1 << 30;  // slice table scene field: the slice's
 
 // Segment t's partials (sum or max over its slices: lane-strided, then a fixed
 // xor butterfly) to its slot of the segment buffer; entered by a whole warp.
-template <int RS>
 __device__ __forceinline__ void write_segment(const PcgArgs& a, const Smem& sm, float* buf, int nv, bool is_max,
                                               int first, int t, int lane) {
     const int lo = sm.segb[t], hi = sm.segb[t + 1];
     for (int k = 0; k < nv; ++k) {
         float acc = 0.f;
         for (int sl = lo + lane; sl < hi; sl += 32) {
-            const float v = sm.part[(sl - first) * RS + k];
+            const float v = sm.part[(sl - first) * 3 + k];
             acc = is_max ? fmaxf(acc, v) : acc + v;
         }
         acc = is_max ? warp_max(acc) : warp_sum(acc);
-        if (lane == 0) buf[(size_t)sm.segb[a.slices_per_cta + 1 + t] * RS + k] = acc;
+        if (lane == 0) buf[(size_t)sm.segb[a.slices_per_cta + 1 + t] * 3 + k] = acc;
     }
 }
 
-template <int RS, class Update>
+template <class Update>
 __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf, int nv, bool is_max, int first,
                                    int last, unsigned& epoch, int* s_ok, int* s_any, Update upd) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -469,13 +465,12 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
     // before the arrival
     const bool spread = sm.nsc > kSegmentsPerWarp0;
     if (spread) {
-        for (int t = warp; t < sm.nsc; t += (int)(blockDim.x >> 5))
-            write_segment<RS>(a, sm, buf, nv, is_max, first, t, lane);
+        for (int t = warp; t < sm.nsc; t += (int)(blockDim.x >> 5)) write_segment(a, sm, buf, nv, is_max, first, t, lane);
         __syncthreads();
     }
     if (warp == 0) {
         if (!spread)
-            for (int t = 0; t < sm.nsc; ++t) write_segment<RS>(a, sm, buf, nv, is_max, first, t, lane);
+            for (int t = 0; t < sm.nsc; ++t) write_segment(a, sm, buf, nv, is_max, first, t, lane);
         __syncwarp();
         int ok = 1;
         if (lane == 0) ok = arrive_and_wait(a.barrier, gridDim.x, epoch, a.status, a.limit_ns);
@@ -483,27 +478,22 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
         if (ok && S <= kWarpReducedScenes) {
             for (int sc = 0; sc < S; ++sc) {
                 const int lo = sm.sseg[sc], hi = sm.sseg[sc + 1];
-                for (int k0 = 0; k0 < nv; k0 += 3) {  // three values at a time keep the batch in registers
-                    const int kn = min(3, nv - k0);
-                    float acc[3] = {0.f, 0.f, 0.f};
-                    for (int g0 = lo + lane; g0 < hi; g0 += 32 * kSegLoadBatch) {
-                        float v[kSegLoadBatch][3];
+                float acc[3] = {0.f, 0.f, 0.f};
+                for (int g0 = lo + lane; g0 < hi; g0 += 32 * kSegLoadBatch) {
+                    float v[kSegLoadBatch][3];
 #pragma unroll
-                        for (int u = 0; u < kSegLoadBatch; ++u) {
-                            const int g = g0 + 32 * u;
-                            for (int k = 0; k < kn; ++k)
-                                v[u][k] = g < hi ? __ldcg(buf + (size_t)g * RS + k0 + k) : 0.f;
-                        }
+                    for (int u = 0; u < kSegLoadBatch; ++u) {
+                        const int g = g0 + 32 * u;
+                        for (int k = 0; k < nv; ++k) v[u][k] = g < hi ? __ldcg(buf + (size_t)g * 3 + k) : 0.f;
+                    }
 #pragma unroll
-                        for (int u = 0; u < kSegLoadBatch; ++u)
-                            if (g0 + 32 * u < hi)
-                                for (int k = 0; k < kn; ++k)
-                                    acc[k] = is_max ? fmaxf(acc[k], v[u][k]) : acc[k] + v[u][k];
-                    }
-                    for (int k = 0; k < kn; ++k) {
-                        const float t = is_max ? warp_max(acc[k]) : warp_sum(acc[k]);
-                        if (lane == 0) sm.tot[sc * RS + k0 + k] = t;
-                    }
+                    for (int u = 0; u < kSegLoadBatch; ++u)
+                        if (g0 + 32 * u < hi)
+                            for (int k = 0; k < nv; ++k) acc[k] = is_max ? fmaxf(acc[k], v[u][k]) : acc[k] + v[u][k];
+                }
+                for (int k = 0; k < nv; ++k) {
+                    const float t = is_max ? warp_max(acc[k]) : warp_sum(acc[k]);
+                    if (lane == 0) sm.tot[sc * 3 + k] = t;
                 }
             }
             __syncwarp();
@@ -519,10 +509,10 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
             for (int k = 0; k < nv; ++k) {
                 float acc = 0.f;
                 for (int g = lo; g < hi; ++g) {
-                    const float v = __ldcg(buf + (size_t)g * RS + k);
+                    const float v = __ldcg(buf + (size_t)g * 3 + k);
                     acc = is_max ? fmaxf(acc, v) : acc + v;
                 }
-                sm.tot[sc * RS + k] = acc;
+                sm.tot[sc * 3 + k] = acc;
             }
             upd(sc);
         }
@@ -574,7 +564,6 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     __shared__ int s_any;
     const int S = a.nscenes;
     const int L = a.slices_per_cta;
-    constexpr int RS = V == 1 ? 8 : 3;  // values per grid reduction (slot stride of part, tot, buffers)
     Smem sm;
     const SmemLayout lay = smem_layout(L, S, a.stage_smem != 0, a.resident, CM == 2, V);
     sm.part = reinterpret_cast<float*>(smem_raw + lay.part);
@@ -672,16 +661,16 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             mx = fmaxf(fabsf(rhs.x), fmaxf(fabsf(rhs.y), fabsf(rhs.z)));
         }
         mx = warp_max(mx);
-        if (lane == 0) sm.part[(sl - first) * RS] = mx;
+        if (lane == 0) sm.part[(sl - first) * 3] = mx;
     }
     float* const buf0 = a.seg_part;
-    float* const buf1 = a.seg_part + (size_t)a.nseg * RS;
+    float* const buf1 = a.seg_part + (size_t)a.nseg * 3;
     auto set_scale = [&](int s) {
-        const float mxs = sm.tot[s * RS];
+        const float mxs = sm.tot[s * 3];
         sm.st[s].scale = rhs_scale(mxs);
         sm.st[s].zero = mxs == 0.0f;
     };
-    if (!reduce_across_grid<RS>(a, sm, buf0, 1, true, first, last, epoch, &s_ok, nullptr, set_scale)) return;
+    if (!reduce_across_grid(a, sm, buf0, 1, true, first, last, epoch, &s_ok, nullptr, set_scale)) return;
 
     // ---------------- phase 1: normalise, initial residual and preconditioned residual
     for (int sl = first + warp; sl < last; sl += W) {
@@ -749,22 +738,20 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         rz = warp_sum(rz);
         bb = warp_sum(bb);
         if (lane == 0) {
-            float* p = sm.part + (sl - first) * RS;
+            float* p = sm.part + (sl - first) * 3;
             p[0] = rr; p[1] = rz; p[2] = bb;
         }
     }
     auto start_cg = [&](int s) {
         SceneState& st = sm.st[s];
-        st.rr = sm.tot[s * RS];
-        st.rz = sm.tot[s * RS + 1];
-        st.bb = sm.tot[s * RS + 2];
+        st.rr = sm.tot[s * 3];
+        st.rz = sm.tot[s * 3 + 1];
+        st.bb = sm.tot[s * 3 + 2];
         st.atol_sq = (double)a.tol * (double)a.tol * st.bb;
         st.iters = 0;
         st.beta = 0.0f;
         st.alpha = 0.0f;
         st.primed = 0;
-        st.final = 0;
-        st.last = 0;
         st.active = (st.rr > st.atol_sq) && (a.maxiter > 0);
         if (!isfinite(st.rr)) {
             st.active = 0;
@@ -772,7 +759,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         }
         if (st.active) atomicOr(&s_any, 1);
     };
-    if (!reduce_across_grid<RS>(a, sm, buf1, 3, false, first, last, epoch, &s_ok, &s_any, start_cg)) return;
+    if (!reduce_across_grid(a, sm, buf1, 3, false, first, last, epoch, &s_ok, &s_any, start_cg)) return;
 
     // ---------------- CG iterations
     if constexpr (V == 0) {
@@ -815,11 +802,11 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 pap = dot3(pc, acc);
             }
             pap = warp_sum(pap);
-            if (lane == 0) sm.part[(sl - first) * RS] = pap;
+            if (lane == 0) sm.part[(sl - first) * 3] = pap;
         }
         auto set_alpha = [&](int s) {
             SceneState& st = sm.st[s];
-            if (st.active) st.alpha = (float)(st.rz / sm.tot[s * RS]);
+            if (st.active) st.alpha = (float)(st.rz / sm.tot[s * 3]);
         };
         if (a.cta_time != nullptr) {  // speed calibration: this CTA's SpMV-phase time
             __syncthreads();
@@ -828,7 +815,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 a.cta_time[2 * blockIdx.x + 1] += 1;
             }
         }
-        if (!reduce_across_grid<RS>(a, sm, buf0, 1, false, first, last, epoch, &s_ok, nullptr, set_alpha)) return;
+        if (!reduce_across_grid(a, sm, buf0, 1, false, first, last, epoch, &s_ok, nullptr, set_alpha)) return;
         // phase B: x += alpha p, r -= alpha y, z = M r, partial r.r and r.z
         for (int sl = first + warp; sl < last; sl += W) {
             const int4 sl4 = sm.slc[sl - first];
@@ -864,14 +851,14 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             rr = warp_sum(rr);
             rz = warp_sum(rz);
             if (lane == 0) {
-                float* p = sm.part + (sl - first) * RS;
+                float* p = sm.part + (sl - first) * 3;
                 p[0] = rr; p[1] = rz;
             }
         }
         auto next_iteration = [&](int s) {
             SceneState& st = sm.st[s];
             if (!st.active) return;
-            const double rr = sm.tot[s * RS], rz_new = sm.tot[s * RS + 1];
+            const double rr = sm.tot[s * 3], rz_new = sm.tot[s * 3 + 1];
             st.iters += 1;
             st.beta = (float)(rz_new / st.rz);
             st.rz = rz_new;
@@ -883,7 +870,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
             }
             if (st.active) atomicOr(&s_any, 1);
         };
-        if (!reduce_across_grid<RS>(a, sm, buf1, 2, false, first, last, epoch, &s_ok, &s_any, next_iteration)) return;
+        if (!reduce_across_grid(a, sm, buf1, 2, false, first, last, epoch, &s_ok, &s_any, next_iteration)) return;
     }
     } else {
     // Single-reduction (Chronopoulos-Gear) CG: one pass and one grid reduction per iteration.  Pass k
@@ -891,12 +878,9 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
     //   p = u + beta p,  s = w + beta s,  x += alpha p,  r -= alpha s,
     //   u' = u - alpha (Mw + beta Ms)  (= M r'),  Ms' = Mw + beta Ms,
     // then forms w' = A u' from the neighbours' records (u' recomputed at the gather), Mw' = M w', writes
-    // the row's next record (u', Mw', Ms') and eight partials: (r', u'), (w', u'), (r', r') and
-    // (r', w'), (r', s), (w', w'), (w', s), (s, s) with s the direction just applied.  Pass 0 only forms
-    // w0 = A u0 (alpha0 = gamma0 / delta0).  From one reduction each scene gets alpha, beta and, without
-    // another SpMV, the next residual norm ||r' - alpha (w' + beta s)||^2 expanded in those products;
-    // when it meets the tolerance (or the next update is the last allowed) that update is applied in
-    // the epilogue instead of in another pass, so the solve takes as many SpMVs as standard CG.
+    // the row's next record (u', Mw', Ms') and the partials (r', u'), (w', u'), (r', r').  Pass 0 only
+    // forms w0 = A u0 (alpha0 = gamma0 / delta0).  The convergence test of update k comes with the
+    // reduction that follows its SpMV, so a converged solve has done one SpMV more than standard CG.
     for (int pass = 0; s_any; ++pass) {
         const float4* rc = (pass & 1) ? a.rec1 : a.rec0;  // (u, Mw, Ms) of this pass
         float4* rn = (pass & 1) ? a.rec0 : a.rec1;         // written for the next one
@@ -905,7 +889,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         for (int sl = first + warp; sl < last; sl += W) {
             const int4 sl4 = sm.slc[sl - first];
             const SceneState& st = sm.st[sl4.z & ~kResidentSlice];
-            float pt[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float gam = 0.f, del = 0.f, rrl = 0.f;
             if (st.active && lane < sl4.y) {
                 const int row = sl4.x + lane;
                 const unsigned info = sm.rinfo[(sl - first) * kSlice + lane];
@@ -914,7 +898,7 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 float* rs = a.resident ? res_slot(sm, sl, first, lane, a.resident, 1) : nullptr;
                 const float4* own = rc + 3 * (size_t)row;
                 const float4 o0 = own[0];
-                float3 un, msn, r, sdir = f3(0.f, 0.f, 0.f);
+                float3 un, msn, r;
                 if (prime) {
                     un = xyz(o0);
                     msn = f3(0.f, 0.f, 0.f);
@@ -933,7 +917,6 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                     sv = f3(fmaf(beta, sv.x, wv.x), fmaf(beta, sv.y, wv.y), fmaf(beta, sv.z, wv.z));
                     x = f3(fmaf(alpha, pv.x, x.x), fmaf(alpha, pv.y, x.y), fmaf(alpha, pv.z, x.z));
                     r = f3(fmaf(-alpha, sv.x, r.x), fmaf(-alpha, sv.y, r.y), fmaf(-alpha, sv.z, r.z));
-                    sdir = sv;
                     if (rs) {
                         res3_store(rs, 0, x);
                         res3_store(rs, 3, r);
@@ -946,14 +929,6 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                         a.s4[row] = f4(sv);
                     }
                 }
-                float4* nx = rn + 3 * (size_t)row;  // u' and Ms' of the next record go out before the SpMV
-                nx[0] = make_float4(un.x, un.y, un.z, msn.x);
-                nx[2] = make_float4(msn.z, 0.f, 0.f, 0.f);
-                const float msy = msn.y;
-                pt[0] = dot3(r, un);
-                pt[2] = dot3(r, r);
-                pt[4] = dot3(r, sdir);
-                pt[7] = dot3(sdir, sdir);
                 float3 w = un;  // fixed rows: identity (their u is zero)
                 if (!(info & kFixedBit)) {
                     const int len = (int)(info & ~kFixedBit);
@@ -965,22 +940,20 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
                 const float3 mw = a.resident == 2 ? res_minv_mul(rs, w, 15) : minv_mul(a.minv, row, w);
                 if (rs) res3_store(rs, 12, w);
                 else a.w4[row] = f4(w);
-                nx[1] = make_float4(mw.x, mw.y, mw.z, msy);
-                // r and s are re-read from the row state rather than kept live across the SpMV
-                asm volatile("" ::: "memory");
-                const float3 r2 = rs ? res3(rs, 3) : xyz(a.r[row]);
-                const float3 s2 = prime ? f3(0.f, 0.f, 0.f) : (rs ? res3(rs, 9) : xyz(a.s4[row]));
-                pt[1] = dot3(w, un);
-                pt[3] = dot3(r2, w);
-                pt[5] = dot3(w, w);
-                pt[6] = dot3(w, s2);
+                float4* nx = rn + 3 * (size_t)row;
+                nx[0] = make_float4(un.x, un.y, un.z, mw.x);
+                nx[1] = make_float4(mw.y, mw.z, msn.x, msn.y);
+                nx[2] = make_float4(msn.z, 0.f, 0.f, 0.f);
+                gam = dot3(r, un);
+                del = dot3(w, un);
+                rrl = dot3(r, r);
             }
-#pragma unroll
-            for (int k = 0; k < 8; ++k) pt[k] = warp_sum(pt[k]);
+            gam = warp_sum(gam);
+            del = warp_sum(del);
+            rrl = warp_sum(rrl);
             if (lane == 0) {
-                float* pp = sm.part + (sl - first) * RS;
-#pragma unroll
-                for (int k = 0; k < 8; ++k) pp[k] = pt[k];
+                float* pp = sm.part + (sl - first) * 3;
+                pp[0] = gam; pp[1] = del; pp[2] = rrl;
             }
         }
         if (a.cta_time != nullptr) {  // speed calibration: this CTA's pass time
@@ -993,47 +966,33 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         auto next_pass = [&](int s) {
             SceneState& st = sm.st[s];
             if (!st.active) return;
-            const float* T = sm.tot + s * RS;
-            const double rr = T[2];
-            double gam = T[0];
+            const double gam = sm.tot[s * 3], del = sm.tot[s * 3 + 1], rr = sm.tot[s * 3 + 2];
             if (!st.primed) {  // gamma0 = r0.u0 came with the start reduction
                 st.primed = 1;
                 st.beta = 0.0f;
-                st.alpha = (float)(st.rz / (double)T[1]);
-                gam = st.rz;
+                st.alpha = (float)(st.rz / del);
+                if (!isfinite(st.alpha)) {
+                    st.active = 0;
+                    atomicOr(a.status, kStatusNonFinite);
+                }
             } else {
                 st.iters += 1;
                 st.rr = rr;
-                st.active = (rr > st.atol_sq) && (st.iters < a.maxiter) && isfinite(rr);
-                if (!st.active) {  // update k met the tolerance after all (or the iteration cap)
-                    if (!isfinite(rr)) atomicOr(a.status, kStatusNonFinite);
-                    return;
+                st.active = (rr > st.atol_sq) && (st.iters < a.maxiter);
+                if (!isfinite(rr)) {
+                    st.active = 0;
+                    atomicOr(a.status, kStatusNonFinite);
                 }
-                const float beta = (float)(gam / st.rz);
-                st.alpha = (float)(gam / ((double)T[1] - (double)beta * gam / (double)st.alpha));
-                st.beta = beta;
-                st.rz = gam;
-            }
-            if (!isfinite(st.alpha)) {
-                st.active = 0;
-                atomicOr(a.status, kStatusNonFinite);
-                return;
-            }
-            // ||r - alpha s'||^2 with s' = w + beta s, from the pass's products
-            const double al = st.alpha, be = st.beta;
-            const double rsd = (double)T[3] + be * (double)T[4];
-            const double ssd = (double)T[5] + 2.0 * be * (double)T[6] + be * be * (double)T[7];
-            const double rr_next = rr - 2.0 * al * rsd + al * al * ssd;
-            if (rr_next <= st.atol_sq || st.iters + 1 >= a.maxiter) {  // the next update is the last
-                st.active = 0;
-                st.final = 1;
-                st.last = pass;
-                st.iters += 1;
-                st.rr = rr_next > 0.0 ? rr_next : 0.0;
+                if (st.active) {
+                    const float beta = (float)(gam / st.rz);
+                    st.alpha = (float)(gam / (del - (double)beta * gam / (double)st.alpha));
+                    st.beta = beta;
+                    st.rz = gam;
+                }
             }
             if (st.active) atomicOr(&s_any, 1);
         };
-        if (!reduce_across_grid<RS>(a, sm, (pass & 1) ? buf1 : buf0, 8, false, first, last, epoch, &s_ok, &s_any,
+        if (!reduce_across_grid(a, sm, (pass & 1) ? buf1 : buf0, 3, false, first, last, epoch, &s_ok, &s_any,
                                 next_pass))
             return;
     }
@@ -1047,15 +1006,6 @@ __global__ void __launch_bounds__(kPcgMaxThreads, 1) pcg_kernel(PcgArgs a) {
         const SceneState& st = sm.st[sl4.z & ~kResidentSlice];
         int row = meta.x + lane;
         float3 dv = a.resident ? res3(res_slot(sm, sl, first, lane, a.resident, V), 0) : xyz(a.x[row]);
-        if constexpr (V == 1) {
-            if (st.final) {  // the scene's last update: p = u + beta p, x += alpha p
-                const float4* rec = ((st.last + 1) & 1) ? a.rec1 : a.rec0;
-                const float3 u = xyz(rec[3 * (size_t)row]);
-                const float3 po = a.resident ? res3(res_slot(sm, sl, first, lane, a.resident, V), 6) : xyz(a.p4[row]);
-                const float3 pv = f3(fmaf(st.beta, po.x, u.x), fmaf(st.beta, po.y, u.y), fmaf(st.beta, po.z, u.z));
-                dv = f3(fmaf(st.alpha, pv.x, dv.x), fmaf(st.alpha, pv.y, dv.y), fmaf(st.alpha, pv.z, dv.z));
-            }
-        }
         float sc = st.scale;
         dv = f3(dv.x / sc, dv.y / sc, dv.z / sc);
         store3(a.dv, row, dv);
