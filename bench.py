@@ -57,9 +57,10 @@ def parse():
     p.add_argument("--no-batched", action="store_true", help="skip the 256-scene batched vs plain measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-beam gradient measurement")
     p.add_argument("--no-tet", action="store_true", help="skip the jittered Tet4 48^3 measurement")
-    p.add_argument("--profile-workload", choices=("batched", "tet"), default=None,
-                   help="run only --steps eager frames of the 256-scene batch or the jittered Tet4 48^3 block, "
-                        "print their time, and exit (a target for ncu launch lists; no JSON line)")
+    p.add_argument("--profile-workload", choices=("batched", "tet", "hex"), default=None,
+                   help="run only --steps eager frames of the 256-scene batch, the jittered Tet4 48^3 block or the "
+                        "Hex8 block (--cells), print their time and the CG iterations of every PCG launch, and exit "
+                        "(a target for ncu captures; no JSON line)")
     p.add_argument("--trace-iterations", action="store_true",
                    help="print the CG iterations of every PCG launch of the eager warm-up frame to stderr "
                         "(maps an ncu launch index to its iteration count)")
@@ -819,13 +820,16 @@ def standalone_spmv(solver, lib, P: int, nnzb: int, peak: float) -> dict:
             "unit": "GB/s", "frac": gbs / peak, "column_index_bytes": col}
 
 
-def profile_workload(name: str, steps: int) -> None:
-    """Eager frames (tangent refresh + substeps) of one secondary workload, for profiling."""
+def profile_workload(name: str, steps: int, cells: int = 64) -> None:
+    """Eager frames (tangent refresh + substeps) of one workload, for profiling; prints the CG
+    iterations of every PCG launch in launch order (maps an ncu launch index to its iteration count)."""
     import torch
 
     from newton_solver_fem_gb300 import scenes
 
-    if name == "batched":
+    if name == "hex":
+        sc, model, solver, _ = build_workload(cells, "cuda:0")
+    elif name == "batched":
         sc = scenes.batched_scenes()
         model, solver = scene_solver(sc, "cuda:0", sc.scene_offsets)
     else:
@@ -843,13 +847,16 @@ def profile_workload(name: str, steps: int) -> None:
     a, b = model.state(), model.state()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
+    iterations = []
     for _ in range(steps):
         solver.refresh_tangent(a.particle_q)
         for _ in range(sc.substeps):
             solver.step(a, b, None, None, sc.dt)
+            iterations.append(solver.stats()["max_iterations"])  # synchronises: launch order is preserved
             a, b = b, a
     e1.record()
     torch.cuda.synchronize()
+    print(json.dumps({"pcg_launch_iterations": iterations}), file=sys.stderr)
     print(f"{name}: {steps} eager frames, {e0.elapsed_time(e1) / max(1, steps):.3f} ms per frame, "
           f"{model.particle_count} nodes, last substep max CG iterations {solver.stats()['max_iterations']}",
           file=sys.stderr)
@@ -858,7 +865,7 @@ def profile_workload(name: str, steps: int) -> None:
 def main():
     args = parse()
     if args.profile_workload is not None:
-        profile_workload(args.profile_workload, args.steps)
+        profile_workload(args.profile_workload, args.steps, args.cells)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -36,6 +36,7 @@ FEM_TUNE_TAIL_PREFETCH = 11
 FEM_TUNE_COMPACT_COLUMNS = 12
 FEM_TUNE_UNIFORM_COLUMN_BLOCKS = 13
 FEM_TUNE_CG_VARIANT = 14
+FEM_TUNE_OPERATOR_BATCH = 15
 
 FEM_TERM_SPRING = 1
 FEM_TERM_TET = 2

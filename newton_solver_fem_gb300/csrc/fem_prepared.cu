@@ -116,7 +116,9 @@ __global__ void prepared_rhs_kernel(int P, const float* __restrict__ impulse, co
 // the blocks through the non-coherent path without L1 allocation, and the
 // fixed columns read from a per-(slice, k) lane mask rather than from each
 // column's row info.
-constexpr int kOperatorBatch = 4;
+// kOperatorBatch block columns in flight per thread: 4 at 48 registers (five 256-thread CTAs per SM), or
+// 2 at 32 registers (eight CTAs, 64 warps per SM), which holds a 64^3 Hex8 matrix's 8,582 slices in one
+// wave on 152 SMs (FEM_TUNE_OPERATOR_BATCH).
 __device__ __forceinline__ float4 ld_stream4(const float4* p) {
     float4 v;
     asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
@@ -127,7 +129,8 @@ __device__ __forceinline__ float ld_stream1(const float* p) {
     asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
     return v;
 }
-__global__ void __launch_bounds__(256) apply_operator_kernel(
+template <int kOperatorBatch>
+__global__ void __launch_bounds__(256, kOperatorBatch == 2 ? 8 : 5) apply_operator_kernel(
     int nslices, const int* __restrict__ slice_ptr, const int2* __restrict__ meta,
     const unsigned* __restrict__ row_info, const float4* __restrict__ valA, const float4* __restrict__ valB,
     const float* __restrict__ valC, const int* __restrict__ scol, const short* __restrict__ dcol,
@@ -282,7 +285,8 @@ int fem_apply_operator(FemHandle* H, const float* x, float* y, void* stream) {
     Handle& h = H->h;
     if (h.P == 0 || h.nslices == 0) return FEM_OK;
     fem::Guard g(H->device);
-    fem::apply_operator_kernel<<<fem::blocks((int64_t)h.nslices * 32, 256), 256, 0, (cudaStream_t)stream>>>(
+    auto kern = h.operator_batch == 2 ? fem::apply_operator_kernel<2> : fem::apply_operator_kernel<4>;
+    kern<<<fem::blocks((int64_t)h.nslices * 32, 256), 256, 0, (cudaStream_t)stream>>>(
         h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.scol, h.dcol, h.fixcol, x, y);
     return fem::report_cuda(cudaGetLastError());
 }
