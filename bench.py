@@ -75,17 +75,22 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def dram_traffic_per_launch():
-    """Per-launch DRAM bytes of the PCG kernel from the committed ncu summary, if present."""
-    path = ROOT / "profiles" / "pcg_kernel_hex8_64.md"
+def dram_traffic_per_launch(iterations: float):
+    """Measured DRAM bytes (read + write) of one PCG launch at this mean iteration count.
+
+    From the committed ncu summary of two full 64^3 launches (18 and 22 CG iterations):
+    ``dram_bytes_fit: <prologue+epilogue bytes> <bytes per iteration>``.  None when absent.
+    """
+    path = ROOT / "profiles" / "pcg_kernel_hex8_64_dram.md"
     if not path.exists():
         return None
     for line in path.read_text().splitlines():
-        if line.strip().startswith("dram_bytes_per_launch_full_size:"):
+        if line.strip().startswith("dram_bytes_fit:"):
             try:
-                return float(line.split(":", 1)[1].strip().split()[0])
+                base, per_iter = (float(v) for v in line.split(":", 1)[1].split()[:2])
             except ValueError:
                 return None
+            return base + per_iter * iterations
     return None
 
 
@@ -622,12 +627,32 @@ def run_gb300(args) -> None:
     build.build()
     sc, model, solver, np = build_workload(args.cells, device)
     lib = _lib.load()
-    # split the PCG rows over the CTAs by their measured SpMV speed (a public tuning key;
-    # about 1% on this workload, deterministic for the handle)
-    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_BALANCE, 1))
     P = model.particle_count
     info = solver.matrix_info()
     s0, s1 = model.state(), model.state()
+    # the project's autotuner picks the PCG launch variant (staging depth, rows per CTA, CG recurrence)
+    # on this workload, timing each candidate's launches from the same initial state
+    from newton_solver_fem_gb300 import autotune
+
+    q_start, v_start = model.particle_q.clone(), model.particle_qd.clone()
+
+    def tune_restore():
+        s0.particle_q.copy_(q_start)
+        s0.particle_qd.copy_(v_start)
+        solver.reset()
+
+    def tune_frame():
+        a, b = s0, s1
+        solver.refresh_tangent(a.particle_q)
+        for _ in range(sc.substeps):
+            solver.step(a, b, None, None, sc.dt)
+            a, b = b, a
+
+    tuned = autotune.autotune(solver, tune_frame, tune_restore, frames=2, use_cache=False)
+    tune_restore()
+    # then split the PCG rows over the CTAs by their measured SpMV speed (a public tuning key;
+    # about 1% on this workload, deterministic for the handle)
+    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_BALANCE, 1))
     substeps = sc.substeps
     stream = torch.cuda.Stream(device)
 
@@ -715,9 +740,11 @@ def run_gb300(args) -> None:
     bytes_launch = pcg_launch_bytes(info["nnzb"], P, iters, col_bytes)
     achieved = bytes_launch / (launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
-    traffic = dram_traffic_per_launch()
+    traffic = dram_traffic_per_launch(iters) if args.cells == 64 else None
 
+    op_tuned = autotune.tune_operator(solver)  # standalone SpMV: block columns in flight per thread
     spmv = standalone_spmv(solver, lib, P, info["nnzb"], peak)
+    spmv["operator_batch"] = op_tuned
 
     # ---- end to end through the public API with host buffers
     host_q = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
@@ -761,12 +788,19 @@ def run_gb300(args) -> None:
                        "cg_maxiter": sc.maxiter, "preconditioner": "block_diag", "parallelism": "replicas",
                        "nnzb": info["nnzb"], "mean_cg_iterations": timed_iterations,
                        "frames": f"0..{args.steps - 1} from the initial state (reset after warm-up)",
+                       "autotuned": {"choice": {k: tuned[k] for k in ("unroll", "threads", "cg_variant", "grid")},
+                                     "us_per_cg_iteration": {
+                                         f"u{r['unroll']}_t{r['threads']}_v{r['cg_variant']}":
+                                             round(r["us_per_iteration"], 2) for r in tuned["candidates"]}},
                        "launch": launch_shape(solver),
                        "pcg_split": "rows split over CTAs by calibrated SpMV speed (FEM_TUNE_BALANCE=1)",
                        "column_mode": int(cc.value), "column_index_bytes": round(col_bytes, 4),
                        "l2": "inputs larger than L2 (A values 259 MB, element blocks 614 MB at 64^3)"},
             "roofline": {"kernel": "pcg_kernel", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of two full 64^3 launches "
+                                           "(18 and 22 CG iterations), linear in the iteration count, at this run's "
+                                           "mean (profiles/pcg_kernel_hex8_64_dram.md)" if traffic else None,
                          "bytes_per_launch": bytes_launch, "launch_ms": launch_ms, "launches": launches},
             "spmv": spmv,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 12 * P,

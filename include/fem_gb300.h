@@ -203,9 +203,9 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
 #define FEM_TUNE_CG_VARIANT 14       /* CG recurrence of the persistent PCG: 0 standard (two grid reductions per
                                         iteration); 1 Chronopoulos-Gear (one reduction per iteration; neighbours'
                                         next preconditioned residual recomputed at every gathered column) */
-#define FEM_TUNE_OPERATOR_BATCH 15   /* fem_apply_operator: block columns loaded before any is used, per thread: 4 at
-                                        48 registers (5 CTAs of 256 threads per SM, the default) or 2 at 32 registers
-                                        (8 CTAs per SM) */
+#define FEM_TUNE_OPERATOR_BATCH 15   /* fem_apply_operator: block columns loaded before any is used, per thread: 2 at
+                                        32 registers (8 CTAs of 256 threads per SM, the default: a 64^3 Hex8 matrix in
+                                        one wave, 51 us) or 4 at 48 registers (5 CTAs per SM: 1.4 waves, 63 us) */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);

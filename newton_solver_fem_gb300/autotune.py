@@ -1,17 +1,33 @@
-"""Autotuner for the persistent PCG kernel's launch variant.
+"""Autotuner for the persistent PCG kernel's launch variant and the standalone SpMV.
 
-Tunables (``fem_set_tuning``): the SpMV unroll (block columns in flight per
-thread: 1, 2, 4), the threads per persistent CTA (256, 512, 1024: the grid is
-as many CTAs as stay co-resident) and the matrix bytes loaded with the L2
-evict_last policy.  Pinning part of a matrix larger than L2 lost every time,
-and pinning a whole matrix that fits won, so the default candidates use the
-automatic rule (-2: the whole matrix when it fits in 60% of L2, else none).
+PCG axes (``fem_set_tuning`` keys):
+
+* staging depth -- ``FEM_TUNE_SPMV_UNROLL``: block columns whose loads are in
+  flight per thread before any is used (1, 2, 4);
+* rows per CTA -- ``FEM_TUNE_CTA_THREADS``: 256, 512 or 1024 threads per
+  persistent CTA; the grid is as many CTAs as stay co-resident, so this sets
+  how many 32-row slices each CTA owns (its share of the rows and of the grid
+  reductions);
+* the CG recurrence -- ``FEM_TUNE_CG_VARIANT``: standard (two grid reductions
+  per iteration) or single-reduction Chronopoulos-Gear;
+* the matrix bytes held in L2 (``FEM_TUNE_L2_RESIDENT_BYTES``): the automatic
+  rule (-2: the whole matrix when it fits in 60% of L2, else none) won every
+  measurement, so candidates keep it.
+
+Warps per row: the matrix is SELL-32 with one lane per row (a warp streams the
+same column slot of 32 rows, coalesced), so each row has exactly one thread;
+the staging depth is the knob that sets how much of a row is in flight.
+
 For a solver and a frame function the tuner restores the same initial state
 for every candidate, runs one warm-up frame, then times the PCG launches of
 ``frames`` eager frames with per-launch CUDA events.  It scores each candidate
 by microseconds per CG iteration, so that candidates with different iteration
 counts compare fairly, and applies the best one.  Results are cached in a JSON
 file keyed by GPU name and problem signature (nodes, stored blocks, scenes).
+
+The standalone SpMV (``fem_apply_operator``) has its own axis,
+``FEM_TUNE_OPERATOR_BATCH`` (block columns in flight per thread: 2 at 32
+registers or 4 at 48); ``tune_operator`` times both after an L2 flush.
 
 Command line (prints one JSON record per candidate, then the choice)::
 
@@ -24,14 +40,24 @@ import argparse
 import ctypes
 import json
 import os
+import statistics
 from pathlib import Path
 
 import torch
 
 from . import _lib
 
-# (unroll, CTA threads, L2-resident bytes)
-DEFAULT_CANDIDATES = [(u, t, -2) for t in (1024, 512, 256) for u in (4, 2)] + [(1, 1024, -2)]
+AXES = {
+    "unroll": _lib.FEM_TUNE_SPMV_UNROLL,
+    "threads": _lib.FEM_TUNE_CTA_THREADS,
+    "cg_variant": _lib.FEM_TUNE_CG_VARIANT,
+    "resident_bytes": _lib.FEM_TUNE_L2_RESIDENT_BYTES,
+}
+# every staging depth at every CTA size with the standard recurrence, plus the single-reduction
+# recurrence at the default shape
+DEFAULT_CANDIDATES = [dict(unroll=u, threads=t, cg_variant=0, resident_bytes=-2)
+                      for t in (1024, 512, 256) for u in (4, 2, 1)] + \
+                     [dict(unroll=u, threads=1024, cg_variant=1, resident_bytes=-2) for u in (4, 2)]
 CACHE = Path(os.environ.get("FEM_GB300_TUNE_CACHE", Path.home() / ".cache" / "fem_gb300_tune.json"))
 
 
@@ -41,19 +67,18 @@ def _key(solver) -> str:
     return f"{name}|P={solver.model.particle_count}|blocks={info['stored_blocks']}|S={solver.model.scene_count}"
 
 
-def apply(solver, unroll: int, threads: int, resident_bytes: int) -> None:
+def apply(solver, choice: dict) -> None:
+    """Set every tuning key named in ``choice`` (axis name -> value)."""
     lib = _lib.load()
-    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_SPMV_UNROLL, int(unroll)))
-    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_CTA_THREADS, int(threads)))
-    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_L2_RESIDENT_BYTES, int(resident_bytes)))
+    for name, value in choice.items():
+        if name in AXES:
+            _lib.check(lib.fem_set_tuning(solver._handle, AXES[name], int(value)))
 
 
 def current(solver) -> dict:
     lib = _lib.load()
     out = {}
-    for name, key in (("unroll", _lib.FEM_TUNE_SPMV_UNROLL), ("threads", _lib.FEM_TUNE_CTA_THREADS),
-                      ("resident_bytes", _lib.FEM_TUNE_L2_RESIDENT_BYTES),
-                      ("resident_slices", _lib.FEM_TUNE_RESIDENT_SLICES), ("grid", _lib.FEM_TUNE_GRID)):
+    for name, key in (*AXES.items(), ("resident_slices", _lib.FEM_TUNE_RESIDENT_SLICES), ("grid", _lib.FEM_TUNE_GRID)):
         v = ctypes.c_int64()
         _lib.check(lib.fem_get_tuning(solver._handle, key, ctypes.byref(v)))
         out[name] = v.value
@@ -82,7 +107,8 @@ def measure(solver, frame, restore, frames: int = 3) -> dict:
 
 def autotune(solver, frame, restore, candidates=None, frames: int = 3, use_cache: bool = True,
              verbose: bool = False) -> dict:
-    """Pick and apply the fastest (unroll, CTA threads, resident bytes) for this solver; returns the record."""
+    """Pick and apply the fastest PCG launch variant for this solver; returns the chosen record with the
+    measured records of every candidate under ``"candidates"``."""
     key = _key(solver)
     cache = {}
     if use_cache and CACHE.exists():
@@ -92,17 +118,18 @@ def autotune(solver, frame, restore, candidates=None, frames: int = 3, use_cache
             cache = {}
     if use_cache and key in cache:
         best = cache[key]
-        apply(solver, best["unroll"], best.get("threads", 1024), best["resident_bytes"])
+        apply(solver, {k: v for k, v in best.items() if k in AXES})
         return best
     records = []
-    for unroll, threads, resident in candidates or DEFAULT_CANDIDATES:
-        apply(solver, unroll, threads, resident)
+    for cand in candidates or DEFAULT_CANDIDATES:
+        apply(solver, cand)
         rec = {**current(solver), **measure(solver, frame, restore, frames)}
         records.append(rec)
         if verbose:
             print(json.dumps(rec), flush=True)
-    best = min(records, key=lambda r: r["us_per_iteration"])
-    apply(solver, best["unroll"], best["threads"], best["resident_bytes"])
+    best = dict(min(records, key=lambda r: r["us_per_iteration"]))
+    apply(solver, {k: v for k, v in best.items() if k in AXES})
+    best["candidates"] = records
     if use_cache:
         cache[key] = best
         try:
@@ -111,6 +138,42 @@ def autotune(solver, frame, restore, candidates=None, frames: int = 3, use_cache
         except OSError:
             pass
     return best
+
+
+def time_operator(solver, repeats: int = 21) -> float:
+    """Median microseconds of one fem_apply_operator after an L2 flush (write, then a clean read)."""
+    lib = _lib.load()
+    P = solver.model.particle_count
+    g = torch.Generator(device=solver.device).manual_seed(0)
+    x = torch.randn((P, 3), device=solver.device, generator=g)
+    y = torch.empty_like(x)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=solver.device)
+    clean = torch.ones(128 << 20, dtype=torch.float32, device=solver.device)
+    stream = torch.cuda.current_stream(solver.device)
+    times = []
+    for _ in range(repeats):
+        flush.fill_(1)
+        clean.sum()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(lib.fem_apply_operator(solver._handle, x.data_ptr(), y.data_ptr(), stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return 1e3 * statistics.median(times[1:])
+
+
+def tune_operator(solver, batches=(2, 4), timer=None) -> dict:
+    """Pick and apply the fastest FEM_TUNE_OPERATOR_BATCH; returns {"operator_batch", "us", "candidates"}."""
+    lib = _lib.load()
+    timer = timer or time_operator
+    records = []
+    for b in batches:
+        _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_BATCH, int(b)))
+        records.append({"operator_batch": int(b), "us": timer(solver)})
+    best = min(records, key=lambda r: r["us"])
+    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_BATCH, best["operator_batch"]))
+    return {**best, "candidates": records}
 
 
 def main():
@@ -144,7 +207,8 @@ def main():
             a, b = b, a
 
     best = autotune(solver, frame, restore, frames=args.frames, use_cache=False, verbose=True)
-    print(json.dumps({"best": best}))
+    op = tune_operator(solver)
+    print(json.dumps({"best": {k: v for k, v in best.items() if k != "candidates"}, "operator": op}))
 
 
 if __name__ == "__main__":

@@ -116,9 +116,10 @@ __global__ void prepared_rhs_kernel(int P, const float* __restrict__ impulse, co
 // the blocks through the non-coherent path without L1 allocation, and the
 // fixed columns read from a per-(slice, k) lane mask rather than from each
 // column's row info.
-// kOperatorBatch block columns in flight per thread: 4 at 48 registers (five 256-thread CTAs per SM), or
-// 2 at 32 registers (eight CTAs, 64 warps per SM), which holds a 64^3 Hex8 matrix's 8,582 slices in one
-// wave on 152 SMs (FEM_TUNE_OPERATOR_BATCH).
+// kOperatorBatch block columns in flight per thread (FEM_TUNE_OPERATOR_BATCH): 2 at 32 registers (eight
+// 256-thread CTAs, 64 warps per SM) holds a 64^3 Hex8 matrix's 8,582 slices in one wave on 152 SMs and
+// streams it in 51 us (0.82 of the measured copy bandwidth); 4 at 48 registers (five CTAs per SM) needs
+// 1.4 waves, and its half-empty second wave takes it to 63 us.
 __device__ __forceinline__ float4 ld_stream4(const float4* p) {
     float4 v;
     asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
