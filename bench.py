@@ -533,7 +533,9 @@ def adjoint_measurement(device: str, repeats: int) -> dict:
         "checkpointed_gradient_value": dof_substeps / med["gradient_s"],
         "gradient_over_plain": med["gradient_s"] / med["plain_s"],
         "recompute": "overlapped on a second handle and stream" if rollout.overlap is not None else "in line",
-        "finite": bool(torch.isfinite(g["mu_scale"]).all()) and bool(torch.isfinite(loss)),
+        "plain_cg_iterations_last_substep": solver.stats()["max_iterations"],
+        "finite": bool(torch.isfinite(g["mu_scale"]).all()) and bool(torch.isfinite(loss))
+                  and bool(torch.isfinite(a.particle_q).all()),
         "timer": "wall clock around synchronised passes, median of repeats", "repeats": max(1, repeats),
     }
 

@@ -177,7 +177,8 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
                                         -2 (default) = the whole matrix when it fits in 60% of L2, else none */
 #define FEM_TUNE_RESIDENT_SLICES 3   /* read-only: resulting number of L2-resident 32-row slices */
 #define FEM_TUNE_GRID 4              /* read-only: cooperative grid size */
-#define FEM_TUNE_CTA_THREADS 5       /* threads per PCG CTA: 256, 512, 1024, or 0 = automatic (default): 1024 when there are
+#define FEM_TUNE_CTA_THREADS 5       /* threads per PCG CTA: 256, 512, 1024, or 0 = automatic (default): one CTA with a
+                                        warp per slice for at most 32 slices (no grid barriers), 1024 when there are
                                         at least 8 slices per SM (then at least one CTA per SM), else 256; the
                                         getter returns the size in use */
 #define FEM_TUNE_GRID_CAP 6          /* upper bound on the PCG grid (0 = as many CTAs as fit, the default) */

@@ -473,7 +473,9 @@ __device__ bool reduce_across_grid(const PcgArgs& a, const Smem& sm, float* buf,
             for (int t = 0; t < sm.nsc; ++t) write_segment(a, sm, buf, nv, is_max, first, t, lane);
         __syncwarp();
         int ok = 1;
-        if (lane == 0) ok = arrive_and_wait(a.barrier, gridDim.x, epoch, a.status, a.limit_ns);
+        // a one-CTA grid needs no grid barrier: the CTA barrier or warp order above already orders
+        // every partial before it is read
+        if (lane == 0 && gridDim.x > 1) ok = arrive_and_wait(a.barrier, gridDim.x, epoch, a.status, a.limit_ns);
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (ok && S <= kWarpReducedScenes) {
             for (int sc = 0; sc < S; ++sc) {
@@ -1081,7 +1083,11 @@ cudaError_t pcg_configure(Handle& h) {
     // CTAs make the grid reductions cheaper: on a 3,677-slice Tet4 system 115
     // such CTAs beat 460 of 256 threads by 8% per CG iteration); small systems
     // keep 256-thread CTAs, whose CTA barriers are cheaper than a wide CTA's.
-    const int threads = h.pcg_threads > 0 ? h.pcg_threads : (h.nslices >= 8 * sms ? 1024 : 256);
+    // Automatic CTA size.  A system of at most 32 slices (32 x 32 rows) runs as one CTA with a warp per
+    // slice, so every reduction is a CTA barrier instead of a grid barrier: on the 425-node beam a CG
+    // iteration is latency-bound, and the grid barrier's L2 round trips were most of it.
+    const int threads = h.pcg_threads > 0 ? h.pcg_threads
+                        : (h.nslices <= 32 ? std::max(64, 32 * h.nslices) : (h.nslices >= 8 * sms ? 1024 : 256));
     h.pcg_threads_used = threads;
     const int warps_per_cta = threads / 32;
     // One configuration: the grid only shrinks from pass to pass (a smaller grid
@@ -1097,7 +1103,7 @@ cudaError_t pcg_configure(Handle& h) {
         // wide CTAs on a system too small to give every SM one slice per warp:
         // one CTA per SM anyway, with fewer slices each (on 3,677 slices, 152 CTAs
         // take 16.3 us per CG iteration against 18.1 us for 115)
-        if (threads == 1024 && grid < sms) grid = std::min(sms, h.nslices);
+        if (threads == 1024 && grid < sms && h.nslices > 32) grid = std::min(sms, h.nslices);
         if (grid < 1) grid = 1;
         if (h.grid_cap > 0 && grid > h.grid_cap) grid = h.grid_cap;
         for (int pass = 0;; ++pass) {
