@@ -570,103 +570,280 @@ __global__ void __launch_bounds__(kTetTangentThreads) tet_tangent_kernel(
     }
 }
 
-constexpr int kHexPerCta = 4;
+// Hex8 tangent (reference kernels.py:1609-1747):
+//   K_ab = h^2 sum_g [c1 (gN_a . gN_b) I + c2 (F gN_a)(F gN_b)^T + c3 (cof F gN_a)(cof F gN_b)^T],
+// c1 = k_mu s w_g, c2 = 2 k_mu w_g / (Ic + 1)^2, c3 = k_lambda w_g, with F, the stretch clamp and
+// cof F formed once per Gauss point.  Every term is an outer product of per-(point, node) vectors,
+// so with r = h (sqrt|c1| gN_a, sqrt|c2| F gN_a, sqrt|c3| cof F gN_a) the block is
+//   K_ab = sum_g [(r1_a . r1_b) I + r2_a r2_b^T + r3_a r3_b^T]   (signs of c applied when negative).
+// A CTA takes kTanHex hexes:
+//   phase 0  the hexes' node positions and the Gauss table are staged in shared memory;
+//   phase 1  one thread per (hex, point) forms gN_a, F, the clamp, cof F and the eight 9-float
+//            records r of its point (no work repeated across lanes);
+//   phase 2  one thread per 2x2 tile of blocks on or above the block diagonal (10 tiles per
+//            hex) sums its four blocks over the 8 points; a tile off the diagonal also gives
+//            the four transposed blocks below it (K_ba = K_ab^T term by term, so A is
+//            exactly symmetric).  Threads are tile-major (16 hexes per tile), so a quarter
+//            warp reads 8 hexes' records in 8 distinct bank groups and a diagonal tile's half
+//            warp skips its column-side loads;
+//   phase 3  the 64 blocks per hex are staged in shared memory in the triplet planes' layout
+//            (hexes padded apart so the staging stores are conflict-free) and written out by
+//            bulk asynchronous copies (cp.async.bulk), one per hex and plane.
+constexpr int kTanHex = 16;
+constexpr int kTanTiles = 10;
+constexpr int kTanThreads = kTanHex * kTanTiles;
+constexpr int kTanRec = 12;                                // words per record (9 used)
+constexpr int kTanPointStride = 8 * kTanRec + 4;           // padded: the 8 points of a hex in distinct banks
+constexpr int kTanHexStride = 8 * kTanPointStride + 4;     // padded: hexes of a warp in distinct banks
+constexpr int kTanTabStride = 28;                          // padded Gauss table row
+constexpr int kTanSgnStride = 9;                           // padded per-hex row of point signs
+constexpr int kTanOut4Stride = 65;                         // staged float4 blocks per hex (padded)
+constexpr int kTanOut1Stride = 68;                         // staged last-entry floats per hex (padded)
+constexpr size_t kTanRecBytes = sizeof(float) * kTanHex * kTanHexStride;
+constexpr size_t kTanOutA = 0, kTanOutB = 16 * kTanOut4Stride * kTanHex, kTanOutC = 2 * kTanOutB;
+constexpr size_t kTanXOff = kTanRecBytes;
+constexpr size_t kTanSgnOff = kTanXOff + 16 * 8 * kTanHex;
+constexpr size_t kTanTabOff = kTanSgnOff + 16 * kTanSgnStride * kTanHex;
+constexpr size_t kTanSmemBytes = kTanTabOff + sizeof(float) * 8 * kTanTabStride;
+static_assert(kTanOutC + 4 * kTanOut1Stride * kTanHex <= kTanRecBytes, "output staging reuses the record area");
+static_assert((16 * kTanOut4Stride) % 16 == 0 && (4 * kTanOut1Stride) % 16 == 0, "16-byte bulk copy sources");
+static_assert(kTanRec % 4 == 0 && kTanPointStride % 4 == 0 && kTanHexStride % 4 == 0, "16-byte records");
 
-// Reference kernels.py:1609-1747.  K_ab = h^2 sum_g w_g [k_mu s (gN_a . gN_b) I
-// + coef (F gN_a)(F gN_b)^T + lambda (cof F gN_a)(cof F gN_b)^T], with F, the
-// clamp and cof F computed once per Gauss point instead of once per (a, b)
-// block.  A CTA takes kHexPerCta hexes, one thread per (hex, point g, node a):
-//   phase 1  thread (g, a) forms x_a (x) gN_a; the 8 lanes of point g sum F with
-//            a fixed xor butterfly (bit-identical in all 8 lanes), apply the
-//            clamp and cof F, and each lane stores gN_a, F gN_a and cof F gN_a
-//            of its node as packed float4 records in shared memory;
-//   phase 2  thread (a, b) accumulates its 3x3 block over the 8 points.
-// Every thread is busy in both phases; one CTA barrier separates them.
-__global__ void __launch_bounds__(256) hex_tangent_kernel(int H, const int* __restrict__ idx,
-                                                          const float* __restrict__ invJ,
-                                                          const float* __restrict__ detw,
-                                                          const float* __restrict__ mat,
-                                                          const float4* __restrict__ q4, float lo, float hi, float dt,
-                                                          int64_t trip_off, TripletPlanes vals) {
-    // The Gauss-point table is read with a different (point, node) in every
-    // lane; from constant memory that serialises, so it is staged in shared memory.
-    __shared__ float s_tab[8][8][3];
-    // per (hex, point, node): q0 = (gN.xyz, Fd.x), q1 = (Fd.yz, cd.xy), q2 = cd.z
-    __shared__ float4 s_q0[kHexPerCta][8][8];
-    __shared__ float4 s_q1[kHexPerCta][8][8];
-    __shared__ float s_q2[kHexPerCta][8][8];
-    __shared__ float4 s_c[kHexPerCta][8];  // per point: k_mu s w, coef w, lambda w
-    const int tid = threadIdx.x;
-    const int hl = tid >> 6, g = (tid >> 3) & 7, a = tid & 7;
-    const int h = blockIdx.x * kHexPerCta + hl;
-    const bool live = h < H;
-    const int64_t he = live ? h : H - 1;  // lanes past the end work on a valid hex and store nothing
-    if (tid < 192) (&s_tab[0][0][0])[tid] = (&c_dNdxi[0][0][0])[tid];
-    __syncthreads();
-    {
-        const float* iJ = invJ + (8 * he + g) * 9;
-        const float3 d = f3(s_tab[g][a][0], s_tab[g][a][1], s_tab[g][a][2]);
-        const float3 dn = f3(iJ[0] * d.x + iJ[3] * d.y + iJ[6] * d.z, iJ[1] * d.x + iJ[4] * d.y + iJ[7] * d.z,
-                             iJ[2] * d.x + iJ[5] * d.y + iJ[8] * d.z);
-        const float3 xa = xyz(q4[idx[8 * he + a]]);
-        M3 F;
-        const float xs[3] = {xa.x, xa.y, xa.z};
+__device__ __forceinline__ void tan_tile_rows(int t, int& A, int& B) {
+    // (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3) (3,3)
+    A = t < 4 ? 0 : (t < 7 ? 1 : (t < 9 ? 2 : 3));
+    B = A + t - (A == 0 ? 0 : (A == 1 ? 4 : (A == 2 ? 7 : 9)));
+}
+
+__device__ __forceinline__ void tan_load_record(const float* p, float (&r)[9]) {
+    const float4 v0 = reinterpret_cast<const float4*>(p)[0];
+    const float4 v1 = reinterpret_cast<const float4*>(p)[1];
+    r[0] = v0.x; r[1] = v0.y; r[2] = v0.z; r[3] = v0.w;
+    r[4] = v1.x; r[5] = v1.y; r[6] = v1.z; r[7] = v1.w;
+    r[8] = p[8];
+}
+
+// The four blocks (a0 + i, b0 + j) of one tile, summed over the 8 points in order; kSigned applies
+// the signs of (c1, c2, c3) to the column side.  A diagonal tile (a0 == b0) reuses its row-side
+// records.
+template <bool kSigned>
+__device__ __forceinline__ void tan_tile_sum(const float* rec_h, const float4* sgn_h, int a0, int b0,
+                                             float (&K)[4][9]) {
+    const bool diag = a0 == b0;
+    float L[4];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            F.m[i][0] = xs[i] * dn.x;
-            F.m[i][1] = xs[i] * dn.y;
-            F.m[i][2] = xs[i] * dn.z;
+    for (int t = 0; t < 4; ++t) {
+        L[t] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) K[t][k] = 0.0f;
+    }
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+        const float* pg = rec_h + g * kTanPointStride;
+        float ra[2][9], rb[2][9];
+        tan_load_record(pg + a0 * kTanRec, ra[0]);
+        tan_load_record(pg + (a0 + 1) * kTanRec, ra[1]);
+        if (!diag) {
+            tan_load_record(pg + b0 * kTanRec, rb[0]);
+            tan_load_record(pg + (b0 + 1) * kTanRec, rb[1]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                rb[0][k] = ra[0][k];
+                rb[1][k] = ra[1][k];
+            }
+        }
+        if constexpr (kSigned) {
+            const float4 s = sgn_h[g];
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    rb[j][k] *= s.x;
+                    rb[j][3 + k] *= s.y;
+                    rb[j][6 + k] *= s.z;
+                }
         }
 #pragma unroll
-        for (int off = 1; off < 8; off <<= 1)
+        for (int i = 0; i < 2; ++i)
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 2; ++j) {
+                float* k9 = K[2 * i + j];
+                float l = L[2 * i + j];
+                l = fmaf(ra[i][0], rb[j][0], l);
+                l = fmaf(ra[i][1], rb[j][1], l);
+                l = fmaf(ra[i][2], rb[j][2], l);
+                L[2 * i + j] = l;
 #pragma unroll
-                for (int j = 0; j < 3; ++j) F.m[i][j] += __shfl_xor_sync(0xffffffffu, F.m[i][j], off);
+                for (int p = 0; p < 3; ++p)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        k9[3 * p + q] = fmaf(ra[i][3 + p], rb[j][3 + q], k9[3 * p + q]);
+                        k9[3 * p + q] = fmaf(ra[i][6 + p], rb[j][6 + q], k9[3 * p + q]);
+                    }
+            }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        K[t][0] += L[t];
+        K[t][4] += L[t];
+        K[t][8] += L[t];
+    }
+}
+
+__device__ __forceinline__ void bulk_store_s2g(void* dst, const void* src, uint32_t bytes) {
+    const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(src));
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(s), "r"(bytes)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(kTanThreads, 4) hex_tangent_kernel(int H, const int* __restrict__ idx,
+                                                                      const float* __restrict__ invJ,
+                                                                      const float* __restrict__ detw,
+                                                                      const float* __restrict__ mat,
+                                                                      const float4* __restrict__ q4, float lo,
+                                                                      float hi, float dt, int64_t trip_off,
+                                                                      TripletPlanes vals) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* s_rec = reinterpret_cast<float*>(smem);
+    float4* s_x = reinterpret_cast<float4*>(smem + kTanXOff);     // [hex][node]
+    float4* s_sgn = reinterpret_cast<float4*>(smem + kTanSgnOff); // [hex][point], padded rows
+    float* s_tab = reinterpret_cast<float*>(smem + kTanTabOff);   // [point][node * 3 + axis], padded rows
+    const int tid = threadIdx.x;
+    const int64_t h0 = (int64_t)blockIdx.x * kTanHex;
+
+    // phase 0: thread (hex, k) stages node k of its hex and loads the data of Gauss point k, so that
+    // every global load of the CTA is in flight before the first barrier
+    const int64_t he = min(h0 + (tid >> 3), (int64_t)H - 1);  // past the end: a valid hex, never stored
+    float ij[9], w = 0.0f, k_mu = 0.0f, k_lambda = 0.0f;
+    if (tid < 8 * kTanHex) {
+        const int g = tid & 7;
+        s_x[tid] = q4[idx[8 * he + g]];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) ij[k] = invJ[(8 * he + g) * 9 + k];
+        w = detw[8 * he + g];
+        k_mu = mat[3 * he];
+        k_lambda = mat[3 * he + 1];
+    }
+    for (int i = tid; i < 192; i += kTanThreads) s_tab[(i / 24) * kTanTabStride + i % 24] = (&c_dNdxi[0][0][0])[i];
+    __syncthreads();
+
+    // phase 1
+    int neg = 0;
+    if (tid < 8 * kTanHex) {
+        const int hl = tid >> 3, g = tid & 7;
+        float d[24];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            const float4 v = reinterpret_cast<const float4*>(s_tab + g * kTanTabStride)[j];
+            d[4 * j] = v.x; d[4 * j + 1] = v.y; d[4 * j + 2] = v.z; d[4 * j + 3] = v.w;
+        }
+        float3 dn[8];
+        M3 F;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const float dx = d[3 * a], dy = d[3 * a + 1], dz = d[3 * a + 2];
+            dn[a] = f3(ij[0] * dx + ij[3] * dy + ij[6] * dz, ij[1] * dx + ij[4] * dy + ij[7] * dz,
+                       ij[2] * dx + ij[5] * dy + ij[8] * dz);
+            const float4 xa = s_x[hl * 8 + a];
+            const float xs[3] = {xa.x, xa.y, xa.z};
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                if (a == 0) {
+                    F.m[i][0] = xs[i] * dn[a].x;
+                    F.m[i][1] = xs[i] * dn[a].y;
+                    F.m[i][2] = xs[i] * dn[a].z;
+                } else {
+                    F.m[i][0] += xs[i] * dn[a].x;
+                    F.m[i][1] += xs[i] * dn[a].y;
+                    F.m[i][2] += xs[i] * dn[a].z;
+                }
+            }
+        }
         F = clamp_stretch(F, lo, hi);
         const float3 fc0 = col(F, 0), fc1 = col(F, 1), fc2 = col(F, 2);
         const float Ic = dot3(fc0, fc0) + dot3(fc1, fc1) + dot3(fc2, fc2);
         const float Ic1 = fmaxf(Ic + 1.0f, 1.0e-6f);
         const float sdev = 1.0f - 1.0f / Ic1;
-        const float k_mu = mat[3 * he], k_lambda = mat[3 * he + 1];
         const float coef = k_mu * 2.0f / (Ic1 * Ic1);
+        const float c1 = k_mu * sdev * w, c2 = coef * w, c3 = k_lambda * w;
+        neg = (c1 < 0.0f) || (c2 < 0.0f) || (c3 < 0.0f);
+        s_sgn[hl * kTanSgnStride + g] = make_float4(c1 < 0.0f ? -1.0f : 1.0f, c2 < 0.0f ? -1.0f : 1.0f, c3 < 0.0f ? -1.0f : 1.0f, 0.0f);
+        // h sqrt|c| per term, so that products of two records carry h^2 c
+        const float q1 = sqrtf(fabsf(c1)) * dt, q2 = sqrtf(fabsf(c2)) * dt, q3 = sqrtf(fabsf(c3)) * dt;
+        M3 Fq, Cq;
         const M3 cof = from_cols(cross3(fc1, fc2), cross3(fc2, fc0), cross3(fc0, fc1));
-        const float3 fd = mul(F, dn), cd = mul(cof, dn);
-        s_q0[hl][g][a] = make_float4(dn.x, dn.y, dn.z, fd.x);
-        s_q1[hl][g][a] = make_float4(fd.y, fd.z, cd.x, cd.y);
-        s_q2[hl][g][a] = cd.z;
-        if (a == 0) {
-            const float w = detw[8 * he + g];
-            s_c[hl][g] = make_float4(k_mu * sdev * w, coef * w, k_lambda * w, 0.0f);
-        }
-    }
-    __syncthreads();
-    if (!live) return;
-    const int ra = (tid >> 3) & 7, cb = tid & 7;
-    float K[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) K[k] = 0.0f;
-#pragma unroll
-    for (int gg = 0; gg < 8; ++gg) {
-        const float4 c = s_c[hl][gg];
-        const float4 a0 = s_q0[hl][gg][ra], a1 = s_q1[hl][gg][ra];
-        const float4 b0 = s_q0[hl][gg][cb], b1 = s_q1[hl][gg][cb];
-        const float a2 = s_q2[hl][gg][ra], b2 = s_q2[hl][gg][cb];
-        const float fa[3] = {a0.w, a1.x, a1.y}, ca[3] = {a1.z, a1.w, a2};
-        const float fb[3] = {b0.w * c.y, b1.x * c.y, b1.y * c.y}, cbv[3] = {b1.z * c.z, b1.w * c.z, b2 * c.z};
-        const float diag = c.x * (a0.x * b0.x + a0.y * b0.y + a0.z * b0.z);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) K[3 * i + j] += fa[i] * fb[j] + ca[i] * cbv[j];
-        K[0] += diag;
-        K[4] += diag;
-        K[8] += diag;
-    }
-    const float scale = dt * dt;
+            for (int j = 0; j < 3; ++j) {
+                Fq.m[i][j] = q2 * F.m[i][j];
+                Cq.m[i][j] = q3 * cof.m[i][j];
+            }
+        float* rp = s_rec + hl * kTanHexStride + g * kTanPointStride;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) K[k] *= scale;
-    store_block(vals, trip_off + 64 * (int64_t)h + 8 * ra + cb, K);
+        for (int a = 0; a < 8; ++a) {
+            const float3 fd = mul(Fq, dn[a]), cd = mul(Cq, dn[a]);
+            float4* r4 = reinterpret_cast<float4*>(rp + a * kTanRec);
+            r4[0] = make_float4(q1 * dn[a].x, q1 * dn[a].y, q1 * dn[a].z, fd.x);
+            r4[1] = make_float4(fd.y, fd.z, cd.x, cd.y);
+            rp[a * kTanRec + 8] = cd.z;
+        }
+    }
+    const int any_neg = __syncthreads_or(neg);
+
+    // phase 2
+    const int tile = tid / kTanHex, hl = tid - tile * kTanHex;
+    int A, B;
+    tan_tile_rows(tile, A, B);
+    const int a0 = 2 * A, b0 = 2 * B;
+    float K[4][9];
+    if (any_neg)
+        tan_tile_sum<true>(s_rec + hl * kTanHexStride, s_sgn + hl * kTanSgnStride, a0, b0, K);
+    else
+        tan_tile_sum<false>(s_rec + hl * kTanHexStride, s_sgn + hl * kTanSgnStride, a0, b0, K);
+    __syncthreads();  // every record is read before the staging below overwrites them
+
+    // phase 3
+    float4* s_A = reinterpret_cast<float4*>(smem + kTanOutA);
+    float4* s_B = reinterpret_cast<float4*>(smem + kTanOutB);
+    float* s_C = reinterpret_cast<float*>(smem + kTanOutC);
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float* k = K[2 * i + j];
+            const int blk = 8 * (a0 + i) + (b0 + j);
+            s_A[hl * kTanOut4Stride + blk] = make_float4(k[0], k[1], k[2], k[3]);
+            s_B[hl * kTanOut4Stride + blk] = make_float4(k[4], k[5], k[6], k[7]);
+            s_C[hl * kTanOut1Stride + blk] = k[8];
+            if (A != B) {
+                const int tr = 8 * (b0 + j) + (a0 + i);
+                s_A[hl * kTanOut4Stride + tr] = make_float4(k[0], k[3], k[6], k[1]);
+                s_B[hl * kTanOut4Stride + tr] = make_float4(k[4], k[7], k[2], k[5]);
+                s_C[hl * kTanOut1Stride + tr] = k[8];
+            }
+        }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // staged blocks visible to the bulk copies
+    __syncthreads();
+    const int nh = (int)min((int64_t)kTanHex, (int64_t)H - h0);
+    const int64_t base = trip_off + 64 * h0;
+    float* c_dst = vals.c + base;
+    const bool c_bulk = (reinterpret_cast<uintptr_t>(c_dst) & 15) == 0;
+    const int copies = c_bulk ? 3 * nh : 2 * nh;  // thread k copies plane k % 3 (or % 2) of hex k / 3 (or / 2)
+    if (tid < copies) {
+        const int per = c_bulk ? 3 : 2, hx = tid / per, plane = tid - hx * per;
+        if (plane == 0)
+            bulk_store_s2g(vals.a + base + 64 * hx, s_A + hx * kTanOut4Stride, 64 * 16);
+        else if (plane == 1)
+            bulk_store_s2g(vals.b + base + 64 * hx, s_B + hx * kTanOut4Stride, 64 * 16);
+        else
+            bulk_store_s2g(c_dst + 64 * hx, s_C + hx * kTanOut1Stride, 64 * 4);
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    }
+    if (!c_bulk)
+        for (int i = tid; i < nh * 64; i += kTanThreads) c_dst[i] = s_C[(i >> 6) * kTanOut1Stride + (i & 63)];
+    if (tid < copies) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // shared memory stays until read
 }
 
 }  // namespace
@@ -808,10 +985,13 @@ cudaError_t launch_element_tangent(Handle& h, float dt, cudaStream_t s) {
         tet_tangent_kernel<<<blocks_for(h.T, kTetTangentThreads), kTetTangentThreads, 0, s>>>(
             h.T, h.tet_idx, h.tet_pose, h.tet_mat, h.mu_scale, h.q4, h.min_stretch, h.max_stretch, dt, tet_off,
             h.trip);
-    if (h.H > 0)
-        hex_tangent_kernel<<<blocks_for(h.H, kHexPerCta), 256, 0, s>>>(
+    if (h.H > 0) {
+        cudaError_t err = allow_dynamic_smem((const void*)hex_tangent_kernel, kTanSmemBytes);
+        if (err != cudaSuccess) return err;
+        hex_tangent_kernel<<<blocks_for(h.H, kTanHex), kTanThreads, kTanSmemBytes, s>>>(
             h.H, h.hex_idx, h.hex_invJ, h.hex_detw, h.hex_mat, h.q4, h.min_stretch, h.max_stretch, dt,
             tet_off + 16 * (int64_t)h.T, h.trip);
+    }
     return cudaGetLastError();
 }
 

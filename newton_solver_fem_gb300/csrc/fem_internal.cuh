@@ -384,6 +384,10 @@ cudaError_t launch_gather(Handle& h, cudaStream_t s);
 cudaError_t launch_export_bsr(Handle& h, float* values, cudaStream_t s);
 cudaError_t launch_export_triplets(Handle& h, float* values, cudaStream_t s);
 // --- launchers (fem_pcg.cu) ---
+// Lets `kernel` launch with up to `bytes` of dynamic shared memory on the current device.  The limit is
+// a property of the kernel, shared by every handle that launches it, so it is only ever raised: setting
+// it for one handle never invalidates another handle's launch (or a captured graph's).
+cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes);
 cudaError_t pcg_configure(Handle& h);
 // Step mode (solve_rhs == nullptr): predictor, normalised PCG from the dv warm start, integration.
 // Solve mode: A x = solve_rhs from zero (projected at fixed rows), x written to x_out.

@@ -27,6 +27,9 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "fem_internal.cuh"
 #include "fem_math.cuh"
@@ -1068,6 +1071,21 @@ PcgKernel pcg_kernel_for(int unroll, int cm, int variant) {
 // only shrinks from pass to pass (a smaller grid means more slices per CTA and
 // possibly more shared memory), and the loop ends with a configuration whose
 // occupancy covers the grid.
+cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> granted;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& g = granted[{dev, kernel}];
+    if (bytes <= g) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) g = bytes;
+    return e;
+}
+
 cudaError_t pcg_configure(Handle& h) {
     int dev = 0;
     cudaError_t err = cudaGetDevice(&dev);
@@ -1123,12 +1141,9 @@ cudaError_t pcg_configure(Handle& h) {
                 if (lay.total > 227 * 1024) {
                     per_sm = 0;
                 } else {
-                    if (lay.total > 48 * 1024) {
-                        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                             (int)lay.total);
-                        if (e != cudaSuccess) return e;
-                    }
-                    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, lay.total);
+                    cudaError_t e = allow_dynamic_smem((const void*)kern, lay.total);
+                    if (e != cudaSuccess) return e;
+                    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, lay.total);
                     if (e != cudaSuccess) return e;
                 }
                 smem = lay.total;
@@ -1167,10 +1182,8 @@ cudaError_t pcg_configure(Handle& h) {
         if (err != cudaSuccess) return err;
         if (wide.grid == c.grid && wide.resident == c.resident && wide.stage == c.stage) c = wide;
     }
-    if (c.smem > 48 * 1024) {
-        err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
-        if (err != cudaSuccess) return err;
-    }
+    err = allow_dynamic_smem((const void*)kern, c.smem);
+    if (err != cudaSuccess) return err;
     h.grid = c.grid;
     h.slices_per_cta = c.L;
     h.stage_smem = c.stage;

@@ -113,6 +113,41 @@ def test_assembled_matrix_pattern_and_values(kind):
     np.testing.assert_allclose(dense, dense.T, atol=2e-8 * max(1.0, np.abs(dense).max()))
 
 
+@pytest.mark.parametrize("dims,loose", [((3, 2, 3), 0), ((5, 3, 2), 3)])
+def test_hex_tangent_tail_alignment_clamp_and_negative_lambda(dims, loose):
+    """Hex8 tangent blocks against the oracle where the kernel's special cases engage.
+
+    * The hex count (18, 30) is not a multiple of the 16 hexes a CTA takes.
+    * The first hex triplet sits at P (64 or 75 nodes with 3 loose particles): the last block plane is
+      bulk-copied when that offset is a multiple of 4 floats, else stored by threads.
+    * One node is pushed through its cell, so the stretch clamp engages (kernels.py:421-444).
+    * Half of the hexes carry a negative lambda, and one hex a negative mu; this covers the signed
+      path of the per-point factors.
+
+    The element matrix is checked to be exactly symmetric, as the tiled kernel writes it."""
+    nx, ny, nz = dims
+    x, hexes, mats, mass = scenes.hex_block(nx, ny, nz, 0.1, (0.0, 0.0, 0.0), 2e4, 0.3, 1000.0)
+    x = np.concatenate([x, 5.0 + np.arange(3 * loose, dtype=float).reshape(loose, 3)])
+    mass = np.concatenate([mass, np.full(loose, 0.01)])
+    mats = mats.copy()
+    mats[::2, 1] *= -0.5
+    mats[1, 0] *= -1.0
+    model, solver, oracle = make_pair(x, mass, hexes=hexes, hex_materials=mats, min_stretch=0.05, max_stretch=20.0)
+    q = rounded(deformed(oracle.rest))
+    corner = hexes[len(hexes) // 2, 6]
+    q[corner] = q[hexes[len(hexes) // 2, 0]] - 0.02
+    dN = O.hex_shape_gradients(oracle.hex_inv_J0)
+    F = np.einsum("hai,hgaj->hgij", q[oracle.hexes], dN).reshape(-1, 3, 3)
+    assert O.clamp_active(F, 0.05, 20.0).any()
+    solver.refresh_tangent(tensor(q))
+    oracle.refresh_tangent(q)
+    np.testing.assert_array_equal(solver.A_bsr.columns.cpu().numpy(), oracle.columns)
+    vals = to_np(solver.A_bsr.values)
+    np.testing.assert_allclose(vals, oracle.values, rtol=0, atol=1e-5 * np.abs(oracle.values).max())
+    dense = solver.A_bsr.dense()
+    assert np.array_equal(dense, dense.T)
+
+
 def test_assembly_is_bitwise_deterministic():
     sc = scenes.hex_block_64(n=6)
     model, solver, _ = scene_pair(sc)

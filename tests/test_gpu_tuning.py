@@ -149,3 +149,52 @@ def test_calibrated_split_of_a_spread_batch():
     dv2, _ = substep(model, solver, sc)
     np.testing.assert_array_equal(dv, dv2)
     assert rel_l2(dv, dv_ref) < 1e-5
+
+
+def test_handles_needing_different_pcg_shared_memory_launch_in_any_order():
+    """Two systems of 32 and 24 slices each run as one CTA (a warp per slice), whose PCG launches need
+    about 79 KB and 60 KB of dynamic shared memory, above the default 48 KB.  That limit belongs to the
+    kernel, not the handle; configuring the smaller system after the larger must leave the larger one's
+    cooperative launch (eager and graph-captured) valid, and every step must match a fresh handle."""
+    from gpu_helpers import make_pair
+
+    def pair(cells):
+        x, hexes, mats, mass = scenes.hex_block(*cells, 0.05, (0.0, 0.0, 0.0), 1e5, 0.3, 1000.0)
+        return make_pair(x, mass, hexes=hexes, hex_materials=mats, gravity=(0.0, 0.0, -9.81), with_oracle=False,
+                         linear_solver_maxiter=40, linear_solver_tolerance=1e-6)
+
+    big_model, big, _ = pair((9, 9, 9))      # 1,000 nodes: 32 slices
+    small_model, small, _ = pair((7, 7, 11))  # 768 nodes: 24 slices
+    assert setting(big, _lib.FEM_TUNE_GRID) == 1 and setting(big, _lib.FEM_TUNE_CTA_THREADS) == 1024
+    assert setting(small, _lib.FEM_TUNE_GRID) == 1 and setting(small, _lib.FEM_TUNE_CTA_THREADS) == 768
+
+    def run(model, solver, steps=3):
+        s0, s1 = model.state(), model.state()
+        solver.reset()
+        solver.refresh_tangent(s0.particle_q)
+        for _ in range(steps):
+            solver.step(s0, s1, None, None, 1.0 / 600.0)
+            s0, s1 = s1, s0
+        torch.cuda.synchronize()
+        return to_np(s0.particle_q)
+
+    q_big, q_small = run(big_model, big), run(small_model, small)
+    again_model, again, _ = pair((9, 9, 9))
+    assert np.array_equal(run(again_model, again), q_big)
+    assert np.array_equal(run(big_model, big), q_big)  # after the small handle was configured
+    assert np.array_equal(run(small_model, small), q_small)
+
+    s0, s1 = big_model.state(), big_model.state()
+    big.reset()
+    graph = torch.cuda.CUDAGraph()
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        big.refresh_tangent(s0.particle_q)
+        big.step(s0, s1, None, None, 1.0 / 600.0)  # allocations outside capture
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=stream):
+            big.step(s0, s1, None, None, 1.0 / 600.0)
+    pair((7, 7, 11))  # a third handle configured between capture and replay
+    graph.replay()
+    torch.cuda.synchronize()
+    assert np.isfinite(to_np(s1.particle_q)).all()
