@@ -17,10 +17,13 @@ namespace {
 // One thread per SELL entry: sum its contributing triplet blocks in ascending
 // triplet order.  Contributor ids and values are loaded kGatherBatch at a time
 // before any is added, so that many independent loads are in flight per thread.
+// The first P triplets are the per-node constant diagonal blocks, so an entry
+// is on the diagonal exactly when its first (smallest) contributor id is below
+// P, and that id is its row: no row or column index is read.  At most 40
+// registers, so 6 CTAs (48 warps) share an SM.
 constexpr int kGatherBatch = 4;
 
-__global__ void gather_kernel(int64_t nsell, const int* __restrict__ cptr, const int* __restrict__ contrib,
-                              const int* __restrict__ sell_row, const int* __restrict__ scol,
+__global__ void __launch_bounds__(256, 6) gather_kernel(int64_t nsell, int P, const int* __restrict__ cptr, const int* __restrict__ contrib,
                               const TripletPlanes trip, float4* __restrict__ valA, float4* __restrict__ valB,
                               float* __restrict__ valC, float* __restrict__ minv, int precond, int clear_empty) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -39,10 +42,12 @@ __global__ void gather_kernel(int64_t nsell, const int* __restrict__ cptr, const
     float b[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) b[k] = 0.0f;
+    int first = -1;
     for (int c = c0; c < c1; c += kGatherBatch) {
         int id[kGatherBatch];
 #pragma unroll
         for (int u = 0; u < kGatherBatch; ++u) id[u] = c + u < c1 ? __ldg(contrib + c + u) : -1;
+        if (c == c0) first = id[0];
         float v[kGatherBatch][9];
 #pragma unroll
         for (int u = 0; u < kGatherBatch; ++u) {
@@ -63,8 +68,8 @@ __global__ void gather_kernel(int64_t nsell, const int* __restrict__ cptr, const
     valA[e] = make_float4(b[0], b[1], b[2], b[3]);
     valB[e] = make_float4(b[4], b[5], b[6], b[7]);
     valC[e] = b[8];
-    const int row = sell_row[e];
-    if (scol[e] == row) {
+    if (first < P) {
+        const int row = first;
         float inv[9];
         if (precond == FEM_PRECOND_DIAG) inverse_point_diagonal(b, inv);
         else inverse_diagonal_block(b, inv);
@@ -104,9 +109,8 @@ cudaError_t launch_gather(Handle& h, cudaStream_t s) {
     if (h.nsell == 0) return cudaSuccess;
     int threads = 256;
     int64_t blocks = (h.nsell + threads - 1) / threads;
-    gather_kernel<<<(unsigned)blocks, threads, 0, s>>>(h.nsell, h.sell_cptr, h.sell_contrib, h.sell_row, h.scol,
-                                                       h.trip, h.valA, h.valB, h.valC, h.minv,
-                                                       h.precond, h.streaming);
+    gather_kernel<<<(unsigned)blocks, threads, 0, s>>>(h.nsell, h.P, h.sell_cptr, h.sell_contrib, h.trip, h.valA,
+                                                       h.valB, h.valC, h.minv, h.precond, h.streaming);
     return cudaGetLastError();
 }
 
