@@ -127,54 +127,74 @@ __global__ void tet_force_kernel(int T, const int4* __restrict__ idx, const floa
     o[3] = f4(r3);
 }
 
-// Reference kernels.py:1481-1601.  Lane g of an 8-lane group evaluates Gauss
-// point g of one hex.  F = (sum_a x_a (x) dN_a/dxi) inv_J0 and likewise dF/dt,
-// so no per-corner gradient is kept; the corner forces of the point are
-// (P inv_J0^T w) dN_a/dxi.  The 8 points' forces are summed per corner by a
-// fixed three-level reduce-scatter over the group (halves, quarters, eighths):
-// 21 shuffles, lane a ending with corner a.
-__global__ void __launch_bounds__(256, 3) hex_force_kernel(int H, const int* __restrict__ idx,
+// Walsh-Hadamard transform over the 8 lanes of a hex group: lane m ends with
+// sum_a chi_m(a) v_a, chi_m(a) = (-1)^popcount(a & m), v_a the value of lane a.
+__device__ __forceinline__ float wht8(float v, int lane8) {
+#pragma unroll
+    for (int b = 1; b < 8; b <<= 1) {
+        const float o = __shfl_xor_sync(0xffffffffu, v, b);
+        v = (lane8 & b) ? o - v : v + o;
+    }
+    return v;
+}
+
+// Reference kernels.py:1481-1601.  Lane g of an 8-lane group evaluates Gauss point g of one hex,
+// lane a holds node a.  In VTK order node a has the signs s_x = (a0 xor a1) ? +1 : -1,
+// s_y = a1 ? +1 : -1, s_z = a2 ? +1 : -1 (a0..a2 its bits), and the trilinear shape functions give
+//   dx/dxi = (c_x + eta c_xy + zeta c_xz + eta zeta c_xyz) / 8 (likewise for eta, zeta),
+// c_S = sum_a (prod_{s in S} s(a)) x_a.  Those sums are Walsh-Hadamard coefficients of the node
+// values over the lanes (c_x = -H3, c_y = -H2, c_z = -H4, c_xy = H1, c_xz = H7, c_yz = H6,
+// c_xyz = -H5), so F = (dx/dxi) inv_J0 and dF/dt come from one 3-stage butterfly and 7 broadcasts
+// per component instead of an 8-node sum per entry.  The corner forces f_a = sum_g (P inv_J0^T w)_g
+// dN_a/dxi(g) use the same identity the other way: a butterfly of the points' P inv_J0^T w gives
+// the sums over points weighted by 1, xi, eta, zeta and their products, from which lane a forms its
+// corner force.
+__global__ void __launch_bounds__(256, 4) hex_force_kernel(int H, const int* __restrict__ idx,
                                                         const float* __restrict__ invJ,
                                                         const float* __restrict__ detw,
                                                         const float* __restrict__ mat,
                                                         const float4* __restrict__ q4,
                                                         const float4* __restrict__ v4, float lo, float hi,
                                                         float4* __restrict__ out) {
-    __shared__ float s_tab[8][8][3];  // Gauss-point table (lane-varying reads serialise in constant memory)
-    if (threadIdx.x < 192) (&s_tab[0][0][0])[threadIdx.x] = (&c_dNdxi[0][0][0])[threadIdx.x];
-    __syncthreads();
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     const int h = gid >> 3, g = gid & 7;
     const bool live = h < H;
     const int64_t he = live ? h : H - 1;  // lanes past the end work on a valid hex and store nothing
     const int node = idx[8 * he + g];
-    const float3 xg = xyz(q4[node]), vg = xyz(v4[node]);
+    const float4 xg = q4[node], vg = v4[node];
     const float k_mu = mat[3 * he], k_lambda = mat[3 * he + 1], k_damp = mat[3 * he + 2];
     const float alpha = 1.0f + k_mu / k_lambda - k_mu / (4.0f * k_lambda);
     M3 iJ;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) iJ.m[k / 3][k % 3] = invJ[(8 * he + g) * 9 + k];
+    for (int k = 0; k < 9; ++k) iJ.m[k / 3][k % 3] = invJ[(8 * he + g) * 9 + k] * 0.125f;  // the 1/8, exactly
     const float w = detw[8 * he + g];
     const int base = threadIdx.x & 24;  // first lane of this 8-lane group within the warp
+    // this lane's point (and, later, node) signs and Gauss coordinates
+    const float sx = ((g ^ (g >> 1)) & 1) ? 1.0f : -1.0f, sy = (g & 2) ? 1.0f : -1.0f, sz = (g & 4) ? 1.0f : -1.0f;
+    const float gp = 0.5773502691896258f;
+    const float xi = sx * gp, eta = sy * gp, zeta = sz * gp;
+    const float ez = eta * zeta, xz = xi * zeta, xe = xi * eta;
+    // (dx/dxi) for positions and velocities: columns (d/dxi, d/deta, d/dzeta)
     M3 GX, GV;
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+    for (int f = 0; f < 2; ++f) {
+        const float4 src = f == 0 ? xg : vg;
+        const float comp[3] = {src.x, src.y, src.z};
 #pragma unroll
-        for (int j = 0; j < 3; ++j) GX.m[i][j] = GV.m[i][j] = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        const float xs[3] = {__shfl_sync(0xffffffffu, xg.x, base + a), __shfl_sync(0xffffffffu, xg.y, base + a),
-                             __shfl_sync(0xffffffffu, xg.z, base + a)};
-        const float vs[3] = {__shfl_sync(0xffffffffu, vg.x, base + a), __shfl_sync(0xffffffffu, vg.y, base + a),
-                             __shfl_sync(0xffffffffu, vg.z, base + a)};
-        const float d[3] = {s_tab[g][a][0], s_tab[g][a][1], s_tab[g][a][2]};
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                GX.m[i][k] += xs[i] * d[k];
-                GV.m[i][k] += vs[i] * d[k];
-            }
+        for (int i = 0; i < 3; ++i) {
+            const float t = wht8(comp[i], g);
+            const float h1 = __shfl_sync(0xffffffffu, t, base + 1), h2 = __shfl_sync(0xffffffffu, t, base + 2);
+            const float h3 = __shfl_sync(0xffffffffu, t, base + 3), h4 = __shfl_sync(0xffffffffu, t, base + 4);
+            const float h5 = __shfl_sync(0xffffffffu, t, base + 5), h6 = __shfl_sync(0xffffffffu, t, base + 6);
+            const float h7 = __shfl_sync(0xffffffffu, t, base + 7);
+            const float d0 = fmaf(-ez, h5, fmaf(zeta, h7, fmaf(eta, h1, -h3)));
+            const float d1 = fmaf(-xz, h5, fmaf(zeta, h6, fmaf(xi, h1, -h2)));
+            const float d2 = fmaf(-xe, h5, fmaf(eta, h6, fmaf(xi, h7, -h4)));
+            M3& G = f == 0 ? GX : GV;
+            G.m[i][0] = d0;
+            G.m[i][1] = d1;
+            G.m[i][2] = d2;
+        }
     }
     M3 F = matmul(GX, iJ);
     const M3 dFdt = matmul(GV, iJ);
@@ -190,31 +210,34 @@ __global__ void __launch_bounds__(256, 3) hex_force_kernel(int H, const int* __r
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) P.m[i][j] = ((F.m[i][j] * sdev + dFdt.m[i][j] * k_damp) + cof.m[i][j] * vol) * w;
-    const M3 PJ = matmulT(P, iJ);  // P inv_J0^T, so that the corner force is PJ dN_a/dxi
-    float3 f[8];
+    // P inv_J0^T w with the 1/8 of the shape-function derivatives (carried by the scaled inv_J0)
+    const M3 PJ = matmulT(P, iJ);
+    // node a = g: f_a[i] = s_x (W0 + s_y Se + s_z Sz + s_y s_z Sez)[i][0]
+    //                    + s_y (W0 + s_x Sx + s_z Sz + s_x s_z Sxz)[i][1]
+    //                    + s_z (W0 + s_x Sx + s_y Se + s_x s_y Sxe)[i][2],
+    // with Sx = -gp W3, Se = -gp W2, Sz = -gp W4, Sez = gp^2 W6, Sxz = gp^2 W7, Sxe = gp^2 W1 and
+    // W_m = sum_g chi_m(g) PJ_g (the butterfly below)
+    const float gp2 = gp * gp;
+    const float cy = -gp * sy, cz = -gp * sz, cx = -gp * sx;
+    const float cyz = gp2 * sy * sz, cxz = gp2 * sx * sz, cxy = gp2 * sx * sy;
+    float fa[3];
 #pragma unroll
-    for (int a = 0; a < 8; ++a) f[a] = mul(PJ, f3(s_tab[g][a][0], s_tab[g][a][1], s_tab[g][a][2]));
-    // reduce-scatter: keep the half / quarter / eighth of the corners whose index
-    // bits match this lane's, send the rest to the partner, add what it sends
-    float3 r4[4];
-    const bool hi4 = (g & 4) != 0, hi2 = (g & 2) != 0, hi1 = (g & 1) != 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float3 keep = hi4 ? f[4 + k] : f[k], send = hi4 ? f[k] : f[4 + k];
-        r4[k] = keep + f3(__shfl_xor_sync(0xffffffffu, send.x, 4), __shfl_xor_sync(0xffffffffu, send.y, 4),
-                          __shfl_xor_sync(0xffffffffu, send.z, 4));
+    for (int i = 0; i < 3; ++i) {
+        const float w0 = wht8(PJ.m[i][0], g), w1 = wht8(PJ.m[i][1], g), w2 = wht8(PJ.m[i][2], g);
+        const float a00 = __shfl_sync(0xffffffffu, w0, base), a01 = __shfl_sync(0xffffffffu, w1, base);
+        const float a02 = __shfl_sync(0xffffffffu, w2, base);
+        const float e20 = __shfl_sync(0xffffffffu, w0, base + 2), e22 = __shfl_sync(0xffffffffu, w2, base + 2);
+        const float z40 = __shfl_sync(0xffffffffu, w0, base + 4), z41 = __shfl_sync(0xffffffffu, w1, base + 4);
+        const float ez60 = __shfl_sync(0xffffffffu, w0, base + 6);
+        const float x31 = __shfl_sync(0xffffffffu, w1, base + 3), x32 = __shfl_sync(0xffffffffu, w2, base + 3);
+        const float xz71 = __shfl_sync(0xffffffffu, w1, base + 7);
+        const float xe12 = __shfl_sync(0xffffffffu, w2, base + 1);
+        const float t0 = fmaf(cyz, ez60, fmaf(cz, z40, fmaf(cy, e20, a00)));
+        const float t1 = fmaf(cxz, xz71, fmaf(cz, z41, fmaf(cx, x31, a01)));
+        const float t2 = fmaf(cxy, xe12, fmaf(cy, e22, fmaf(cx, x32, a02)));
+        fa[i] = fmaf(sz, t2, fmaf(sy, t1, sx * t0));
     }
-    float3 r2[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const float3 keep = hi2 ? r4[2 + k] : r4[k], send = hi2 ? r4[k] : r4[2 + k];
-        r2[k] = keep + f3(__shfl_xor_sync(0xffffffffu, send.x, 2), __shfl_xor_sync(0xffffffffu, send.y, 2),
-                          __shfl_xor_sync(0xffffffffu, send.z, 2));
-    }
-    const float3 keep = hi1 ? r2[1] : r2[0], send = hi1 ? r2[0] : r2[1];
-    const float3 mine = keep + f3(__shfl_xor_sync(0xffffffffu, send.x, 1), __shfl_xor_sync(0xffffffffu, send.y, 1),
-                                  __shfl_xor_sync(0xffffffffu, send.z, 1));
-    if (live) out[8 * h + g] = f4(-mine);
+    if (live) out[8 * h + g] = make_float4(-fa[0], -fa[1], -fa[2], 0.0f);
 }
 
 // Reference kernels.py:876-960: one thread per triangle writes its three

@@ -59,6 +59,27 @@ def test_elastic_forces_match_oracle(kind):
     np.testing.assert_allclose(f, want, rtol=0, atol=1e-5 * np.abs(want).max())
 
 
+def test_hex_forces_on_distorted_cells_under_non_affine_motion_match_oracle():
+    """Hex8 forces (elastic and damping) on jittered rest cells under a random non-affine deformation
+    with random velocities.  For affine motion of box-shaped cells the bilinear and trilinear parts of
+    dx/dxi vanish; here every part of the shape-function gradient contributes (kernels.py:1481-1601)."""
+    rng = np.random.default_rng(17)
+    x, hexes, mats, mass = scenes.hex_block(4, 3, 3, 0.05, (0.0, 0.0, 0.3), 2e5, 0.35, 1000.0, k_damp=0.02)
+    x = x + rng.uniform(-0.005, 0.005, x.shape)
+    model, solver, oracle = make_pair(x, mass, hexes=hexes, hex_materials=mats, min_stretch=0.05)
+    q = rounded(oracle.rest + rng.normal(0.0, 0.004, x.shape))
+    v = rounded(rng.normal(0.0, 0.1, x.shape))
+    dN = O.hex_shape_gradients(oracle.hex_inv_J0)
+    F = np.einsum("hai,hgaj->hgij", q[oracle.hexes], dN).reshape(-1, 3, 3)
+    assert not O.clamp_active(F, 0.05, 20.0).any()
+    state = model.state()
+    state.particle_q.copy_(tensor(q))
+    state.particle_qd.copy_(tensor(v))
+    f = to_np(solver.eval_hexahedral_forces(model, None, state))
+    want = oracle.forces(q, v, terms=("hex",))["hex"]
+    np.testing.assert_allclose(f, want, rtol=0, atol=1e-5 * np.abs(want).max())
+
+
 def test_tet_clamp_engages_on_inverted_element():
     """An inverted tet gives a negative smallest stretch that the clamp lifts (kernels.py:421-444)."""
     x, tets, mass, mats = one_tet()
