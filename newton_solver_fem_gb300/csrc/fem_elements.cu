@@ -61,7 +61,7 @@ __global__ void node_prepare_kernel(int P, float* __restrict__ q, float* __restr
 
 // Reference kernels.py:511-632 (force) and 484-508 (activation).  Writes the
 // restoring force of each corner into out[4 t + a].
-__global__ void tet_force_kernel(int T, const int4* __restrict__ idx, const float* __restrict__ pose,
+__global__ void __launch_bounds__(128, 8) tet_force_kernel(int T, const int4* __restrict__ idx, const float* __restrict__ pose,
                                  const float* __restrict__ mat, const float4* __restrict__ q4,
                                  const float4* __restrict__ v4, const float* __restrict__ act,
                                  const float* __restrict__ mu_scale, float lo, float hi, float4* __restrict__ out) {
@@ -304,6 +304,9 @@ struct NodeForceArgs {
 // 1273-1307 (gravity, damping), soft_surface_contacts.py (surface).  Term
 // order: spring, tet, hex, tri, particle, ground, soft contact, gravity,
 // damping, surface.
+// kFull = false compiles out the spring (and bend torque) and contact terms, for scenes that have
+// none: the remaining gather then fits in fewer registers, so more warps cover its load latency.
+template <bool kFull>
 __global__ void node_forces_kernel(NodeForceArgs a) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.P) return;
@@ -315,7 +318,7 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
     // kCornerBatch at a time (ids, then the data they index) before any is
     // added, so that many independent loads are in flight; the sums keep the
     // ascending incidence order.
-    if (a.terms & FEM_TERM_SPRING) {
+    if (kFull && (a.terms & FEM_TERM_SPRING)) {
         constexpr int kSpringBatch = 2;
         const int e1 = a.spring_ptr[i + 1];
         for (int e0 = a.spring_ptr[i]; e0 < e1; e0 += kSpringBatch) {
@@ -385,7 +388,7 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
             }
         }
     }
-    if ((a.terms & FEM_TERM_PARTICLE) && a.pforce != nullptr) fp = xyz(a.pforce[i]);
+    if (kFull && (a.terms & FEM_TERM_PARTICLE) && a.pforce != nullptr) fp = xyz(a.pforce[i]);
     bool active = (a.flags[i] & 1) != 0;
     float3 grav = f3(a.gravity[0], a.gravity[1], a.gravity[2]);
     if ((a.terms & FEM_TERM_GROUND) && a.has_ground && active) {
@@ -408,7 +411,7 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
             fg = zero - n * fn - vt * ftan;
         }
     }
-    if ((a.terms & FEM_TERM_SOFT_CONTACT) && a.sc_head != nullptr) {
+    if (kFull && (a.terms & FEM_TERM_SOFT_CONTACT) && a.sc_head != nullptr) {
         // the list holds this node's penetrating contacts in arbitrary order: add
         // them in ascending contact id (repeated minimum search, lists are short)
         int last = -1;
@@ -428,7 +431,7 @@ __global__ void node_forces_kernel(NodeForceArgs a) {
     if ((a.terms & FEM_TERM_DAMPING) && active && a.linear_damping > 0.0f) {
         fd = vi * (-a.linear_damping * a.mass[i]);
     }
-    if ((a.terms & FEM_TERM_SURFACE) && a.sforce != nullptr) fsf = xyz(a.sforce[i]);
+    if (kFull && (a.terms & FEM_TERM_SURFACE) && a.sforce != nullptr) fsf = xyz(a.sforce[i]);
     float3 f;
     if (a.scale_by_dt) {
         float h = a.dt;
@@ -985,7 +988,10 @@ cudaError_t launch_node_forces(Handle& h, const float* ext, const float* gravity
     a.terms = terms;
     a.scale_by_dt = scale_by_dt ? 1 : 0;
     a.out = out;
-    node_forces_kernel<<<blocks_for(h.P, 128), 128, 0, s>>>(a);
+    const bool full = (h.S > 0 && (terms & FEM_TERM_SPRING)) || a.pforce != nullptr || a.sc_head != nullptr ||
+                      a.sforce != nullptr;
+    if (full) node_forces_kernel<true><<<blocks_for(h.P, 128), 128, 0, s>>>(a);
+    else node_forces_kernel<false><<<blocks_for(h.P, 128), 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 
