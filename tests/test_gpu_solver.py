@@ -576,7 +576,7 @@ def test_full_size_jittered_tet_block_with_springs_and_ground():
             a, b = b, a
     A = solver.A_bsr
     P = model.particle_count
-    assert A.columns.numel() == 1_707_697  # nnzb of the survey's size table
+    assert A.columns.numel() == 1_707_697  # stored 3x3 blocks of the jittered Tet4 48^3 block with its edge springs
     M = sp.bsr_matrix((A.values.cpu().numpy().astype(np.float64), A.columns.cpu().numpy(),
                        A.offsets.cpu().numpy()), shape=(3 * P, 3 * P))
     rhs = to_np(b.particle_f).ravel()
