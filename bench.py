@@ -746,9 +746,9 @@ def run_gb300(args) -> None:
     peak, peak_kind = peaks()
     traffic = dram_traffic_per_launch(iters) if args.cells == 64 else None
 
-    op_tuned = autotune.tune_operator(solver)  # standalone SpMV: block columns in flight per thread
+    op_tuned = autotune.tune_operator(solver)  # standalone SpMV: loads in flight, or bulk-copy staging
     spmv = standalone_spmv(solver, lib, P, info["nnzb"], peak)
-    spmv["operator_batch"] = op_tuned
+    spmv["operator_tuning"] = op_tuned
 
     # ---- end to end through the public API with host buffers, driven the way the reference's own
     # example drives its solver (examples/example_linear_fem.py:107-128): per frame an eager tangent
@@ -877,7 +877,12 @@ def standalone_spmv(solver, lib, P: int, nnzb: int, peak: float) -> dict:
     us = 1e3 * statistics.median(times[1:])
     col = 4 if cc.value == 0 else 2  # the operator reads 16-bit offsets whenever the handle has them
     gbs = spmv_bytes(nnzb, P, col) / (us / 1e6) / 1e9
-    return {"kernel": "apply_operator_kernel (fem_apply_operator)", "us": us, "achieved": gbs, "peak": peak,
+    stage, batch = ctypes.c_int64(), ctypes.c_int64()
+    _lib.check(lib.fem_get_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_STAGE, ctypes.byref(stage)))
+    _lib.check(lib.fem_get_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_BATCH, ctypes.byref(batch)))
+    kernel = (f"apply_operator_staged_kernel<{stage.value}> (fem_apply_operator, bulk-copy staging)"
+              if stage.value and col == 2 else f"apply_operator_kernel<{batch.value}> (fem_apply_operator)")
+    return {"kernel": kernel, "us": us, "achieved": gbs, "peak": peak,
             "unit": "GB/s", "frac": gbs / peak, "column_index_bytes": col}
 
 

@@ -207,6 +207,13 @@ int fem_set_wait_limit(FemHandle* handle, int64_t nanoseconds);
 #define FEM_TUNE_OPERATOR_BATCH 15   /* fem_apply_operator: block columns loaded before any is used, per thread: 2 at
                                         32 registers (8 CTAs of 256 threads per SM, the default: a 64^3 Hex8 matrix in
                                         one wave, 51 us) or 4 at 48 registers (5 CTAs per SM: 1.4 waves, 63 us) */
+#define FEM_TUNE_OPERATOR_STAGE 16   /* fem_apply_operator: 4 (default) or 8 stages the block planes through shared
+                                        memory with bulk asynchronous copies (cp.async.bulk), that many block columns
+                                        of a slice per copy, double-buffered per warp (64^3 Hex8: 49 us with 4, 74 us
+                                        with 8); 0 loads them directly (FEM_TUNE_OPERATOR_BATCH applies).  Staging
+                                        needs the 16-bit column offsets (FEM_TUNE_COMPACT_COLUMNS not 0); otherwise
+                                        the direct loads run.  A copy that does not complete within the wait limit
+                                        sets the timeout status that fem_get_stats reports. */
 int fem_set_tuning(FemHandle* handle, int32_t key, int64_t value);
 int fem_get_tuning(FemHandle* handle, int32_t key, int64_t* value);
 int fem_set_maxiter(FemHandle* handle, int32_t maxiter);

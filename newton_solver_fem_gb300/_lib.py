@@ -37,6 +37,7 @@ FEM_TUNE_COMPACT_COLUMNS = 12
 FEM_TUNE_UNIFORM_COLUMN_BLOCKS = 13
 FEM_TUNE_CG_VARIANT = 14
 FEM_TUNE_OPERATOR_BATCH = 15
+FEM_TUNE_OPERATOR_STAGE = 16
 
 FEM_TERM_SPRING = 1
 FEM_TERM_TET = 2

@@ -25,9 +25,12 @@ by microseconds per CG iteration, so that candidates with different iteration
 counts compare fairly, and applies the best one.  Results are cached in a JSON
 file keyed by GPU name and problem signature (nodes, stored blocks, scenes).
 
-The standalone SpMV (``fem_apply_operator``) has its own axis,
+The standalone SpMV (``fem_apply_operator``) has its own axes:
 ``FEM_TUNE_OPERATOR_BATCH`` (block columns in flight per thread: 2 at 32
-registers or 4 at 48); ``tune_operator`` times both after an L2 flush.
+registers or 4 at 48) and ``FEM_TUNE_OPERATOR_STAGE`` (0: direct loads; 4 or 8:
+the block planes staged through shared memory by bulk asynchronous copies of
+that many block columns); ``tune_operator`` times each candidate after an L2
+flush.
 
 Command line (prints one JSON record per candidate, then the choice)::
 
@@ -163,16 +166,29 @@ def time_operator(solver, repeats: int = 21) -> float:
     return 1e3 * statistics.median(times[1:])
 
 
-def tune_operator(solver, batches=(2, 4), timer=None) -> dict:
-    """Pick and apply the fastest FEM_TUNE_OPERATOR_BATCH; returns {"operator_batch", "us", "candidates"}."""
+OPERATOR_AXES = {"operator_batch": _lib.FEM_TUNE_OPERATOR_BATCH, "operator_stage": _lib.FEM_TUNE_OPERATOR_STAGE}
+# direct loads with 2 or 4 block columns in flight, and the planes staged through shared memory by bulk
+# copies of 4 or 8 block columns
+OPERATOR_CANDIDATES = [dict(operator_batch=2, operator_stage=0), dict(operator_batch=4, operator_stage=0),
+                       dict(operator_batch=2, operator_stage=4), dict(operator_batch=2, operator_stage=8)]
+
+
+def tune_operator(solver, candidates=None, timer=None) -> dict:
+    """Pick and apply the fastest fem_apply_operator variant (FEM_TUNE_OPERATOR_BATCH and
+    FEM_TUNE_OPERATOR_STAGE); returns the chosen keys with "us", and every candidate's record."""
     lib = _lib.load()
     timer = timer or time_operator
+
+    def set_keys(choice):
+        for name, key in OPERATOR_AXES.items():
+            _lib.check(lib.fem_set_tuning(solver._handle, key, int(choice[name])))
+
     records = []
-    for b in batches:
-        _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_BATCH, int(b)))
-        records.append({"operator_batch": int(b), "us": timer(solver)})
+    for cand in candidates or OPERATOR_CANDIDATES:
+        set_keys(cand)
+        records.append({**{k: int(v) for k, v in cand.items()}, "us": timer(solver)})
     best = min(records, key=lambda r: r["us"])
-    _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_BATCH, best["operator_batch"]))
+    set_keys(best)
     return {**best, "candidates": records}
 
 

@@ -1105,6 +1105,7 @@ int fem_prepare_tet_updates(FemHandle* H, const FemDesc* d, int32_t original_nod
     n.resident_pref = h.resident_pref;
     n.cg_variant = h.cg_variant;
     n.operator_batch = h.operator_batch;
+    n.operator_stage = h.operator_stage;
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
     if (code == FEM_OK) code = configure_launch(n);
@@ -1189,6 +1190,7 @@ int fem_refresh_topology(FemHandle* H, const FemDesc* d, float* q, float dt, voi
     n.resident_pref = h.resident_pref;
     n.cg_variant = h.cg_variant;
     n.operator_batch = h.operator_batch;
+    n.operator_stage = h.operator_stage;
     n.cta_speed = h.cta_speed;  // speeds belong to CTA indices, so they carry over to the new split
     code = register_soft_contacts(n, h.sc_count, h.sc_particle, h.sc_pos, h.sc_vel, h.sc_normal, h.sc_cap);
     if (code == FEM_OK) code = configure_launch(n);
@@ -1294,6 +1296,10 @@ int fem_set_tuning(FemHandle* H, int32_t key, int64_t value) {
         if (value != 2 && value != 4) return set_error(FEM_ERR_BAD_ARG, "operator batch must be 2 or 4");
         h.operator_batch = (int)value;
         return FEM_OK;  // fem_apply_operator only: no PCG launch tables to rebuild
+    } else if (key == FEM_TUNE_OPERATOR_STAGE) {
+        if (value != 0 && value != 4 && value != 8) return set_error(FEM_ERR_BAD_ARG, "operator stage must be 0, 4 or 8");
+        h.operator_stage = (int)value;
+        return FEM_OK;
     } else if (key == FEM_TUNE_CG_VARIANT) {
         if (value != 0 && value != 1) return set_error(FEM_ERR_BAD_ARG, "CG variant must be 0 or 1");
         h.cg_variant = (int)value;
@@ -1340,6 +1346,7 @@ int fem_get_tuning(FemHandle* H, int32_t key, int64_t* value) {
         case FEM_TUNE_UNIFORM_COLUMN_BLOCKS: *value = column_mode(h) == 2 ? h.uniform_blocks : 0; return FEM_OK;
         case FEM_TUNE_CG_VARIANT: *value = h.cg_variant; return FEM_OK;
         case FEM_TUNE_OPERATOR_BATCH: *value = h.operator_batch; return FEM_OK;
+        case FEM_TUNE_OPERATOR_STAGE: *value = h.operator_stage; return FEM_OK;
         default: return set_error(FEM_ERR_BAD_ARG, "unknown tuning key");
     }
 }

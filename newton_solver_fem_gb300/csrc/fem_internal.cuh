@@ -143,6 +143,7 @@ struct Handle {
     int resident_pref = -1;          // resident row-state layout: -1 automatic, 0 none, 1 x/r/z, 2 x/r/z + inverse
     int cg_variant = 0;              // FEM_TUNE_CG_VARIANT: 0 standard CG, 1 single-reduction (Chronopoulos-Gear)
     int operator_batch = 2;          // FEM_TUNE_OPERATOR_BATCH: block columns in flight per thread in fem_apply_operator
+    int operator_stage = 4;          // FEM_TUNE_OPERATOR_STAGE: 0 direct loads, else block columns per bulk copy
     std::vector<double> cta_speed;   // calibrated SpMV speed per CTA index (cost units per ns)
     std::vector<int64_t> host_slice_cost;  // stored blocks + 4 per live row, per slice
     std::vector<int> host_cta_slice0;      // the partition in use: CTA c owns host_cta_list[cta_slice0[c] ..)

@@ -173,6 +173,149 @@ __global__ void __launch_bounds__(256, kOperatorBatch == 2 ? 8 : 5) apply_operat
     st3(y, row, acc);
 }
 
+// The same product with the block planes staged through shared memory by bulk asynchronous copies
+// (cp.async.bulk, completing on an mbarrier): lane 0 of each warp copies kCols block columns of its
+// slice (values and 16-bit column offsets: 38 B per block, contiguous per plane in the SELL layout)
+// into one half of the warp's double buffer while the warp computes from the other half.  Waits
+// are bounded by limit_ns; on a timeout the kernel sets the timeout status, waits (again bounded)
+// for the copies it issued and returns.  Same arithmetic in the same order as the direct kernel.
+constexpr int kStageWarps = 4;
+template <int kCols>
+struct StageLayout {
+    static constexpr int a = 0, b = kCols * kSlice * 16, c = 2 * kCols * kSlice * 16, d = c + kCols * kSlice * 4;
+    static constexpr int bytes = d + kCols * kSlice * 2;  // per buffer
+    static constexpr int total = kStageWarps * 2 * bytes + kStageWarps * 2 * 8;  // buffers, then mbarriers
+    static_assert(b % 16 == 0 && c % 16 == 0 && d % 16 == 0 && bytes % 16 == 0, "16-byte bulk copy targets");
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait of a whole warp for phase `parity` of `bar`: every lane observes the phase (so the
+// copied bytes are visible to it), and the timeout decision is the same in every lane (lane 0's
+// clock).  False after limit_ns.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, long long limit_ns) {
+    bool done = mbar_try_wait(bar, parity);
+    if (__all_sync(0xffffffffu, done)) return true;
+    const unsigned long long t0 = __shfl_sync(0xffffffffu, global_ns(), 0);
+    for (;;) {
+        if (!done) done = mbar_try_wait(bar, parity);
+        if (__all_sync(0xffffffffu, done)) return true;
+        const unsigned long long t = __shfl_sync(0xffffffffu, global_ns(), 0);
+        if ((long long)(t - t0) >= limit_ns) return false;
+    }
+}
+// Bounded wait of one thread (the timeout path's drain of copies still in flight).
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity, long long limit_ns) {
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try_wait(bar, parity) && (long long)(global_ns() - t0) < limit_ns) {
+    }
+}
+
+template <int kCols>
+__global__ void __launch_bounds__(kStageWarps * 32) apply_operator_staged_kernel(
+    int nslices, const int* __restrict__ slice_ptr, const int2* __restrict__ meta,
+    const unsigned* __restrict__ row_info, const float4* __restrict__ valA, const float4* __restrict__ valB,
+    const float* __restrict__ valC, const short* __restrict__ dcol, const unsigned* __restrict__ fixcol,
+    const float* __restrict__ x, float* __restrict__ y, int* __restrict__ status, long long limit_ns) {
+    using L = StageLayout<kCols>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sl = blockIdx.x * kStageWarps + w;
+    if (sl >= nslices) return;  // the whole warp: nothing below synchronises across warps
+    unsigned char* buf = smem + (size_t)w * 2 * L::bytes;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + (size_t)kStageWarps * 2 * L::bytes) + 2 * w;
+    const int base = slice_ptr[sl], len_slice = slice_ptr[sl + 1] - base;
+    const int nchunks = (len_slice + kCols - 1) / kCols;
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar + 1)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    auto issue = [&](int c) {  // lane 0: chunk c into buffer c & 1
+        const int k0 = c * kCols, nk = min(kCols, len_slice - k0);
+        const size_t e0 = (size_t)(base + k0) * kSlice;
+        unsigned char* dst = buf + (size_t)(c & 1) * L::bytes;
+        uint64_t* b = bar + (c & 1);
+        const uint32_t tx = (uint32_t)nk * kSlice * (16 + 16 + 4 + 2);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of this buffer first
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(tx)
+                     : "memory");
+        bulk_g2s(dst + L::a, valA + e0, (uint32_t)nk * kSlice * 16, b);
+        bulk_g2s(dst + L::b, valB + e0, (uint32_t)nk * kSlice * 16, b);
+        bulk_g2s(dst + L::c, valC + e0, (uint32_t)nk * kSlice * 4, b);
+        bulk_g2s(dst + L::d, dcol + e0, (uint32_t)nk * kSlice * 2, b);
+    };
+    if (lane == 0) {
+        issue(0);
+        if (nchunks > 1) issue(1);
+    }
+    const int2 m = meta[sl];
+    const int row = m.x + lane;
+    const bool valid = lane < m.y;
+    const unsigned info = valid ? row_info[row] : 0u;
+    const bool fixed = valid && (info & kFixedBit) != 0;
+    const int len = valid ? (int)(info & ~kFixedBit) : 0;
+    float3 acc = f3(0.f, 0.f, 0.f);
+    int failed = -1;  // the chunk whose wait ran out (chunks failed and failed + 1 may be in flight)
+    for (int c = 0; c < nchunks; ++c) {
+        if (!mbar_wait_warp(bar + (c & 1), (uint32_t)((c >> 1) & 1), limit_ns)) {
+            failed = c;
+            break;
+        }
+        const unsigned char* src = buf + (size_t)(c & 1) * L::bytes;
+        const float4* sA = reinterpret_cast<const float4*>(src + L::a);
+        const float4* sB = reinterpret_cast<const float4*>(src + L::b);
+        const float* sC = reinterpret_cast<const float*>(src + L::c);
+        const short* sD = reinterpret_cast<const short*>(src + L::d);
+        const int k0 = c * kCols, nk = min(kCols, len_slice - k0);
+#pragma unroll
+        for (int kk = 0; kk < kCols; ++kk) {
+            const int k = k0 + kk;
+            if (kk < nk && !fixed && k < len) {
+                const int i = kk * kSlice + lane;
+                const bool use = fixcol == nullptr || ((__ldg(fixcol + base + k) >> lane) & 1u) == 0u;
+                const float3 xj = ld3(x, row + (int)sD[i]);
+                if (use) acc = acc + block_mul(sA[i], sB[i], sC[i], xj);
+            }
+        }
+        __syncwarp();  // every lane is done with this buffer before it is refilled
+        if (lane == 0 && c + 2 < nchunks) issue(c + 2);
+    }
+    if (failed >= 0) {  // warp-uniform
+        if (lane == 0) {
+            atomicOr(status, kStatusTimeout);
+            // the copies of chunks failed and failed + 1 were issued and may still be landing
+            for (int c = failed; c < nchunks && c <= failed + 1; ++c)
+                mbar_drain(bar + (c & 1), (uint32_t)((c >> 1) & 1), limit_ns);
+        }
+        __syncwarp();
+        return;
+    }
+    if (!valid) return;
+    if (fixed) {
+        st3(y, row, ld3(x, row));
+        return;
+    }
+    st3(y, row, acc);
+}
+
 __global__ void apply_preconditioner_kernel(int P, const float* __restrict__ minv, const float* __restrict__ r,
                                             float* __restrict__ z) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -286,6 +429,27 @@ int fem_apply_operator(FemHandle* H, const float* x, float* y, void* stream) {
     Handle& h = H->h;
     if (h.P == 0 || h.nslices == 0) return FEM_OK;
     fem::Guard g(H->device);
+    if (h.operator_stage != 0 && h.dcol != nullptr) {
+        const int grid = (h.nslices + fem::kStageWarps - 1) / fem::kStageWarps;
+        cudaError_t err;
+        if (h.operator_stage == 4) {
+            using L = fem::StageLayout<4>;
+            err = fem::allow_dynamic_smem((const void*)fem::apply_operator_staged_kernel<4>, L::total);
+            if (err == cudaSuccess)
+                fem::apply_operator_staged_kernel<4><<<grid, fem::kStageWarps * 32, L::total, (cudaStream_t)stream>>>(
+                    h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.dcol, h.fixcol, x, y,
+                    h.status, h.wait_limit_ns);
+        } else {
+            using L = fem::StageLayout<8>;
+            err = fem::allow_dynamic_smem((const void*)fem::apply_operator_staged_kernel<8>, L::total);
+            if (err == cudaSuccess)
+                fem::apply_operator_staged_kernel<8><<<grid, fem::kStageWarps * 32, L::total, (cudaStream_t)stream>>>(
+                    h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.dcol, h.fixcol, x, y,
+                    h.status, h.wait_limit_ns);
+        }
+        if (err != cudaSuccess) return fem::report_cuda(err);
+        return fem::report_cuda(cudaGetLastError());
+    }
     auto kern = h.operator_batch == 2 ? fem::apply_operator_kernel<2> : fem::apply_operator_kernel<4>;
     kern<<<fem::blocks((int64_t)h.nslices * 32, 256), 256, 0, (cudaStream_t)stream>>>(
         h.nslices, h.slice_ptr, h.slice_meta, h.row_info, h.valA, h.valB, h.valC, h.scol, h.dcol, h.fixcol, x, y);

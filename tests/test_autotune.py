@@ -62,12 +62,12 @@ def test_default_candidates_cover_every_axis():
                                            _lib.FEM_TUNE_CG_VARIANT}
 
 
-def test_operator_batch_search_picks_the_faster(monkeypatch):
-    calls = []
+def test_operator_search_covers_batch_and_bulk_staging_and_applies_the_faster(monkeypatch):
+    state = {}
 
     class Lib:
         def fem_set_tuning(self, handle, key, value):
-            calls.append((key, value))
+            state[key] = value
             return 0
 
     monkeypatch.setattr(_lib, "load", lambda: Lib())
@@ -75,7 +75,9 @@ def test_operator_batch_search_picks_the_faster(monkeypatch):
     class S:
         _handle = None
 
-    times = {2: 51.0, 4: 63.0}
-    out = autotune.tune_operator(S(), timer=lambda solver: times[calls[-1][1]])
-    assert out["operator_batch"] == 2 and calls[-1] == (_lib.FEM_TUNE_OPERATOR_BATCH, 2)
-    assert [r["operator_batch"] for r in out["candidates"]] == [2, 4]
+    times = {(2, 0): 51.0, (4, 0): 63.0, (2, 4): 49.0, (2, 8): 55.0}
+    timer = lambda solver: times[(state[_lib.FEM_TUNE_OPERATOR_BATCH], state[_lib.FEM_TUNE_OPERATOR_STAGE])]
+    out = autotune.tune_operator(S(), timer=timer)
+    assert (out["operator_batch"], out["operator_stage"]) == (2, 4)
+    assert (state[_lib.FEM_TUNE_OPERATOR_BATCH], state[_lib.FEM_TUNE_OPERATOR_STAGE]) == (2, 4)
+    assert {(r["operator_batch"], r["operator_stage"]) for r in out["candidates"]} == set(times)

@@ -201,3 +201,39 @@ def test_prepared_sequence_replays_in_a_cuda_graph():
         trial()
         torch.cuda.synchronize()
         np.testing.assert_array_equal(q_graph, to_np(result.particle_q))
+
+
+@pytest.mark.parametrize("stage", [4, 8])
+def test_bulk_staged_operator_equals_direct_loads(stage):
+    """fem_apply_operator with the block planes staged through shared memory by bulk asynchronous
+    copies (FEM_TUNE_OPERATOR_STAGE) gives the direct kernel's result bit for bit (same products in the
+    same order): mixed elements with fixed supports, slices whose length is not a multiple of the
+    chunk, and the 64-row tail of a Hex8 block."""
+    import ctypes
+
+    from newton_solver_fem_gb300 import _lib, scenes
+
+    lib = _lib.load()
+    cases = [mixed_model(seed=7)]
+    sc = scenes.hex_block_64(n=9)  # 1,000 nodes: a last slice of 8 rows
+    from gpu_helpers import scene_pair
+
+    hex_model, _, _ = scene_pair(sc, with_oracle=False)
+    cases.append((hex_model, None, np.random.default_rng(8)))
+    for model, fixed, rng in cases:
+        solver = solver_for(model, fixed)
+        solver.refresh_tangent(perturbed_state(model, rng).particle_q)
+        P = model.particle_count
+        x = tensor(rng.normal(size=(P, 3)))
+        direct, staged = torch.empty_like(x), torch.empty_like(x)
+        stream = torch.cuda.current_stream().cuda_stream
+        _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_STAGE, 0))
+        _lib.check(lib.fem_apply_operator(solver._handle, x.data_ptr(), direct.data_ptr(), stream))
+        _lib.check(lib.fem_set_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_STAGE, stage))
+        v = ctypes.c_int64()
+        _lib.check(lib.fem_get_tuning(solver._handle, _lib.FEM_TUNE_OPERATOR_STAGE, ctypes.byref(v)))
+        assert v.value == stage
+        _lib.check(lib.fem_apply_operator(solver._handle, x.data_ptr(), staged.data_ptr(), stream))
+        torch.cuda.synchronize()
+        assert solver.stats()["status"] == 0
+        assert torch.equal(direct, staged)
