@@ -603,7 +603,9 @@ __global__ void __launch_bounds__(kTetTangentThreads) tet_tangent_kernel(
 // so with r = h (sqrt|c1| gN_a, sqrt|c2| F gN_a, sqrt|c3| cof F gN_a) the block is
 //   K_ab = sum_g [(r1_a . r1_b) I + r2_a r2_b^T + r3_a r3_b^T]   (signs of c applied when negative).
 // A CTA takes kTanHex hexes:
-//   phase 0  the hexes' node positions and the Gauss table are staged in shared memory;
+//   phase 0  the hexes' node positions and the Gauss table are staged in shared memory, and the
+//            phase-1 threads load their point's inverse Jacobian, weight and materials, so every
+//            global load of the CTA is in flight before the first barrier;
 //   phase 1  one thread per (hex, point) forms gN_a, F, the clamp, cof F and the eight 9-float
 //            records r of its point (no work repeated across lanes);
 //   phase 2  one thread per 2x2 tile of blocks on or above the block diagonal (10 tiles per
