@@ -1065,12 +1065,6 @@ PcgKernel pcg_kernel_for(int unroll, int cm, int variant) {
 }
 
 
-// Grid size, slices per CTA and staging place for the handle's kernel variant
-// and CTA size: as many CTAs as stay co-resident (the cooperative limit, and
-// the optional cap), but no more than one per warp-count of slices.  The grid
-// only shrinks from pass to pass (a smaller grid means more slices per CTA and
-// possibly more shared memory), and the loop ends with a configuration whose
-// occupancy covers the grid.
 cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes) {
     if (bytes <= 48 * 1024) return cudaSuccess;
     static std::mutex mu;
@@ -1086,6 +1080,12 @@ cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes) {
     return e;
 }
 
+// Grid size, slices per CTA and staging place for the handle's kernel variant
+// and CTA size: as many CTAs as stay co-resident (the cooperative limit, and
+// the optional cap), but no more than one per warp-count of slices.  The grid
+// only shrinks from pass to pass (a smaller grid means more slices per CTA and
+// possibly more shared memory), and the loop ends with a configuration whose
+// occupancy covers the grid.
 cudaError_t pcg_configure(Handle& h) {
     int dev = 0;
     cudaError_t err = cudaGetDevice(&dev);
